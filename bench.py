@@ -1,0 +1,365 @@
+"""Benchmark of the curvedSpaceSim per-timestep hot path on GB300.
+
+Workload (default): the plain exact GPU path with submeshing -
+torus R=3, r=1 from a 200x100 grid with alternating diagonals (20,000 vertices / 40,000 faces), N=2,000 particles at
+area-weighted random positions (seed 2), harmonic repulsion sigma = range = cutoff = 0.3 (k = 1/sigma^2),
+Nose-Hoover NVT at T=0.05, dt=0.002, reference patches.  One step = one noseHooverNVT::performUpdate: two geodesic
+walks with velocity transport, one neighbour + exact-geodesic + force pass, the chain updates.
+
+Metric: particle-steps/s (N x steps / time).
+  value : inputs resident in HBM; K steps, each one CUDA-graph replay, timed with CUDA events on the launching
+          stream; L2 flushed (a 512 MB write) before every timed step.
+  e2e   : the same steps through the C ABI with host buffers: per step the state (face, barycentrics, velocities,
+          forces) is copied from pinned host memory to the device, stepped, and copied back; wall clock.
+The reference arm (--impl reference) times the CPU oracle (the C++ restatement of the reference path; the CGAL-based
+reference itself cannot be built here) with all host threads on the same workload.
+Multi-GPU: one process per GPU, each an independent replica of the system (weak scaling, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from curvedspacesim_gb300 import meshes as ms  # noqa: E402
+
+# algorithmic work constants of the geodesic+force kernel ("Roofline accounting")
+FLOPS_PER_WINDOW = 250          # FP64 flops of one window step (trim, target/vertex updates, two children)
+BYTES_PER_SOURCE = 4 + 24 + 24 + 24   # read face, barycentrics, R3 position; write force
+BYTES_PER_CANDIDATE = 4 + 4 + 24 + 24  # read index, face, barycentrics, R3 position
+BYTES_PER_FACE = 12 + 12 + 72         # patch face: vertex ids, neighbours, edge frames
+
+
+def workload_config(name):
+    if name == "torus_nvt":
+        return dict(workload="torus200x100_N2000_nvt_patch", mesh=("torus", 200, 100), n=2000, sigma=0.3,
+                    integrator="nvt", submesh=True, range_=0.3, dt=0.002, T=0.05, seed=2)
+    if name == "ico_nve":
+        return dict(workload="icosphere4_N100_nve_alltoall", mesh=("ico", 4), n=100, sigma=0.2, integrator="nve",
+                    submesh=False, range_=0.0, dt=0.005, T=0.1, seed=1)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def build_inputs(cfg):
+    if cfg["mesh"][0] == "torus":
+        V, F = ms.torus(cfg["mesh"][1], cfg["mesh"][2], 3.0, 1.0)
+    else:
+        V, F = ms.icosphere(cfg["mesh"][1])
+    rng = np.random.default_rng(cfg["seed"])
+    f, b = ms.area_weighted_positions(V, F, cfg["n"], rng)
+    vel = ms.tangent_velocities(V, F, f, cfg["T"], rng)
+    return V, F, f, b, vel
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, max clock, throttle reasons)."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, val in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"],
+                                 p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, cfg):
+    """CPU oracle (restatement of the reference path) with all host threads, same workload."""
+    world, rank, _, pg = dist_setup()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    V, F, f, b, vel = build_inputs(cfg)
+    OM = oracle.OracleMesh(V, F)
+    sigma = cfg["sigma"]
+    prm = OM.params(0, k=1.0 / sigma ** 2, sigma=sigma, rng=cfg["range_"], submesh=int(cfg["submesh"]),
+                    max_dist=sigma, cutoff=sigma, dt=cfg["dt"], T=cfg["T"])
+    kind = 0 if cfg["integrator"] == "nve" else 1
+    threads = os.cpu_count() or 1
+    force = np.zeros((cfg["n"], 3))
+    chain = OM.nvt_chain(cfg["n"], prm)
+    state = (f, b, vel, force, chain)
+    for _ in range(args.warmup):
+        f2, b2, v2, fo2, ch2, err, _ = OM.simulate(kind, 1, *state[:4], prm, chain=state[4], threads=threads)
+        state = (f2, b2, v2, fo2, ch2)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        f2, b2, v2, fo2, ch2, err, _ = OM.simulate(kind, 1, *state[:4], prm, chain=state[4], threads=threads)
+        state = (f2, b2, v2, fo2, ch2)
+    dt_s = time.perf_counter() - t0
+    value = cfg["n"] * args.steps / dt_s
+    line = {
+        "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": cfg["workload"], "n": cfg["n"], "sigma": sigma, "integrator": cfg["integrator"],
+                   "submesh": cfg["submesh"], "l2": "cpu run"},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full steps of the workload (oracle restatement; CGAL reference "
+                                   f"not buildable)"},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(cfg, seconds_budget=15.0):
+    """Bounded sample of the same workload on the host: the oracle, single-threaded and all threads."""
+    import oracle
+    oracle.build()
+    V, F, f, b, vel = build_inputs(cfg)
+    OM = oracle.OracleMesh(V, F)
+    sigma = cfg["sigma"]
+    prm = OM.params(0, k=1.0 / sigma ** 2, sigma=sigma, rng=cfg["range_"], submesh=int(cfg["submesh"]),
+                    max_dist=sigma, cutoff=sigma, dt=cfg["dt"], T=cfg["T"])
+    kind = 0 if cfg["integrator"] == "nve" else 1
+    threads = os.cpu_count() or 1
+    res = {}
+    for th in (threads, 1):
+        steps = 0
+        t0 = time.perf_counter()
+        state = (f, b, vel, np.zeros((cfg["n"], 3)), OM.nvt_chain(cfg["n"], prm))
+        while True:
+            out = OM.simulate(kind, 1, *state[:4], prm, chain=state[4], threads=th)
+            state = out[:5]
+            steps += 1
+            el = time.perf_counter() - t0
+            if el > seconds_budget / 2 or steps >= 200:
+                break
+        res[th] = (cfg["n"] * steps / el, steps)
+    v, steps = res[threads]
+    return {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} steps of the workload on {threads} threads (oracle restatement; CGAL reference not "
+                      f"buildable); single thread: {res[1][0]:.1f} particle-steps/s over {res[1][1]} steps"}
+
+
+def run_ours(args, cfg):
+    import torch
+    world, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    from curvedspacesim_gb300 import api
+
+    V, F, f, b, vel = build_inputs(cfg)
+    n = cfg["n"]
+    sigma = cfg["sigma"]
+    ctx = api.Context(local)
+    M = api.Mesh(V, F, device=local)
+    p = api.make_params(cfg["integrator"], "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=cfg["range_"],
+                        submesh=cfg["submesh"], max_dist=sigma, cutoff=sigma, dt=cfg["dt"], temperature=cfg["T"])
+    S = api.System(ctx, M, n, p)
+    S.set_state(f, b, vel, np.zeros((n, 3)))
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    # warm-up (also captures the graph)
+    S.step(max(args.warmup, 1), graph=True)
+    torch.cuda.synchronize()
+    bits, cnt = S.check()
+    if bits:
+        raise RuntimeError(f"per-item errors during warm-up: {bits:#x} {cnt}")
+
+    # ---- value: resident inputs, one graph replay per step, L2 flushed before each step ----
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    barrier(pg)
+    torch.cuda.synchronize()
+    sampler.start()
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record(stream)
+        S.step(1, graph=True)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    barrier(pg)
+    ms_steps = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t_ms = sum(ms_steps)
+    t_ms = max_over_ranks(pg, t_ms)
+    bits, cnt = S.check()
+    if bits:
+        raise RuntimeError(f"per-item errors in the timed region: {bits:#x} {cnt}")
+    value = world * n * args.steps / (t_ms * 1e-3)
+    kps = S.kernels_per_step()
+
+    # ---- kernel times (events around the geodesic and walk kernels, no graph) ----
+    S.timing(True)
+    S.step(args.steps, graph=False)
+    torch.cuda.synchronize()
+    kt = S.last_times()
+    S.timing(False)
+    bits, cnt2 = S.check()
+    geo_ms = kt["geodesic_ms"] / args.steps
+    walk_ms = kt["walk_ms"] / args.steps
+
+    # algorithmic work of the geodesic kernel per launch (counters of the timed-kernel pass)
+    windows = cnt2["windows"] / args.steps
+    S.enable_pairs()
+    S.compute_forces()
+    _, pj, _, _ = S.pairs()
+    cands = len(pj)
+    faces_per_source = float(os.environ.get("CSSG_FACES_PER_SOURCE", "0")) or (
+        math.pi * sigma ** 2 / (M.area / M.nF) * 1.5)
+    geo_bytes = n * BYTES_PER_SOURCE + cands * BYTES_PER_CANDIDATE + n * faces_per_source * BYTES_PER_FACE
+    geo_flops = windows * FLOPS_PER_WINDOW
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    fp64_peak = api.fp64_peak_gflops(ctx)
+    achieved_gbs = geo_bytes / (geo_ms * 1e-3) / 1e9
+    achieved_fp64 = geo_flops / (geo_ms * 1e-3) / 1e9
+    traffic = os.environ.get("CSSG_GEO_TRAFFIC_BYTES")
+
+    # ---- e2e: host state in, step, host state out, every step ----
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    hf, hb, hv, hfo = pin((n,), torch.int32), pin((n, 3), torch.float64), pin((n, 3), torch.float64), \
+        pin((n, 3), torch.float64)
+    hf[:], hb[:], hv[:], hfo[:] = S.get_state()
+    barrier(pg)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        S.set_state(hf, hb, hv, hfo)
+        S.step(1, graph=True)
+        a, bb, c, d = S.get_state()
+        hf[:], hb[:], hv[:], hfo[:] = a, bb, c, d
+    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(pg, e2e_s)
+    e2e = world * n * args.steps / e2e_s
+    io_bytes = n * (4 + 24 + 24 + 24)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(cfg)
+
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": cfg["workload"], "n": n, "sigma": sigma, "integrator": cfg["integrator"],
+                       "submesh": cfg["submesh"], "graph": True,
+                       "l2": "flushed before every timed step (512 MB write)", "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": io_bytes,
+                    "d2h_bytes_per_step": io_bytes},
+            "gpu_launches": kps * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved_gbs / hbm_peak, "traffic": int(traffic) if traffic else None,
+                         "kernel": "geodesic_kernel", "kernel_ms": geo_ms,
+                         "algorithmic_bytes_per_launch": geo_bytes,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
+                         "fp64": {"achieved_gflops": achieved_fp64, "peak_gflops": fp64_peak,
+                                  "frac": achieved_fp64 / fp64_peak, "flops_per_launch": geo_flops,
+                                  "windows_per_launch": windows, "peak_source": "measured FMA-chain kernel"}},
+            "kernels_ms_per_step": {"geodesic": geo_ms, "walk": walk_ms},
+            "counters_per_step": {k: v / args.steps for k, v in cnt2.items()},
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="torus_nvt")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    cfg = workload_config(args.workload)
+    if args.impl == "reference":
+        run_reference(args, cfg)
+    else:
+        run_ours(args, cfg)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,250 @@
+"""Python front end of libcssg.so: device meshes, batched walks and distance queries, device-resident systems.
+
+Every call goes through the C ABI (include/cssg.h).  Device buffers for the batched calls are torch tensors (torch
+is used only for allocation and streams); the library launches on the stream of the context, which by default is
+torch's current stream so ordering with torch copies is implicit.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, cssg_params
+
+_P = ctypes.c_void_p
+
+
+def _np_ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise _lib.CssgError("CUDA device required: libcssg has no CPU path")
+    return torch
+
+
+class Context:
+    """cssg_ctx: a CUDA stream (torch's current stream unless one is given)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        L = _lib.load()
+        torch = _torch()
+        if stream is None:
+            with torch.cuda.device(device):
+                stream = torch.cuda.current_stream().cuda_stream
+        self.device = device
+        h = ctypes.c_void_p()
+        check(L.cssg_ctx_create(device, ctypes.c_void_p(stream), ctypes.byref(h)), "cssg_ctx_create")
+        self.h = h
+
+    @property
+    def stream(self):
+        return _lib.load().cssg_ctx_stream(self.h)
+
+    def synchronize(self):
+        check(_lib.load().cssg_ctx_synchronize(self.h), "cssg_ctx_synchronize")
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and _lib._lib is not None:
+            _lib._lib.cssg_ctx_destroy(self.h)
+            self.h = None
+
+
+class Mesh:
+    """cssg_mesh: the triangulated surface on the device (triangulatedMeshSpace::loadMeshFromFile)."""
+
+    def __init__(self, V, F, device: int = 0):
+        L = _lib.load()
+        self.V = np.ascontiguousarray(V, dtype=np.float64)
+        self.F = np.ascontiguousarray(F, dtype=np.int32)
+        h = ctypes.c_void_p()
+        check(L.cssg_mesh_create(_np_ptr(self.V), self.V.shape[0], _np_ptr(self.F), self.F.shape[0], device,
+                                 ctypes.byref(h)), "cssg_mesh_create")
+        self.h = h
+        nv, nf = ctypes.c_int(), ctypes.c_int()
+        area = ctypes.c_double()
+        bbox = np.zeros(6)
+        check(L.cssg_mesh_info(h, ctypes.byref(nv), ctypes.byref(nf), ctypes.byref(area), _np_ptr(bbox)),
+              "cssg_mesh_info")
+        self.nV, self.nF, self.area = nv.value, nf.value, area.value
+        self.bbox = (bbox[:3].copy(), bbox[3:].copy())
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and _lib._lib is not None:
+            _lib._lib.cssg_mesh_destroy(self.h)
+            self.h = None
+
+
+def transport_batch(ctx: Context, mesh: Mesh, face, bary, disp, transport=None):
+    """Batched transportParticleAndVectors on host arrays; returns (face, bary, disp, transport, status)."""
+    torch = _torch()
+    dev = f"cuda:{ctx.device}"
+    n = len(face)
+    f = torch.tensor(np.asarray(face, dtype=np.int32), device=dev)
+    b = torch.tensor(np.asarray(bary, dtype=np.float64).reshape(n, 3), device=dev)
+    d = torch.tensor(np.asarray(disp, dtype=np.float64).reshape(n, 3), device=dev)
+    ntv = 0
+    tv = None
+    if transport is not None:
+        tvh = np.asarray(transport, dtype=np.float64).reshape(n, -1, 3)
+        ntv = tvh.shape[1]
+        tv = torch.tensor(tvh, device=dev)
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    L = _lib.load()
+    check(L.cssg_transport_batch(ctx.h, mesh.h, n, _P(f.data_ptr()), _P(b.data_ptr()), _P(d.data_ptr()),
+                                 _P(tv.data_ptr()) if tv is not None else None, ntv, _P(st.data_ptr()),
+                                 _P(cnt.data_ptr())), "cssg_transport_batch")
+    ctx.synchronize()
+    return (f.cpu().numpy(), b.cpu().numpy(), d.cpu().numpy(), tv.cpu().numpy() if tv is not None else None,
+            st.cpu().numpy(), int(cnt.cpu().item()))
+
+
+def distance_batch(ctx: Context, mesh: Mesh, src_face, src_bary, cand_off, cand_face, cand_bary, submesh=False,
+                   max_dist=1.0, threshold=None, cutoff=math.inf):
+    """Batched triangulatedMeshSpace::distance over sources with CSR candidate lists (host arrays in and out)."""
+    torch = _torch()
+    dev = f"cuda:{ctx.device}"
+    ns = len(src_face)
+    sf = torch.tensor(np.asarray(src_face, dtype=np.int32), device=dev)
+    sb = torch.tensor(np.asarray(src_bary, dtype=np.float64).reshape(ns, 3), device=dev)
+    co = torch.tensor(np.asarray(cand_off, dtype=np.int32), device=dev)
+    m = int(cand_off[-1])
+    cf = torch.tensor(np.asarray(cand_face, dtype=np.int32).reshape(m), device=dev)
+    cb = torch.tensor(np.asarray(cand_bary, dtype=np.float64).reshape(m, 3), device=dev)
+    th = torch.tensor(np.asarray(threshold, dtype=np.float64), device=dev) if threshold is not None else None
+    d = torch.zeros(max(m, 1), dtype=torch.float64, device=dev)
+    ts = torch.zeros((max(m, 1), 3), dtype=torch.float64, device=dev)
+    te = torch.zeros((max(m, 1), 3), dtype=torch.float64, device=dev)
+    st = torch.zeros(max(ns, 1), dtype=torch.int32, device=dev)
+    L = _lib.load()
+    check(L.cssg_distance_batch(ctx.h, mesh.h, ns, _P(sf.data_ptr()), _P(sb.data_ptr()), _P(co.data_ptr()),
+                                _P(cf.data_ptr()), _P(cb.data_ptr()), int(bool(submesh)), float(max_dist),
+                                _P(th.data_ptr()) if th is not None else None, float(cutoff), _P(d.data_ptr()),
+                                _P(ts.data_ptr()), _P(te.data_ptr()), _P(st.data_ptr())), "cssg_distance_batch")
+    ctx.synchronize()
+    return d.cpu().numpy()[:m], ts.cpu().numpy()[:m], te.cpu().numpy()[:m], st.cpu().numpy()[:ns]
+
+
+def fp64_peak_gflops(ctx: Context) -> float:
+    out = ctypes.c_double()
+    check(_lib.load().cssg_diag_fp64_peak(ctx.h, ctypes.byref(out)), "cssg_diag_fp64_peak")
+    return out.value
+
+
+def make_params(integrator="nve", force="harmonic", k=1.0, sigma=1.0, range_=None, submesh=False, max_dist=None,
+                cutoff=None, dt=0.001, temperature=0.0, tau=1.0, chain_length=2):
+    p = cssg_params()
+    p.integrator = {"nve": 0, "nvt": 1}[integrator] if isinstance(integrator, str) else int(integrator)
+    p.force_kind = {"harmonic": 0, "gaussian": 1}[force] if isinstance(force, str) else int(force)
+    p.k = float(k)
+    p.sigma = float(sigma)
+    p.range = float(sigma if range_ is None else range_)
+    p.submesh = int(bool(submesh))
+    p.max_dist = float(sigma if max_dist is None else max_dist)
+    p.cutoff = float(sigma if cutoff is None else cutoff)
+    p.dt = float(dt)
+    p.temperature = float(temperature)
+    p.tau = float(tau)
+    p.chain_length = int(chain_length)
+    return p
+
+
+class System:
+    """cssg_system: particles, forces and the updater resident on the device."""
+
+    def __init__(self, ctx: Context, mesh: Mesh, n: int, params: cssg_params):
+        L = _lib.load()
+        self.ctx, self.mesh, self.n, self.params = ctx, mesh, n, params
+        h = ctypes.c_void_p()
+        check(L.cssg_system_create(ctx.h, mesh.h, n, ctypes.byref(params), ctypes.byref(h)), "cssg_system_create")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and _lib._lib is not None:
+            _lib._lib.cssg_system_destroy(self.h)
+            self.h = None
+
+    def set_state(self, face=None, bary=None, vel=None, force=None):
+        def prep(a, dt, shape):
+            if a is None:
+                return None, None
+            arr = np.ascontiguousarray(np.asarray(a, dtype=dt).reshape(shape))
+            return arr, _np_ptr(arr)
+        fa, fp = prep(face, np.int32, (self.n,))
+        ba, bp = prep(bary, np.float64, (self.n, 3))
+        va, vp = prep(vel, np.float64, (self.n, 3))
+        qa, qp = prep(force, np.float64, (self.n, 3))
+        check(_lib.load().cssg_system_set_state(self.h, fp, bp, vp, qp), "cssg_system_set_state")
+
+    def reset_thermostat(self):
+        check(_lib.load().cssg_system_reset_thermostat(self.h), "cssg_system_reset_thermostat")
+
+    def kernels_per_step(self):
+        c = ctypes.c_int()
+        check(_lib.load().cssg_system_kernels_per_step(self.h, ctypes.byref(c)), "cssg_system_kernels_per_step")
+        return c.value
+
+    def get_state(self):
+        face = np.zeros(self.n, dtype=np.int32)
+        bary = np.zeros((self.n, 3))
+        vel = np.zeros((self.n, 3))
+        force = np.zeros((self.n, 3))
+        check(_lib.load().cssg_system_get_state(self.h, _np_ptr(face), _np_ptr(bary), _np_ptr(vel), _np_ptr(force)),
+              "cssg_system_get_state")
+        return face, bary, vel, force
+
+    def device_state(self):
+        ptrs = [ctypes.c_void_p() for _ in range(4)]
+        check(_lib.load().cssg_system_device_state(self.h, *[ctypes.byref(p) for p in ptrs]),
+              "cssg_system_device_state")
+        return [p.value for p in ptrs]
+
+    def step(self, steps: int = 1, graph: bool = True):
+        check(_lib.load().cssg_system_step(self.h, int(steps), int(bool(graph))), "cssg_system_step")
+
+    def compute_forces(self):
+        check(_lib.load().cssg_system_compute_forces(self.h), "cssg_system_compute_forces")
+
+    def check(self):
+        bits = ctypes.c_int()
+        cnt = np.zeros(5, dtype=np.uint64)
+        check(_lib.load().cssg_system_check(self.h, ctypes.byref(bits), _np_ptr(cnt)), "cssg_system_check")
+        return bits.value, {"crossings": int(cnt[0]), "windows": int(cnt[1]), "launches": int(cnt[2]),
+                            "in_range_pairs": int(cnt[3]), "capacity_hits": int(cnt[4])}
+
+    def enable_pairs(self):
+        cnt = ctypes.c_int()
+        check(_lib.load().cssg_system_pairs(self.h, 0, None, None, None, None, ctypes.byref(cnt)), "pairs")
+
+    def pairs(self):
+        L = _lib.load()
+        cnt = ctypes.c_int()
+        check(L.cssg_system_pairs(self.h, 0, None, None, None, None, ctypes.byref(cnt)), "pairs")
+        m = cnt.value
+        i = np.zeros(m, dtype=np.int32)
+        j = np.zeros(m, dtype=np.int32)
+        d = np.zeros(m)
+        t = np.zeros((m, 3))
+        check(L.cssg_system_pairs(self.h, m, _np_ptr(i), _np_ptr(j), _np_ptr(d), _np_ptr(t), ctypes.byref(cnt)),
+              "pairs")
+        return i, j, d, t
+
+    def chain(self):
+        cap = 4 * (max(1, self.params.chain_length) + 1) + 2
+        out = np.zeros(cap)
+        check(_lib.load().cssg_system_chain(self.h, _np_ptr(out), cap), "cssg_system_chain")
+        return out
+
+    def timing(self, enable: bool):
+        check(_lib.load().cssg_system_timing(self.h, int(bool(enable))), "cssg_system_timing")
+
+    def last_times(self):
+        out = np.zeros(2)
+        check(_lib.load().cssg_system_last_times(self.h, _np_ptr(out), 2), "cssg_system_last_times")
+        return {"geodesic_ms": float(out[0]), "walk_ms": float(out[1])}

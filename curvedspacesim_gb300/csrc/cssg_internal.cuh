@@ -1,0 +1,125 @@
+// Internal declarations shared by the translation units of libcssg.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/cssg.h"
+
+// Device-resident mesh (structure of arrays).  Local edge k of face f runs F[3f+k] -> F[3f+(k+1)%3].
+struct DevMesh {
+    int nV, nF;
+    const double* V;            // 3 nV vertex positions
+    const int* F;               // 3 nF vertex indices (counter-clockwise)
+    const int* twin;            // 3 nF: face*3 + local edge of the neighbour across local edge k, -1 on a border
+    const double* N;            // 3 nF unit face normals
+    const double* geom;         // 9 nF: [9f + 3k + 0] edge length, [+1],[+2] third vertex in the edge frame
+    const int* vfStart;         // nV + 1: vertex -> incident faces (CSR)
+    const int* vfList;
+    const int* ringStart;       // nV + 1: clockwise neighbour ring of closed vertices (throughVertex order)
+    const int* ringV;
+    const unsigned char* vflag; // bit0 closed ring available, bit1 border vertex, bit2 saddle (angle sum > 2 pi)
+    double bbMin[3], bbMax[3];
+};
+
+enum { VF_RING = 1, VF_BORDER = 2, VF_SADDLE = 4 };
+
+struct cssg_mesh {
+    DevMesh d;
+    int device;
+    double area;
+    double meanEdge;
+    double meanFaceArea;
+    void* buffers[12];
+};
+
+struct cssg_ctx {
+    int device;
+    cudaStream_t stream;
+    bool ownStream;
+};
+
+// error plumbing
+void cssg_set_error(const std::string& msg);
+int cssg_cuda_fail(cudaError_t e, const char* what);
+#define CSSG_CUDA(call)                                      \
+    do {                                                     \
+        cudaError_t e__ = (call);                            \
+        if (e__ != cudaSuccess) return cssg_cuda_fail(e__, #call); \
+    } while (0)
+
+// ---- walk (walk.cu) ----------------------------------------------------------------------------------------------
+// Launches the batched transport kernel; pos_out (nullable) receives the final R3 positions, crossings (nullable)
+// accumulates the launch's crossings.
+void cssg_launch_transport(const DevMesh& M, int n, int* face, double* bary, double* disp, double* transport, int nT,
+                           int* status, unsigned long long* crossings, double* pos_out, cudaStream_t s);
+void cssg_launch_positions(const DevMesh& M, int n, const int* face, const double* bary, double* pos, cudaStream_t s);
+
+// ---- geodesics (geodesic.cu) -------------------------------------------------------------------------------------
+struct GeoCaps {
+    int CT;    // targets per source
+    int CV;    // vertex hash capacity (power of two)
+    int CF;    // face hash capacity (power of two)
+    int CW;    // windows per frontier buffer
+    int CL;    // launch list entries per buffer
+    int CLOG;  // target-face window log entries
+};
+
+// Per-launch configuration of the fused neighbour / geodesic / force kernel.
+struct GeoLaunch {
+    // sources
+    int nSrc;
+    const int* srcFace;
+    const double* srcBary;
+    const double* srcPos;        // nullable: R3 positions of the sources (system mode)
+    const int* order;            // nullable: processing order of the sources (cell order)
+    // targets: CSR mode (distance API) ...
+    const int* candOff;
+    const int* candFace;
+    const double* candBary;
+    // ... or neighbour search mode (system): particles + cell list
+    int searchMode;              // 0 CSR, 1 cell list, 2 all-to-all
+    int nPart;
+    const int* partFace;
+    const double* partBary;
+    const double* partPos;
+    const int* cellStart;        // totalCells + 1
+    const int* cellList;         // particle indices sorted by cell (stable)
+    int nc[3];
+    double cs[3];
+    double range2;               // candidate test: chord^2 < range2
+    // domain
+    int submesh;
+    double maxDist;
+    const double* threshold;     // nullable (CSR mode)
+    double cutoff;
+    // outputs
+    double* dOut;                // per candidate (CSR mode) or per pair slot (system mode, nullable)
+    double* tsOut;
+    double* teOut;
+    int* pairJ;                  // system mode pair output: target particle index (nullable)
+    int* pairCount;              // system mode: candidates per source (nullable)
+    int pairCap;                 // system mode: pair slots per source
+    double* force;               // system mode: force per source (nullable)
+    int forceKind;
+    double k, sigma;
+    int* status;                 // per source
+    unsigned long long* counters;  // [0] windows processed, [1] vertex launches, [2] in-range pairs, [3] capacity hits
+    int patchDisconnected;       // CSR mode with cutoff = inf: unreached -> 2*maxDist, tangent (0,0,1)
+    double delta;                // bucket width of the propagation order (inf = plain rounds)
+    int maxRounds;
+    // scratch
+    GeoCaps caps;
+    void* scratch;
+    size_t slotBytes;
+    int nSlots;                  // warps with a slot
+    int* workCounter;            // persistent-warp work queue
+    const int* itemCountDev;     // nullable: number of work items read from the device (retry pass)
+    int* failList;               // nullable: sources whose tables overflowed are queued here for a retry pass
+    int* failCount;
+};
+
+size_t cssg_geo_slot_bytes(const GeoCaps& c);
+// Fills slots with their initial (empty) state; call once after allocating the scratch.
+void cssg_geo_init_scratch(void* scratch, size_t slotBytes, int nSlots, const GeoCaps& c, cudaStream_t s);
+void cssg_launch_geodesic(const DevMesh& M, const GeoLaunch& L, int blocks, cudaStream_t s);

@@ -1,0 +1,1209 @@
+// Exact geodesic distances + start tangents + pair forces: one warp per source particle, persistent warps.
+//
+// Replaces, per timestep, the reference's per-source loop in simpleModel::findNeighbors
+// (src/models/simpleModel.cpp:68-112): candidate search (cellListNeighborStructure::constructCandidateNeighborList,
+// src/utility/cellListNeighborStructure.cpp:45-84, or the all-to-all baseNeighborStructure), the patch
+// (submesher::constructSubmeshFromSourceAndTargets, src/utility/submesher.cpp:55-147), the CGAL
+// Surface_mesh_shortest_path solve and path tangents (triangulatedMeshSpace.cpp:155-238,
+// meshUtilities.cpp:360-380) and the force sum of force::computeForces (src/forces/baseForce.cpp:12-28) with
+// harmonicRepulsion / gaussianRepulsion::pairwiseForce.
+//
+// Geodesics: continuous-Dijkstra window propagation (the Chen-Han / Xin-Wang family of exact algorithms that CGAL
+// implements), restated from the published method:
+//   * a window lives on the edge through which it enters face g; its frame has the origin at the edge's first
+//     vertex, x along the edge and y into g; the pseudo-source I = (sx, sy) lies behind the edge at path length
+//     sigma from the source; [b0, b1] is the part of the edge it covers;
+//   * propagating through g splits the window at the ray through g's opposite vertex C into children on the two
+//     other edges (rigid 2D frame changes, no trigonometry);
+//   * vertex labels (best known path lengths) trim windows exactly against the two endpoint vertices of their edge
+//     (the excess of the window path over an endpoint-vertex path is monotone along the edge) and discard windows
+//     that the opposite vertex dominates everywhere;
+//   * saddle vertices (angle sum > 2 pi) and border vertices of the domain become pseudo-sources when their label
+//     improves; windows never re-enter the source face (the chord inside it is optimal);
+//   * start tangents ride along: windows from the source carry the rotation of their frame into the source face
+//     frame, windows from a vertex pseudo-source carry that vertex's start direction.
+// The lanes of a warp process a round of windows in parallel; vertex labels are updated with 64-bit atomicMin on
+// the bit patterns of non-negative doubles and the start direction of a label is written, after a __syncwarp, by
+// the lane whose proposal survived.  Processing order only affects how much gets pruned, not the result.
+//
+// Roofline: this kernel is FP64 latency/issue bound (scalar double arithmetic on irregular, data-dependent work);
+// its memory footprint per source is a few KB of L2-resident scratch plus mesh reads.
+#include <math_constants.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "cssg_internal.cuh"
+
+namespace {
+
+constexpr unsigned long long INF_BITS = 0x7FF0000000000000ull;
+constexpr unsigned FULL = 0xffffffffu;
+
+struct __align__(16) Win {
+    double b0, b1, sx, sy, sigma, c, s;
+    int he;   // entered face * 4 + local edge
+    int src;  // -1: the source, else the vertex pseudo-source
+};
+
+__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ double bitsd(unsigned long long b)
+{
+    return b >= INF_BITS ? CUDART_INF : __longlong_as_double((long long)b);
+}
+
+struct WarpCtl {
+    int nA, nB, nLA, nLB, nLog, nV, nF, nT, err, nBA, nBB, pad;
+};
+
+struct Slot {
+    int* tface;
+    int* tidx;
+    int* tnext;
+    double* tb;
+    double* tp;
+    unsigned long long* tbest;
+    int* vkey;
+    unsigned long long* vlab;
+    double* vtx;
+    double* vty;
+    unsigned long long* vtok;
+    int* vlist;
+    int* fkey;
+    int* fhead;
+    int* flist;
+    Win* wA;
+    Win* wB;
+    Win* wlog;
+    int* lA;
+    int* lB;
+    double* ld;  // per launch entry: label, start direction (x, y) it launched with
+    int* bA;
+    int* bB;
+};
+
+__host__ __device__ inline size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+__host__ __device__ inline size_t carve(const GeoCaps& c, char* base, Slot* S)
+{
+    size_t o = 0;
+#define CARVE(field, type, count)                                  \
+    if (S) S->field = (type*)(base + o);                           \
+    o = align_up(o + sizeof(type) * (size_t)(count));
+    CARVE(tface, int, c.CT);
+    CARVE(tidx, int, c.CT);
+    CARVE(tnext, int, c.CT);
+    CARVE(tb, double, 3 * c.CT);
+    CARVE(tp, double, 3 * c.CT);
+    CARVE(tbest, unsigned long long, c.CT);
+    CARVE(vkey, int, c.CV);
+    CARVE(vlab, unsigned long long, c.CV);
+    CARVE(vtx, double, c.CV);
+    CARVE(vty, double, c.CV);
+    CARVE(vtok, unsigned long long, c.CV);
+    CARVE(vlist, int, c.CV);
+    CARVE(fkey, int, c.CF);
+    CARVE(fhead, int, c.CF);
+    CARVE(flist, int, c.CF);
+    CARVE(wA, Win, c.CW);
+    CARVE(wB, Win, c.CW);
+    CARVE(wlog, Win, c.CLOG);
+    CARVE(lA, int, c.CL);
+    CARVE(lB, int, c.CL);
+    CARVE(ld, double, 3 * c.CL);
+    CARVE(bA, int, c.CF);
+    CARVE(bB, int, c.CF);
+#undef CARVE
+    return o;
+}
+
+__device__ __forceinline__ unsigned hash_int(int k) { return (unsigned)k * 2654435761u; }
+
+// ---- hash tables ----------------------------------------------------------------------------------------------
+__device__ int vfind(const Slot& S, int CV, int v)
+{
+    unsigned h = hash_int(v) & (CV - 1);
+    for (int p = 0; p < CV; ++p) {
+        int k = __ldcg(&S.vkey[h]);
+        if (k == v) return (int)h;
+        if (k == -1) return -1;
+        h = (h + 1) & (CV - 1);
+    }
+    return -1;
+}
+
+__device__ int vinsert(const Slot& S, int CV, int v, WarpCtl* ctl)
+{
+    unsigned h = hash_int(v) & (CV - 1);
+    for (int p = 0; p < CV; ++p) {
+        int k = __ldcg(&S.vkey[h]);
+        if (k == v) return (int)h;
+        if (k == -1) {
+            int old = atomicCAS(&S.vkey[h], -1, v);
+            if (old == -1) {
+                int pos = atomicAdd(&ctl->nV, 1);
+                if (pos < CV) S.vlist[pos] = (int)h;
+                return (int)h;
+            }
+            if (old == v) return (int)h;
+        }
+        h = (h + 1) & (CV - 1);
+    }
+    atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+    return -1;
+}
+
+__device__ int ffind(const Slot& S, int CF, int f)
+{
+    unsigned h = hash_int(f) & (CF - 1);
+    for (int p = 0; p < CF; ++p) {
+        int k = __ldcg(&S.fkey[h]);
+        if (k == f) return (int)h;
+        if (k == -1) return -1;
+        h = (h + 1) & (CF - 1);
+    }
+    return -1;
+}
+
+// returns slot; *fresh = 1 when this call inserted the key
+__device__ int finsert(const Slot& S, int CF, int f, WarpCtl* ctl, int* fresh)
+{
+    *fresh = 0;
+    unsigned h = hash_int(f) & (CF - 1);
+    for (int p = 0; p < CF; ++p) {
+        int k = __ldcg(&S.fkey[h]);
+        if (k == f) return (int)h;
+        if (k == -1) {
+            int old = atomicCAS(&S.fkey[h], -1, f);
+            if (old == -1) {
+                int pos = atomicAdd(&ctl->nF, 1);
+                if (pos < CF) S.flist[pos] = (int)h;
+                else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                *fresh = 1;
+                return (int)h;
+            }
+            if (old == f) return (int)h;
+        }
+        h = (h + 1) & (CF - 1);
+    }
+    atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+    return -1;
+}
+
+__device__ __forceinline__ double vlabel(const Slot& S, int CV, int v)
+{
+    int h = vfind(S, CV, v);
+    return h < 0 ? CUDART_INF : bitsd(__ldcg(&S.vlab[h]));
+}
+
+// ---- per-source solver state ----------------------------------------------------------------------------------
+struct Src {
+    int f0;
+    double S[3];
+    double e1[3], e2[3];
+    bool full;
+    double cutoff;
+};
+
+struct VRec {
+    int slot, v;
+    double d, dx, dy;
+};
+
+__device__ __forceinline__ double key_of(const Win& w)
+{
+    double m;
+    if (w.sx < w.b0) m = hypot(w.sx - w.b0, w.sy);
+    else if (w.sx > w.b1) m = hypot(w.sx - w.b1, w.sy);
+    else m = fabs(w.sy);
+    return w.sigma + m;
+}
+
+__device__ __forceinline__ bool in_domain(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int g)
+{
+    if (g < 0) return false;
+    if (src.full) return true;
+    return ffind(S, C.CF, g) >= 0;
+}
+
+__device__ bool trim(const DevMesh& M, const Slot& S, const GeoCaps& C, Win& w)
+{
+    const int g = w.he >> 2, j = w.he & 3;
+    const double L = M.geom[9 * g + 3 * j];
+    const int A = M.F[3 * g + j], B = M.F[3 * g + (j + 1) % 3], Cv = M.F[3 * g + (j + 2) % 3];
+    double dA = vlabel(S, C.CV, A);
+    if (dA < CUDART_INF) {
+        double a = dA - w.sigma;
+        double fb0 = hypot(w.b0 - w.sx, w.sy) - a - w.b0;
+        if (fb0 > 0) {
+            if (a + w.sx <= 0) return false;
+            double xs = (w.sx * w.sx + w.sy * w.sy - a * a) / (2.0 * (a + w.sx));
+            if (xs >= w.b1) return false;
+            w.b0 = fmax(w.b0, xs);
+        }
+    }
+    double dB = vlabel(S, C.CV, B);
+    if (dB < CUDART_INF) {
+        double a = dB - w.sigma;
+        double sxm = L - w.sx, xm = L - w.b1;
+        double fb1 = hypot(xm - sxm, w.sy) - a - xm;
+        if (fb1 > 0) {
+            if (a + sxm <= 0) return false;
+            double xs = (sxm * sxm + w.sy * w.sy - a * a) / (2.0 * (a + sxm));
+            if (L - xs <= w.b0) return false;
+            w.b1 = fmin(w.b1, L - xs);
+        }
+    }
+    double dC = vlabel(S, C.CV, Cv);
+    if (dC < CUDART_INF) {
+        double cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
+        double m0 = hypot(cx - w.b0, cy), m1 = hypot(cx - w.b1, cy);
+        if (dC + fmax(m0, m1) < key_of(w)) return false;
+    }
+    return w.b1 - w.b0 > 1e-14 * L;
+}
+
+__device__ void push_win(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, Win w)
+{
+    const int g = w.he >> 2, j = w.he & 3;
+    if (g == src.f0 || !in_domain(M, S, C, src, g)) return;
+    w.b0 = fmax(0.0, w.b0);
+    w.b1 = fmin(M.geom[9 * g + 3 * j], w.b1);
+    if (!trim(M, S, C, w)) return;
+    if (key_of(w) > src.cutoff) return;
+    int pos = atomicAdd(&ctl->nB, 1);
+    if (pos >= C.CW) {
+        atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+        return;
+    }
+    S.wB[pos] = w;
+}
+
+__device__ __forceinline__ void start_dir(const Win& w, double px, double py, double& dx, double& dy)
+{
+    if (w.sigma == 0) {
+        double ux = px - w.sx, uy = py - w.sy;
+        double l = hypot(ux, uy);
+        ux /= l;
+        uy /= l;
+        dx = w.c * ux - w.s * uy;
+        dy = w.s * ux + w.c * uy;
+    } else {
+        dx = w.c;
+        dy = w.s;
+    }
+}
+
+__device__ __forceinline__ void propose(const Slot& S, const GeoCaps& C, WarpCtl* ctl, int v, double d, double dx,
+                                        double dy, VRec& rec)
+{
+    rec.slot = -1;
+    int h = vinsert(S, C.CV, v, ctl);
+    if (h < 0) return;
+    unsigned long long b = dbits(d);
+    unsigned long long old = atomicMin(&S.vlab[h], b);
+    if (b < old) {
+        rec.slot = h;
+        rec.v = v;
+        rec.d = d;
+        rec.dx = dx;
+        rec.dy = dy;
+    }
+}
+
+__device__ bool launchable(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int v)
+{
+    if (M.vflag[v] & (VF_BORDER | VF_SADDLE)) return true;
+    if (src.full) return false;
+    for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i)
+        if (ffind(S, C.CF, M.vfList[i]) < 0) return true;
+    return false;
+}
+
+// after __syncwarp: the surviving proposal writes the start direction and queues a pseudo-source launch
+__device__ void resolve(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl,
+                        const VRec& r)
+{
+    if (r.slot < 0) return;
+    unsigned long long b = dbits(r.d);
+    if (__ldcg(&S.vlab[r.slot]) != b) return;
+    S.vtx[r.slot] = r.dx;
+    S.vty[r.slot] = r.dy;
+    if (r.d <= src.cutoff && launchable(M, S, C, src, r.v)) {
+        if (atomicExch(&S.vtok[r.slot], b) != b) {
+            int pos = atomicAdd(&ctl->nLA, 1);
+            if (pos < C.CL) S.lA[pos] = r.v;
+            else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+        }
+    }
+}
+
+// process one window (lane-local); records up to three vertex proposals
+__device__ void process(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, Win w,
+                        VRec* rec, int& processed)
+{
+    rec[0].slot = rec[1].slot = rec[2].slot = -1;
+    if (!trim(M, S, C, w)) return;
+    processed++;
+    const int g = w.he >> 2, j = w.he & 3;
+    const double L = M.geom[9 * g + 3 * j], cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
+    const int A = M.F[3 * g + j], B = M.F[3 * g + (j + 1) % 3], Cv = M.F[3 * g + (j + 2) % 3];
+    const double tol = 1e-12 * L;
+    // targets in g: log the window for the final query and update the running bests (early exit)
+    int fh = ffind(S, C.CF, g);
+    if (fh >= 0) {
+        int head = __ldcg(&S.fhead[fh]);
+        if (head >= 0) {
+            int pos = atomicAdd(&ctl->nLog, 1);
+            if (pos < C.CLOG) S.wlog[pos] = w;
+            else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+            for (int t = head; t >= 0; t = S.tnext[t]) {
+                double b1 = S.tb[3 * t + (j + 1) % 3], b2 = S.tb[3 * t + (j + 2) % 3];
+                double px = b1 * L + b2 * cx, py = b2 * cy;
+                double xp = w.sx + (px - w.sx) * (-w.sy) / (py - w.sy);
+                if (xp >= w.b0 - tol && xp <= w.b1 + tol) {
+                    double d = w.sigma + hypot(px - w.sx, py - w.sy);
+                    atomicMin(&S.tbest[t], dbits(d));
+                }
+            }
+        }
+    }
+    double xC = w.sx + (cx - w.sx) * (-w.sy) / (cy - w.sy);
+    if (xC >= w.b0 - tol && xC <= w.b1 + tol) {
+        double dx, dy;
+        start_dir(w, cx, cy, dx, dy);
+        propose(S, C, ctl, Cv, w.sigma + hypot(cx - w.sx, cy - w.sy), dx, dy, rec[0]);
+    }
+    if (w.b0 <= tol) {
+        double dx, dy;
+        start_dir(w, 0, 0, dx, dy);
+        propose(S, C, ctl, A, w.sigma + hypot(w.sx, w.sy), dx, dy, rec[1]);
+    }
+    if (w.b1 >= L - tol) {
+        double dx, dy;
+        start_dir(w, L, 0, dx, dy);
+        propose(S, C, ctl, B, w.sigma + hypot(L - w.sx, w.sy), dx, dy, rec[2]);
+    }
+    if (w.b0 < xC) {  // exit through edge C->A (local j+2); child frame: origin A, x toward C
+        int t = M.twin[3 * g + (j + 2) % 3];
+        if (t >= 0) {
+            double n = hypot(cx, cy);
+            double ux = cx / n, uy = cy / n;
+            double isx = ux * w.sx + uy * w.sy, isy = -uy * w.sx + ux * w.sy;
+            Win c;
+            c.he = (t / 3) * 4 + t % 3;
+            c.src = w.src;
+            c.sigma = w.sigma;
+            c.sx = isx;
+            c.sy = isy;
+            {
+                double X = ux * w.b0, Y = -uy * w.b0;
+                c.b0 = isx + (X - isx) * (-isy) / (Y - isy);
+            }
+            if (w.b1 >= xC) c.b1 = M.geom[9 * (t / 3) + 3 * (t % 3)];
+            else {
+                double X = ux * w.b1, Y = -uy * w.b1;
+                c.b1 = isx + (X - isx) * (-isy) / (Y - isy);
+            }
+            if (w.sigma == 0) {
+                c.c = w.c * ux - w.s * uy;
+                c.s = w.s * ux + w.c * uy;
+            } else {
+                c.c = w.c;
+                c.s = w.s;
+            }
+            push_win(M, S, C, src, ctl, c);
+        }
+    }
+    if (w.b1 > xC) {  // exit through edge B->C (local j+1); child frame: origin C, x toward B
+        int t = M.twin[3 * g + (j + 1) % 3];
+        if (t >= 0) {
+            double bx = L - cx, by = -cy;
+            double n = hypot(bx, by);
+            double ux = bx / n, uy = by / n;
+            double rx = w.sx - cx, ry = w.sy - cy;
+            double isx = ux * rx + uy * ry, isy = -uy * rx + ux * ry;
+            Win c;
+            c.he = (t / 3) * 4 + t % 3;
+            c.src = w.src;
+            c.sigma = w.sigma;
+            c.sx = isx;
+            c.sy = isy;
+            if (w.b0 <= xC) c.b0 = 0.0;
+            else {
+                double X = ux * (w.b0 - cx) + uy * (-cy), Y = -uy * (w.b0 - cx) + ux * (-cy);
+                c.b0 = isx + (X - isx) * (-isy) / (Y - isy);
+            }
+            {
+                double X = ux * (w.b1 - cx) + uy * (-cy), Y = -uy * (w.b1 - cx) + ux * (-cy);
+                c.b1 = isx + (X - isx) * (-isy) / (Y - isy);
+            }
+            if (w.sigma == 0) {
+                c.c = w.c * ux - w.s * uy;
+                c.s = w.s * ux + w.c * uy;
+            } else {
+                c.c = w.c;
+                c.s = w.s;
+            }
+            push_win(M, S, C, src, ctl, c);
+        }
+    }
+}
+
+__device__ __forceinline__ double warp_min(double x)
+{
+    for (int o = 16; o > 0; o >>= 1) x = fmin(x, __shfl_xor_sync(FULL, x, o));
+    return x;
+}
+__device__ __forceinline__ double warp_max(double x)
+{
+    for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(FULL, x, o));
+    return x;
+}
+__device__ __forceinline__ double warp_sum(double x)
+{
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+    return x;
+}
+__device__ __forceinline__ int warp_sum_i(int x)
+{
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+    return x;
+}
+
+__device__ __forceinline__ void load_pt(const DevMesh& M, int f, const double* b, double* out)
+{
+    const double* p0 = &M.V[3 * M.F[3 * f]];
+    const double* p1 = &M.V[3 * M.F[3 * f + 1]];
+    const double* p2 = &M.V[3 * M.F[3 * f + 2]];
+    double s = b[0] + b[1] + b[2];
+    for (int c = 0; c < 3; ++c) out[c] = (b[0] * p0[c] + b[1] * p1[c] + b[2] * p2[c]) / s;
+}
+
+// final distance of target t: source face, logged windows and face-vertex labels
+__device__ double target_query(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int t, int nLog,
+                               double* ts, double* te)
+{
+    const int f = S.tface[t];
+    const double* P = &S.tp[3 * t];
+    ts[0] = ts[1] = ts[2] = 0;
+    te[0] = te[1] = te[2] = 0;
+    if (f == src.f0) {
+        double u[3] = {P[0] - src.S[0], P[1] - src.S[1], P[2] - src.S[2]};
+        double d = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+        if (d > 0)
+            for (int c = 0; c < 3; ++c) ts[c] = te[c] = u[c] / d;
+        return d;
+    }
+    double best = CUDART_INF, bdx = 0, bdy = 0;
+    int bw = -1;
+    double bux = 0, buy = 0;
+    for (int e = 0; e < nLog; ++e) {
+        const Win w = S.wlog[e];
+        const int g = w.he >> 2;
+        if (g != f) continue;
+        const int j = w.he & 3;
+        const double L = M.geom[9 * g + 3 * j], cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
+        double b1 = S.tb[3 * t + (j + 1) % 3], b2 = S.tb[3 * t + (j + 2) % 3];
+        double px = b1 * L + b2 * cx, py = b2 * cy;
+        double xp = w.sx + (px - w.sx) * (-w.sy) / (py - w.sy);
+        const double tol = 1e-12 * L;
+        if (xp >= w.b0 - tol && xp <= w.b1 + tol) {
+            double d = w.sigma + hypot(px - w.sx, py - w.sy);
+            if (d < best) {
+                best = d;
+                start_dir(w, px, py, bdx, bdy);
+                bw = e;
+                bux = px - w.sx;
+                buy = py - w.sy;
+            }
+        }
+    }
+    if (bw >= 0) {
+        const Win w = S.wlog[bw];
+        const int g = w.he >> 2, j = w.he & 3;
+        const double L = M.geom[9 * g + 3 * j], cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
+        const double* PA = &M.V[3 * M.F[3 * g + j]];
+        const double* PB = &M.V[3 * M.F[3 * g + (j + 1) % 3]];
+        const double* PC = &M.V[3 * M.F[3 * g + (j + 2) % 3]];
+        double ul = hypot(bux, buy);
+        for (int c = 0; c < 3; ++c) {
+            double ex = (PB[c] - PA[c]) / L;
+            double ey = (PC[c] - PA[c] - cx * ex) / cy;
+            te[c] = (bux * ex + buy * ey) / ul;
+        }
+    }
+    for (int c = 0; c < 3; ++c) {
+        int v = M.F[3 * f + c];
+        int h = vfind(S, C.CV, v);
+        if (h < 0) continue;
+        double lab = bitsd(__ldcg(&S.vlab[h]));
+        if (!(lab < CUDART_INF)) continue;
+        const double* pv = &M.V[3 * v];
+        double u[3] = {P[0] - pv[0], P[1] - pv[1], P[2] - pv[2]};
+        double l = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+        double d = lab + l;
+        if (d < best) {
+            best = d;
+            bdx = S.vtx[h];
+            bdy = S.vty[h];
+            for (int q = 0; q < 3; ++q) te[q] = l > 0 ? u[q] / l : 0;
+        }
+    }
+    if (best < CUDART_INF)
+        for (int c = 0; c < 3; ++c) ts[c] = bdx * src.e1[c] + bdy * src.e2[c];
+    return best;
+}
+
+// candidate-based early exit: no queued window can improve any target any more
+__device__ bool settled(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int nT, double minKey,
+                        int lane)
+{
+    bool ok = true;
+    for (int t = lane; t < nT; t += 32) {
+        if (S.tface[t] == src.f0) continue;
+        double b = bitsd(__ldcg(&S.tbest[t]));
+        const double* P = &S.tp[3 * t];
+        for (int c = 0; c < 3; ++c) {
+            int v = M.F[3 * S.tface[t] + c];
+            int h = vfind(S, C.CV, v);
+            if (h < 0) continue;
+            double lab = bitsd(__ldcg(&S.vlab[h]));
+            if (!(lab < CUDART_INF)) continue;
+            const double* pv = &M.V[3 * v];
+            double u[3] = {P[0] - pv[0], P[1] - pv[1], P[2] - pv[2]};
+            b = fmin(b, lab + sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
+        }
+        if (!(b <= minKey || minKey > src.cutoff)) ok = false;
+    }
+    return __all_sync(FULL, ok);
+}
+
+// The per-source solve (whole warp).  Returns the number of targets; leaves results in the slot.
+__device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, int lane,
+                             unsigned long long* cnt)
+{
+    const GeoCaps& C = Lp.caps;
+    Src src;
+    src.f0 = Lp.srcFace[si];
+    src.cutoff = Lp.cutoff;
+    double b0[3] = {Lp.srcBary[3 * si], Lp.srcBary[3 * si + 1], Lp.srcBary[3 * si + 2]};
+    load_pt(M, src.f0, b0, src.S);
+    if (lane == 0) {
+        ctl->nA = ctl->nB = ctl->nLA = ctl->nLB = ctl->nLog = ctl->nV = ctl->nF = ctl->nT = ctl->err = 0;
+        ctl->nBA = ctl->nBB = 0;
+    }
+    __syncwarp();
+    // ---- targets ---------------------------------------------------------------------------------------------
+    double maxChord2 = 0;
+    if (Lp.searchMode == 0) {
+        int beg = Lp.candOff[si], nT = Lp.candOff[si + 1] - beg;
+        if (nT > C.CT) {
+            if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
+            nT = 0;
+        }
+        for (int t = lane; t < nT; t += 32) {
+            S.tface[t] = Lp.candFace[beg + t];
+            S.tidx[t] = beg + t;
+            for (int c = 0; c < 3; ++c) S.tb[3 * t + c] = Lp.candBary[3 * (beg + t) + c];
+        }
+        if (lane == 0) ctl->nT = nT;
+    } else {
+        // candidates j != i with chord^2 < range2 (cell list: 27 cells in (x, y, z) loop order; or all particles)
+        const double* Pi = &Lp.srcPos[3 * si];
+        int count = 0;
+        auto consider = [&](int jj, bool valid) {
+            bool take = false;
+            double d2 = 0;
+            if (valid && jj != si) {
+                const double* Pj = &Lp.partPos[3 * jj];
+                double dx = Pi[0] - Pj[0], dy = Pi[1] - Pj[1], dz = Pi[2] - Pj[2];
+                d2 = dx * dx + dy * dy + dz * dz;
+                take = (Lp.searchMode == 2) || (d2 < Lp.range2);
+            }
+            unsigned m = __ballot_sync(FULL, take);
+            if (take) {
+                int pos = count + __popc(m & ((1u << lane) - 1));
+                if (pos < C.CT) {
+                    S.tface[pos] = Lp.partFace[jj];
+                    S.tidx[pos] = jj;
+                    for (int c = 0; c < 3; ++c) S.tb[3 * pos + c] = Lp.partBary[3 * jj + c];
+                }
+                maxChord2 = fmax(maxChord2, d2);
+            }
+            count += __popc(m);
+        };
+        if (Lp.searchMode == 2) {
+            for (int base = 0; base < Lp.nPart; base += 32) consider(base + lane, base + lane < Lp.nPart);
+        } else {
+            int ci[3];
+            for (int c = 0; c < 3; ++c) {
+                int q = (int)floor((Pi[c] - M.bbMin[c]) / Lp.cs[c]);
+                ci[c] = max(0, min(Lp.nc[c] - 1, q));
+            }
+            for (int xx = max(0, ci[0] - 1); xx <= min(Lp.nc[0] - 1, ci[0] + 1); ++xx)
+                for (int yy = max(0, ci[1] - 1); yy <= min(Lp.nc[1] - 1, ci[1] + 1); ++yy)
+                    for (int zz = max(0, ci[2] - 1); zz <= min(Lp.nc[2] - 1, ci[2] + 1); ++zz) {
+                        int cell = xx + Lp.nc[0] * (yy + Lp.nc[1] * zz);
+                        int a = Lp.cellStart[cell], b = Lp.cellStart[cell + 1];
+                        for (int base = a; base < b; base += 32) {
+                            int q = base + lane;
+                            consider(q < b ? Lp.cellList[q] : 0, q < b);
+                        }
+                    }
+        }
+        maxChord2 = warp_max(maxChord2);
+        if (count > C.CT) {
+            if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
+            count = 0;
+        }
+        if (lane == 0) ctl->nT = count;
+        if (Lp.pairCount && lane == 0) Lp.pairCount[si] = count;
+    }
+    __syncwarp();
+    const int nT = ctl->nT;
+    if (ctl->err == CSSG_ST_CAPACITY && Lp.failList) {
+        if (lane == 0) {
+            Lp.status[si] = 0;
+            Lp.failList[atomicAdd(Lp.failCount, 1)] = si;
+        }
+        return;
+    }
+    if (nT == 0) {
+        if (Lp.force && lane == 0) {
+            Lp.force[3 * si] = Lp.force[3 * si + 1] = Lp.force[3 * si + 2] = 0;
+        }
+        if (lane == 0) Lp.status[si] = ctl->err;
+        return;
+    }
+    for (int t = lane; t < nT; t += 32) {
+        load_pt(M, S.tface[t], &S.tb[3 * t], &S.tp[3 * t]);
+        S.tbest[t] = INF_BITS;
+        S.tnext[t] = -1;
+    }
+    __syncwarp();
+    // ---- domain: whole mesh or the reference patch ---------------------------------------------------------------
+    src.full = !Lp.submesh;
+    double r = Lp.maxDist;
+    if (Lp.searchMode == 0) {
+        if (Lp.threshold && Lp.threshold[si] < r) r = Lp.threshold[si];
+    } else {
+        double mc = sqrt(maxChord2);
+        if (Lp.searchMode == 2) mc = 1e20;
+        if (mc < r) r = mc;
+    }
+    if (Lp.submesh) {
+        int fresh;
+        bool notInF0 = false, notInSeeds = false;
+        int nb[3];
+        for (int k = 0; k < 3; ++k) {
+            int t = M.twin[3 * src.f0 + k];
+            nb[k] = t < 0 ? -1 : t / 3;
+        }
+        for (int t = lane; t < nT; t += 32) {
+            int f = S.tface[t];
+            if (f != src.f0) {
+                notInF0 = true;
+                if (f != nb[0] && f != nb[1] && f != nb[2]) notInSeeds = true;
+            }
+        }
+        notInF0 = __any_sync(FULL, notInF0);
+        notInSeeds = __any_sync(FULL, notInSeeds);
+        if (lane == 0) finsert(S, C.CF, src.f0, ctl, &fresh);
+        __syncwarp();
+        if (notInF0) {
+            if (lane < 3 && nb[lane] >= 0) {
+                int h = finsert(S, C.CF, nb[lane], ctl, &fresh);
+                if (fresh && notInSeeds) {
+                    int pos = atomicAdd(&ctl->nBA, 1);
+                    S.bA[pos] = nb[lane];
+                }
+            }
+            __syncwarp();
+            if (notInSeeds) {
+                const double r2 = r * r;
+                int* cur = S.bA;
+                int* nxt = S.bB;
+                int nCur = ctl->nBA;
+                int guard = 0;
+                while (nCur > 0 && ctl->err == 0 && guard++ < 100000) {
+                    if (lane == 0) ctl->nBB = 0;
+                    __syncwarp();
+                    for (int q = lane; q < 3 * nCur; q += 32) {
+                        int f = cur[q / 3], k = q % 3;
+                        int t = M.twin[3 * f + k];
+                        if (t < 0) continue;
+                        int g = t / 3;
+                        if (ffind(S, C.CF, g) >= 0) continue;
+                        bool near = false;
+                        for (int c = 0; c < 3; ++c) {
+                            const double* pv = &M.V[3 * M.F[3 * g + c]];
+                            double dx = src.S[0] - pv[0], dy = src.S[1] - pv[1], dz = src.S[2] - pv[2];
+                            if (!(dx * dx + dy * dy + dz * dz > r2)) near = true;
+                        }
+                        if (!near) continue;
+                        finsert(S, C.CF, g, ctl, &fresh);
+                        if (fresh) {
+                            int pos = atomicAdd(&ctl->nBB, 1);
+                            if (pos < C.CF) nxt[pos] = g;
+                            else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                        }
+                    }
+                    __syncwarp();
+                    nCur = min(ctl->nBB, C.CF);
+                    int* tmp = cur;
+                    cur = nxt;
+                    nxt = tmp;
+                }
+            }
+        }
+        // goal faces (targets) complete the patch
+        for (int t = lane; t < nT; t += 32) finsert(S, C.CF, S.tface[t], ctl, &fresh);
+        __syncwarp();
+    }
+    // target lists per face (full mode: the face table holds only target faces)
+    for (int t = lane; t < nT; t += 32) {
+        int fresh;
+        int h = finsert(S, C.CF, S.tface[t], ctl, &fresh);
+        if (h >= 0) S.tnext[t] = atomicExch(&S.fhead[h], t);
+    }
+    __syncwarp();
+    // ---- source: frame, face-vertex labels, initial windows -------------------------------------------------------
+    const int f0 = src.f0;
+    const double L0 = M.geom[9 * f0], cx0 = M.geom[9 * f0 + 1], cy0 = M.geom[9 * f0 + 2];
+    {
+        const double* p0 = &M.V[3 * M.F[3 * f0]];
+        const double* p1 = &M.V[3 * M.F[3 * f0 + 1]];
+        const double* p2 = &M.V[3 * M.F[3 * f0 + 2]];
+        for (int c = 0; c < 3; ++c) src.e1[c] = (p1[c] - p0[c]) / L0;
+        for (int c = 0; c < 3; ++c) src.e2[c] = (p2[c] - p0[c] - cx0 * src.e1[c]) / cy0;
+    }
+    const double P2[3][2] = {{0, 0}, {L0, 0}, {cx0, cy0}};
+    const double S2x = b0[1] * L0 + b0[2] * cx0, S2y = b0[2] * cy0;
+    VRec rec[3];
+    rec[0].slot = rec[1].slot = rec[2].slot = -1;
+    if (lane < 3) {
+        int k = lane;
+        int v = M.F[3 * f0 + k];
+        double dx = P2[k][0] - S2x, dy = P2[k][1] - S2y;
+        double l = hypot(dx, dy);
+        const double* pv = &M.V[3 * v];
+        double u[3] = {pv[0] - src.S[0], pv[1] - src.S[1], pv[2] - src.S[2]};
+        propose(S, C, ctl, v, sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]), dx / l, dy / l, rec[0]);
+    }
+    __syncwarp();
+    resolve(M, S, C, src, ctl, rec[0]);
+    __syncwarp();
+    if (lane < 3) {
+        int k = lane;
+        int t = M.twin[3 * f0 + k];
+        if (t >= 0) {
+            double L = M.geom[9 * f0 + 3 * k];
+            double skx = b0[(k + 1) % 3] * L + b0[(k + 2) % 3] * M.geom[9 * f0 + 3 * k + 1];
+            double sky = b0[(k + 2) % 3] * M.geom[9 * f0 + 3 * k + 2];
+            Win w;
+            w.he = (t / 3) * 4 + t % 3;
+            w.src = -1;
+            w.sigma = 0;
+            w.sx = L - skx;
+            w.sy = fmin(-sky, -1e-15 * L);
+            w.b0 = 0;
+            w.b1 = L;
+            double ddx = P2[(k + 1) % 3][0] - P2[k][0], ddy = P2[(k + 1) % 3][1] - P2[k][1];
+            double dl = hypot(ddx, ddy);
+            w.c = -ddx / dl;
+            w.s = -ddy / dl;
+            push_win(M, S, C, src, ctl, w);
+        }
+    }
+    __syncwarp();
+    // ---- rounds ---------------------------------------------------------------------------------------------------
+    // the initial windows sit in S.wB (ctl->nB); each round swaps the buffers and processes S.wA into S.wB
+    int processed = 0, launches = 0;
+    int round = 0;
+    while (true) {
+        // pseudo-source launches queued by resolve() run first; their windows join the next round
+        for (int guard = 0;; ++guard) {
+            __syncwarp();
+            int nL = min(ctl->nLA, C.CL);
+            if (nL == 0 || ctl->err) break;
+            if (guard > Lp.maxRounds) {
+                if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
+                break;
+            }
+            __syncwarp();
+            if (lane == 0) ctl->nLA = 0;
+            for (int q = lane; q < nL; q += 32) S.lB[q] = S.lA[q];
+            __syncwarp();
+            for (int q = lane; q < nL; q += 32) {
+                int v = S.lB[q];
+                int h = vfind(S, C.CV, v);
+                double d = bitsd(__ldcg(&S.vlab[h]));
+                double tx = S.vtx[h], ty = S.vty[h];
+                S.ld[3 * q] = d;
+                S.ld[3 * q + 1] = tx;
+                S.ld[3 * q + 2] = ty;
+                launches++;
+                for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
+                    int f = M.vfList[i];
+                    if (!in_domain(M, S, C, src, f)) continue;
+                    int k = 0;
+                    while (M.F[3 * f + k] != v) ++k;
+                    int e = (k + 1) % 3;
+                    VRec r1, r2;
+                    propose(S, C, ctl, M.F[3 * f + e], d + M.geom[9 * f + 3 * k], tx, ty, r1);
+                    propose(S, C, ctl, M.F[3 * f + (k + 2) % 3], d + M.geom[9 * f + 3 * ((k + 2) % 3)], tx, ty, r2);
+                    int t = M.twin[3 * f + e];
+                    if (t < 0) continue;
+                    Win c;
+                    c.he = (t / 3) * 4 + t % 3;
+                    c.src = v;
+                    c.sigma = d;
+                    double L = M.geom[9 * f + 3 * e];
+                    c.sx = L - M.geom[9 * f + 3 * e + 1];
+                    c.sy = -M.geom[9 * f + 3 * e + 2];
+                    c.b0 = 0;
+                    c.b1 = L;
+                    c.c = tx;
+                    c.s = ty;
+                    push_win(M, S, C, src, ctl, c);
+                }
+            }
+            __syncwarp();
+            // second pass: surviving edge-path proposals take the start direction their launcher had
+            for (int q = lane; q < nL; q += 32) {
+                int v = S.lB[q];
+                double d = S.ld[3 * q], tx = S.ld[3 * q + 1], ty = S.ld[3 * q + 2];
+                for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
+                    int f = M.vfList[i];
+                    if (!in_domain(M, S, C, src, f)) continue;
+                    int k = 0;
+                    while (M.F[3 * f + k] != v) ++k;
+                    VRec r;
+                    r.dx = tx;
+                    r.dy = ty;
+                    r.v = M.F[3 * f + (k + 1) % 3];
+                    r.d = d + M.geom[9 * f + 3 * k];
+                    r.slot = vfind(S, C.CV, r.v);
+                    resolve(M, S, C, src, ctl, r);
+                    r.v = M.F[3 * f + (k + 2) % 3];
+                    r.d = d + M.geom[9 * f + 3 * ((k + 2) % 3)];
+                    r.slot = vfind(S, C.CV, r.v);
+                    resolve(M, S, C, src, ctl, r);
+                }
+            }
+        }
+        __syncwarp();
+        int nA = ctl->nB;
+        if (nA > C.CW) nA = C.CW;
+        if (nA == 0 || ctl->err) break;
+        if (++round > Lp.maxRounds) {
+            if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
+            break;
+        }
+        {
+            Win* t = S.wA;
+            S.wA = S.wB;
+            S.wB = t;
+        }
+        __syncwarp();
+        if (lane == 0) ctl->nB = 0;
+        double mk = CUDART_INF;
+        for (int q = lane; q < nA; q += 32) mk = fmin(mk, key_of(S.wA[q]));
+        mk = warp_min(mk);
+        __syncwarp();
+        if (settled(M, S, C, src, nT, mk, lane)) break;
+        const double thr = mk + Lp.delta;
+        for (int base = 0; base < nA; base += 32) {
+            int q = base + lane;
+            VRec r[3];
+            r[0].slot = r[1].slot = r[2].slot = -1;
+            if (q < nA) {
+                Win w = S.wA[q];
+                if (key_of(w) > thr) {
+                    int pos = atomicAdd(&ctl->nB, 1);
+                    if (pos < C.CW) S.wB[pos] = w;
+                    else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                } else {
+                    process(M, S, C, src, ctl, w, r, processed);
+                }
+            }
+            __syncwarp();
+            for (int k = 0; k < 3; ++k) resolve(M, S, C, src, ctl, r[k]);
+            __syncwarp();
+        }
+    }
+    __syncwarp();
+    // ---- results -------------------------------------------------------------------------------------------------
+    const int nLog = min(ctl->nLog, C.CLOG);
+    const int err = ctl->err;
+    if (err == CSSG_ST_CAPACITY && Lp.failList) {
+        // tables too small for this source: queue it for the large-table pass, which writes all its outputs
+        if (lane == 0) {
+            Lp.status[si] = 0;
+            Lp.failList[atomicAdd(Lp.failCount, 1)] = si;
+        }
+        return;
+    }
+    double fx = 0, fy = 0, fz = 0;
+    int inRange = 0;
+    for (int t = lane; t < nT; t += 32) {
+        double ts[3], te[3];
+        double d = err ? CUDART_INF : target_query(M, S, C, src, t, nLog, ts, te);
+        if (d > src.cutoff) {
+            d = CUDART_INF;
+            ts[0] = ts[1] = ts[2] = te[0] = te[1] = te[2] = 0;
+        }
+        if (Lp.searchMode == 0) {
+            int o = S.tidx[t];
+            if (!(d < CUDART_INF) && Lp.patchDisconnected) {
+                d = 2.0 * Lp.maxDist;
+                ts[0] = ts[1] = te[0] = te[1] = 0;
+                ts[2] = te[2] = 1;
+            }
+            Lp.dOut[o] = d;
+            if (Lp.tsOut)
+                for (int c = 0; c < 3; ++c) Lp.tsOut[3 * o + c] = ts[c];
+            if (Lp.teOut)
+                for (int c = 0; c < 3; ++c) Lp.teOut[3 * o + c] = te[c];
+        } else {
+            if (Lp.dOut && t < Lp.pairCap) {
+                size_t o = (size_t)si * Lp.pairCap + t;
+                Lp.dOut[o] = d;
+                Lp.pairJ[o] = S.tidx[t];
+                for (int c = 0; c < 3; ++c) Lp.tsOut[3 * o + c] = ts[c];
+            }
+            if (d < CUDART_INF) {
+                double fm = 0;
+                if (Lp.forceKind == 0) {
+                    if (d <= Lp.sigma) fm = -Lp.k * (Lp.sigma - d);
+                } else {
+                    const double sqrtTwoPi = 2.50662827463100050241576528481104525300698674061;
+                    fm = -(d * Lp.k * exp(-d * d / (2.0 * Lp.sigma * Lp.sigma)) /
+                           ((sqrtTwoPi * Lp.sigma) * sqrt(Lp.sigma)));
+                }
+                fx += fm * ts[0];
+                fy += fm * ts[1];
+                fz += fm * ts[2];
+                if (d <= Lp.sigma) inRange++;
+            }
+        }
+    }
+    if (Lp.force) {
+        fx = warp_sum(fx);
+        fy = warp_sum(fy);
+        fz = warp_sum(fz);
+        if (lane == 0) {
+            Lp.force[3 * si] = fx;
+            Lp.force[3 * si + 1] = fy;
+            Lp.force[3 * si + 2] = fz;
+        }
+    }
+    inRange = warp_sum_i(inRange);
+    processed = warp_sum_i(processed);
+    launches = warp_sum_i(launches);
+    if (lane == 0) {
+        Lp.status[si] = err;
+        cnt[0] += processed;
+        cnt[1] += launches;
+        cnt[2] += inRange;
+        cnt[3] += err ? 1 : 0;
+    }
+}
+
+__device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, int lane)
+{
+    __syncwarp();
+    int nV = min(ctl->nV, C.CV), nF = min(ctl->nF, C.CF);
+    for (int q = lane; q < nV; q += 32) {
+        int h = S.vlist[q];
+        S.vkey[h] = -1;
+        S.vlab[h] = INF_BITS;
+        S.vtok[h] = ~0ull;
+    }
+    for (int q = lane; q < nF; q += 32) {
+        int h = S.flist[q];
+        S.fkey[h] = -1;
+        S.fhead[h] = -1;
+    }
+    if (ctl->nV > C.CV || ctl->nF > C.CF) {
+        // a table overflowed its touched list: clear it whole
+        for (int q = lane; q < C.CV; q += 32) {
+            S.vkey[q] = -1;
+            S.vlab[q] = INF_BITS;
+            S.vtok[q] = ~0ull;
+        }
+        for (int q = lane; q < C.CF; q += 32) {
+            S.fkey[q] = -1;
+            S.fhead[q] = -1;
+        }
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(256) geodesic_kernel(DevMesh M, GeoLaunch L)
+{
+    __shared__ WarpCtl ctls[8];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int warp = blockIdx.x * (blockDim.x >> 5) + wib;
+    if (warp >= L.nSlots) return;
+    WarpCtl* ctl = &ctls[wib];
+    Slot S;
+    carve(L.caps, (char*)L.scratch + (size_t)warp * L.slotBytes, &S);
+    unsigned long long cnt[4] = {0, 0, 0, 0};
+    while (true) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(L.workCounter, 1);
+        item = __shfl_sync(FULL, item, 0);
+        int nItems = L.nSrc;
+        if (L.itemCountDev) nItems = min(nItems, *(volatile const int*)L.itemCountDev);
+        if (item >= nItems) break;
+        int si = L.order ? L.order[item] : item;
+        solve_source(M, L, S, ctl, si, lane, cnt);
+        reset_slot(S, L.caps, ctl, lane);
+    }
+    if (lane == 0 && L.counters) {
+        for (int k = 0; k < 4; ++k)
+            if (cnt[k]) atomicAdd(&L.counters[k], cnt[k]);
+    }
+}
+
+__global__ void init_scratch_kernel(char* scratch, size_t slotBytes, int nSlots, GeoCaps C)
+{
+    int warp = blockIdx.x;
+    if (warp >= nSlots) return;
+    Slot S;
+    carve(C, scratch + (size_t)warp * slotBytes, &S);
+    for (int q = threadIdx.x; q < C.CV; q += blockDim.x) {
+        S.vkey[q] = -1;
+        S.vlab[q] = INF_BITS;
+        S.vtok[q] = ~0ull;
+    }
+    for (int q = threadIdx.x; q < C.CF; q += blockDim.x) {
+        S.fkey[q] = -1;
+        S.fhead[q] = -1;
+    }
+}
+
+__global__ void max_count_kernel(int n, const int* off, int* out)
+{
+    int m = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m = max(m, off[i + 1] - off[i]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULL, m, o));
+    __shared__ int s[32];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int r = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) r = max(r, s[k]);
+        *out = r;
+    }
+}
+
+int next_pow2(long long x)
+{
+    int p = 1;
+    while (p < x && p < (1 << 30)) p <<= 1;
+    return p;
+}
+
+}  // namespace
+
+size_t cssg_geo_slot_bytes(const GeoCaps& c) { return align_up(carve(c, nullptr, nullptr)); }
+
+void cssg_geo_init_scratch(void* scratch, size_t slotBytes, int nSlots, const GeoCaps& c, cudaStream_t s)
+{
+    if (nSlots > 0) init_scratch_kernel<<<nSlots, 256, 0, s>>>((char*)scratch, slotBytes, nSlots, c);
+}
+
+void cssg_launch_geodesic(const DevMesh& M, const GeoLaunch& L, int blocks, cudaStream_t s)
+{
+    geodesic_kernel<<<blocks, 256, 0, s>>>(M, L);
+}
+
+// --------------------------------------------------------------------------------------------------------------------
+// C ABI: batched distance queries (per-source API of triangulatedMeshSpace::distance)
+// --------------------------------------------------------------------------------------------------------------------
+extern "C" int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSrc, const int* src_face,
+                                   const double* src_bary, const int* cand_offsets, const int* cand_face,
+                                   const double* cand_bary, int submesh, double max_dist, const double* threshold,
+                                   double cutoff, double* d_out, double* tstart_out, double* tend_out, int* status)
+{
+    if (!ctx || !mesh || nSrc < 0 || (nSrc > 0 && (!src_face || !src_bary || !cand_offsets || !d_out || !status))) {
+        cssg_set_error("cssg_distance_batch: bad arguments");
+        return CSSG_ERR_ARG;
+    }
+    if (nSrc == 0) return CSSG_OK;
+    cudaStream_t s = ctx->stream;
+    // size the per-warp tables: targets = the largest candidate list, the rest from the domain size
+    int* dmax = nullptr;
+    CSSG_CUDA(cudaMallocAsync((void**)&dmax, sizeof(int), s));
+    max_count_kernel<<<1, 1024, 0, s>>>(nSrc, cand_offsets, dmax);
+    int hmax = 0;
+    CSSG_CUDA(cudaMemcpyAsync(&hmax, dmax, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CSSG_CUDA(cudaStreamSynchronize(s));
+    CSSG_CUDA(cudaFreeAsync(dmax, s));
+    // domain estimate: faces within the cutoff (or the whole mesh)
+    long long est;
+    double reach = cutoff;
+    if (submesh && max_dist < reach) reach = max_dist;
+    if (reach < 1e30) est = (long long)(3.14159 * reach * reach / mesh->meanFaceArea * 4.0) + 64;
+    else est = mesh->d.nF;
+    if (est > mesh->d.nF) est = mesh->d.nF;
+    GeoCaps caps;
+    caps.CT = std::max(32, hmax);
+    caps.CF = next_pow2(4 * (est + caps.CT) + 64);
+    caps.CV = next_pow2(4 * est + 64);
+    caps.CW = (int)std::min<long long>(1 << 22, 16 * est + 1024);
+    caps.CL = (int)std::min<long long>(1 << 20, 2 * est + 256);
+    caps.CLOG = (int)std::min<long long>(1 << 22, 32 * (long long)caps.CT + 16 * est + 1024);
+    size_t slotBytes = cssg_geo_slot_bytes(caps);
+    int dev = ctx->device;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    size_t freeB = 0, totalB = 0;
+    cudaMemGetInfo(&freeB, &totalB);
+    long long nSlots = std::min<long long>((long long)sms * 16, nSrc);
+    long long fit = (long long)(freeB / 4 / slotBytes);
+    if (nSlots > fit) nSlots = std::max<long long>(1, fit);
+    void* scratch = nullptr;
+    int* work = nullptr;
+    unsigned long long* counters = nullptr;
+    CSSG_CUDA(cudaMallocAsync(&scratch, slotBytes * nSlots, s));
+    CSSG_CUDA(cudaMallocAsync((void**)&work, sizeof(int), s));
+    CSSG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
+    cssg_geo_init_scratch(scratch, slotBytes, (int)nSlots, caps, s);
+    GeoLaunch L;
+    memset(&L, 0, sizeof(L));
+    L.nSrc = nSrc;
+    L.srcFace = src_face;
+    L.srcBary = src_bary;
+    L.candOff = cand_offsets;
+    L.candFace = cand_face;
+    L.candBary = cand_bary;
+    L.searchMode = 0;
+    L.submesh = submesh;
+    L.maxDist = max_dist;
+    L.threshold = threshold;
+    L.cutoff = cutoff;
+    L.dOut = d_out;
+    L.tsOut = tstart_out;
+    L.teOut = tend_out;
+    L.status = status;
+    L.patchDisconnected = (submesh && !(cutoff < 1e300)) ? 1 : 0;
+    L.delta = 1e300;
+    L.maxRounds = 1 << 20;
+    L.caps = caps;
+    L.scratch = scratch;
+    L.slotBytes = slotBytes;
+    L.nSlots = (int)nSlots;
+    L.workCounter = work;
+    int blocks = (int)((nSlots + 7) / 8);
+    cssg_launch_geodesic(mesh->d, L, blocks, s);
+    CSSG_CUDA(cudaGetLastError());
+    CSSG_CUDA(cudaFreeAsync(scratch, s));
+    CSSG_CUDA(cudaFreeAsync(work, s));
+    return CSSG_OK;
+}

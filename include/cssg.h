@@ -1,0 +1,146 @@
+/* cssg.h - C ABI of the GB300 (sm_103a) curvedSpaceSim hot path.
+ *
+ * One shared library (curvedspacesim_gb300/_build/libcssg.so) exports these entry points.  All arguments are
+ * plain pointers and sizes; nothing crosses the ABI but C types.  Every function returns an int status
+ * (CSSG_OK = 0); per-item errors (a walk that hit a border, a propagation that ran out of queue capacity) are
+ * reported in caller-provided int arrays with the CSSG_ST_* codes below, never by exceptions.
+ *
+ * Pointers are DEVICE pointers unless the name ends in _host.  A context owns a CUDA stream; every launch goes to
+ * that stream and returns without synchronising unless the comment says otherwise.
+ *
+ * Reference interfaces each entry point replaces are cited as path:line in sussmanLab/curvedSpaceSim.
+ */
+#ifndef CSSG_H
+#define CSSG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ---------------------------------------------------------------------------------------- */
+#define CSSG_OK 0
+#define CSSG_ERR_ARG 1       /* bad argument (null pointer, negative size, non-triangle mesh) */
+#define CSSG_ERR_CUDA 2      /* a CUDA runtime call failed; cssg_last_error() has the message */
+#define CSSG_ERR_ITEMS 3     /* at least one item reported a non-zero per-item status */
+#define CSSG_ERR_CAPACITY 4  /* a fixed-size buffer was too small (see the function) */
+
+/* ---- per-item status codes (walk and propagation) ------------------------------------------------------------ */
+#define CSSG_ST_OK 0
+#define CSSG_ST_BORDER 1           /* walk reached a border of a closed-mesh space (triangulatedMeshSpace.cpp:522-548) */
+#define CSSG_ST_NAN 2              /* barycentric NaN (meshUtilities.cpp:184-195) */
+#define CSSG_ST_VERTEX 3           /* throughVertex found no outgoing face (triangulatedMeshSpace.cpp:339-405) */
+#define CSSG_ST_ITER 4             /* walk exceeded its crossing cap */
+#define CSSG_ST_NO_INTERSECTION 5  /* target outside the face but no edge crossing found (:534-541) */
+#define CSSG_ST_CAPACITY 6         /* propagation queue / table capacity exceeded for this source */
+
+typedef struct cssg_mesh cssg_mesh;     /* device-resident mesh with connectivity and edge frames */
+typedef struct cssg_ctx cssg_ctx;       /* stream + scratch for batched calls; use one per host thread */
+typedef struct cssg_system cssg_system; /* device-resident particle system (model + force + updater state) */
+
+/* Message of the last error on this thread (static storage). */
+const char* cssg_last_error(void);
+/* Library version string. */
+const char* cssg_version(void);
+
+/* ---- mesh ------------------------------------------------------------------------------------------------------
+ * Replaces triangulatedMeshSpace::loadMeshFromFile + updateMeshSpanAndTree (src/models/triangulatedMeshSpace.cpp:6-72):
+ * host arrays vertices_host[3*nV] (x,y,z) and faces_host[3*nF] (counter-clockwise vertex indices; the order also
+ * defines the barycentric order of positions on that face).  Builds adjacency, edge frames, vertex rings, angle
+ * sums and the bounding box on the host and uploads them. */
+int cssg_mesh_create(const double* vertices_host, int nV, const int* faces_host, int nF, int device, cssg_mesh** out);
+int cssg_mesh_destroy(cssg_mesh* mesh);
+/* area (triangulatedMeshSpace::getArea, :153), bbox_host[6] = min xyz, max xyz with the origin included (:6-30). */
+int cssg_mesh_info(const cssg_mesh* mesh, int* nV, int* nF, double* area, double* bbox_host);
+
+/* ---- context ----------------------------------------------------------------------------------------------- */
+/* stream: a cudaStream_t, or NULL to create a private non-blocking stream. */
+int cssg_ctx_create(int device, void* stream, cssg_ctx** out);
+int cssg_ctx_destroy(cssg_ctx* ctx);
+int cssg_ctx_synchronize(cssg_ctx* ctx);
+void* cssg_ctx_stream(cssg_ctx* ctx);
+
+/* ---- walk: triangulatedMeshSpace::transportParticleAndVectors, batched ----------------------------------------
+ * Replaces src/models/triangulatedMeshSpace.cpp:448-564 (plus :247-407, :566-658) called once per particle by
+ * simpleModel::moveParticles (src/models/simpleModel.cpp:44-66).  In place: face[n], bary[3n], disp[3n] (modified
+ * the same way the reference modifies its displacementVector), transport[n*nTransport*3] (vectors carried along,
+ * e.g. velocities).  status[n] gets CSSG_ST_* per particle; crossings (nullable) accumulates the edge+vertex
+ * crossings of the launch in one unsigned long long on the device. */
+int cssg_transport_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int n, int* face, double* bary, double* disp,
+                         double* transport, int nTransport, int* status, unsigned long long* crossings);
+
+/* ---- distances: triangulatedMeshSpace::distance / distanceWithSubmeshing, batched over sources -----------------
+ * Replaces src/models/triangulatedMeshSpace.cpp:155-238 with computePathDistanceAndTangents
+ * (src/utility/meshUtilities.cpp:360-380), called once per source by simpleModel::findNeighbors
+ * (src/models/simpleModel.cpp:68-112).
+ *   sources: src_face[nSrc], src_bary[3*nSrc]
+ *   targets: CSR cand_offsets[nSrc+1] into cand_face[], cand_bary[3*]
+ *   submesh = 0: whole mesh; submesh = 1: the reference's patch (submesher.cpp:55-147) of radius
+ *            min(max_dist, threshold[i]) per source (threshold nullable = +inf)
+ *   cutoff: paths longer than cutoff are not followed; such targets report +inf (use +inf for exact reference
+ *           semantics, where a disconnected patch target reports 2*max_dist and tangent (0,0,1) (:197-203))
+ * Outputs per candidate: d_out[], tstart_out[3*] (unit start tangent at the source), tend_out[3*] (nullable; unit
+ * direction of travel at the target).  status[nSrc]. */
+int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSrc, const int* src_face, const double* src_bary,
+                        const int* cand_offsets, const int* cand_face, const double* cand_bary, int submesh,
+                        double max_dist, const double* threshold, double cutoff, double* d_out, double* tstart_out,
+                        double* tend_out, int* status);
+
+/* ---- particle system: simpleModel + force + updater on the device -------------------------------------------- */
+typedef struct cssg_params {
+    int integrator;      /* 0 velocityVerletNVE (velocityVerletNVE.cpp:3-29), 1 noseHooverNVT (noseHooverNVT.cpp:3-150) */
+    int force_kind;      /* 0 harmonicRepulsion (harmonicRepulsion.cpp:3-34), 1 gaussianRepulsion (gaussianRepulsion.cpp:3-12) */
+    double k;            /* harmonic stiffness / gaussian alpha */
+    double sigma;        /* harmonic range / gaussian width */
+    double range;        /* candidate range (force maximumInteractionRange); <= 0: all-to-all (baseNeighborStructure) */
+    int submesh;         /* 1: per-source reference patches (useSubmeshingRoutines(true, max_dist)) */
+    double max_dist;     /* submesh radius cap */
+    double cutoff;       /* geodesic pruning radius, >= the largest distance a force reads (sigma for harmonic) */
+    double dt;           /* timestep */
+    double temperature;  /* NVT target temperature */
+    double tau;          /* NVT chain time scale */
+    int chain_length;    /* NVT chain length M (default 2) */
+} cssg_params;
+
+int cssg_system_create(cssg_ctx* ctx, const cssg_mesh* mesh, int n, const cssg_params* params, cssg_system** out);
+int cssg_system_destroy(cssg_system* sys);
+/* simpleModel::setParticlePositions (simpleModel.cpp:204-212) + velocities/forces; host arrays; nullable fields
+ * are left unchanged.  Synchronises. */
+int cssg_system_set_state(cssg_system* sys, const int* face_host, const double* bary_host, const double* vel_host,
+                          const double* force_host);
+/* noseHooverNVT::setBathVariables (noseHooverNVT.cpp:28-36): chain masses from N, T, tau; chain at rest.  Called by
+ * cssg_system_create; call again after replacing the particles of an NVT system. */
+int cssg_system_reset_thermostat(cssg_system* sys);
+/* Copies the state to host arrays (nullable) and synchronises. */
+int cssg_system_get_state(cssg_system* sys, int* face_host, double* bary_host, double* vel_host, double* force_host);
+/* Device pointers of the state arrays (face[n], bary[3n], vel[3n], force[3n]). */
+int cssg_system_device_state(cssg_system* sys, int** face, double** bary, double** vel, double** force);
+/* simulation::performTimestep x steps (simulation.cpp:84-95); asynchronous on the context stream.  use_graph=1
+ * replays one captured CUDA graph per step. */
+int cssg_system_step(cssg_system* sys, int steps, int use_graph);
+/* simulation::computeForces (simulation.cpp:61-70 -> baseForce.cpp:12-28): neighbours, geodesics, forces. */
+int cssg_system_compute_forces(cssg_system* sys);
+/* Error summary since the last call (synchronises): OR of (1 << CSSG_ST_*) over walks and sources, and counters
+ * out_host[4] = {walk crossings, windows processed, vertex launches, in-range pairs} (nullable). */
+int cssg_system_check(cssg_system* sys, int* status_bits, unsigned long long* counters_host);
+/* Pair data of the last force evaluation, host arrays with capacity cap: source i, target j, distance, start
+ * tangent (3).  Returns the number of candidate pairs in *count (which may exceed cap). */
+int cssg_system_pairs(cssg_system* sys, int cap, int* i_host, int* j_host, double* d_host, double* t_host, int* count);
+/* Nose-Hoover chain state: (M+1) x 4 bath variables + {kinetic energy, scale factor}, host array. */
+int cssg_system_chain(cssg_system* sys, double* chain_host, int capacity);
+/* Timing of the last step() call: milliseconds of the dominant kernel (geodesic+force) and of the walk, from
+ * CUDA events on the system stream (filled when timing is enabled with cssg_system_timing(sys, 1)). */
+int cssg_system_timing(cssg_system* sys, int enable);
+int cssg_system_last_times(cssg_system* sys, double* ms_host, int capacity);
+/* Number of kernels one step() launches (the integrator's fixed sequence). */
+int cssg_system_kernels_per_step(cssg_system* sys, int* count);
+
+/* ---- diagnostics ------------------------------------------------------------------------------------------------
+ * Measured FP64 fused-multiply-add issue rate of the device (GFLOP/s, 2 flops per FMA), from a register-resident
+ * dependent-chain kernel timed with CUDA events on the context stream; the denominator of the FP64 roofline of the
+ * geodesic kernel.  Synchronises. */
+int cssg_diag_fp64_peak(cssg_ctx* ctx, double* gflops_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CSSG_H */

@@ -1,0 +1,175 @@
+"""GPU parity tests: the CUDA path through the C ABI against the CPU oracle on the same seeded inputs."""
+import math
+
+import numpy as np
+import pytest
+
+from curvedspacesim_gb300 import meshes as ms
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from curvedspacesim_gb300 import api
+    ctx = api.Context(0)
+    return api, ctx
+
+
+def _tangent(V, F, f, rng, scale):
+    N = ms.face_normals(V, F)[f]
+    raw = rng.standard_normal((len(f), 3))
+    d = raw - (raw * N).sum(1, keepdims=True) * N
+    return d * scale
+
+
+@pytest.mark.parametrize("mesh,scale", [("ico4", 0.02), ("ico4", 0.3), ("torus", 0.1), ("torus", 1.5)])
+def test_walk_matches_oracle(gpu, oracle_mod, mesh, scale):
+    api, ctx = gpu
+    rng = np.random.default_rng(100)
+    V, F = ms.icosphere(4) if mesh == "ico4" else ms.torus(200, 100)
+    OM = oracle_mod.OracleMesh(V, F)
+    M = api.Mesh(V, F)
+    n = 4000
+    f, b = ms.area_weighted_positions(V, F, n, rng)
+    disp = _tangent(V, F, f, rng, scale)
+    vel = _tangent(V, F, f, rng, 1.0)
+    fo, bo, do, to, so, co = OM.transport(f, b, disp, vel[:, None, :])
+    fg, bg, dg, tg, sg, cg = api.transport_batch(ctx, M, f, b, disp, vel[:, None, :])
+    assert np.all(so == 0) and np.all(sg == 0)
+    assert cg == int(co.sum()) and cg > 0
+    assert np.array_equal(fg, fo)
+    # edge crossings use the same IEEE operations on both sides (no FMA contraction): bitwise equal
+    np.testing.assert_array_equal(bg, bo)
+    np.testing.assert_array_equal(tg[:, 0], to[:, 0])
+    np.testing.assert_array_equal(dg, do)
+
+
+def test_distances_full_mesh_match_oracle(gpu, oracle_mod):
+    """All-to-all geodesics on the icosphere-4 (N=100): whole mesh, no cutoff (triangulatedMeshSpace::distance)."""
+    api, ctx = gpu
+    rng = np.random.default_rng(1)
+    V, F = ms.icosphere(4)
+    OM = oracle_mod.OracleMesh(V, F)
+    M = api.Mesh(V, F)
+    n = 100
+    f, b = ms.area_weighted_positions(V, F, n, rng)
+    src = np.arange(0, 100, 10)
+    off = [0]
+    cf, cb = [], []
+    for s in src:
+        o = np.array([i for i in range(n) if i != s])
+        cf.append(f[o])
+        cb.append(b[o])
+        off.append(off[-1] + len(o))
+    cf = np.concatenate(cf)
+    cb = np.concatenate(cb)
+    d, ts, te, st = api.distance_batch(ctx, M, f[src], b[src], np.array(off), cf, cb, submesh=False)
+    assert np.all(st == 0)
+    for q, s in enumerate(src):
+        a, e = off[q], off[q + 1]
+        do, tso, teo, _ = OM.distance(f[s], b[s], cf[a:e], cb[a:e])
+        np.testing.assert_allclose(d[a:e], do, rtol=1e-12, atol=1e-13)
+        np.testing.assert_allclose(ts[a:e], tso, atol=1e-9)
+        np.testing.assert_allclose(te[a:e], teo, atol=1e-9)
+
+
+@pytest.mark.parametrize("cutoff", [math.inf, 0.3])
+def test_distances_patch_mode_match_oracle(gpu, oracle_mod, cutoff):
+    """Torus 200x100, N=2000, range 0.3: reference patches (distanceWithSubmeshing)."""
+    api, ctx = gpu
+    rng = np.random.default_rng(2)
+    V, F = ms.torus(200, 100)
+    OM = oracle_mod.OracleMesh(V, F)
+    M = api.Mesh(V, F)
+    n = 2000
+    f, b = ms.area_weighted_positions(V, F, n, rng)
+    off, idx, mc = OM.candidates(f, b, 0.3)
+    d, ts, te, st = api.distance_batch(ctx, M, f, b, off, f[idx], b[idx], submesh=True, max_dist=0.3,
+                                       threshold=mc, cutoff=cutoff)
+    assert np.all(st == 0)
+    do, tso, _ = OM.neighbor_distances(f, b, off, idx, mc, 1, 0.3, cutoff)
+    if not math.isfinite(cutoff):
+        do = np.where(np.isfinite(do), do, 0.6)
+    fin = np.isfinite(do)
+    assert np.array_equal(fin, np.isfinite(d))
+    np.testing.assert_allclose(d[fin], do[fin], rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(ts[fin], tso[fin], atol=1e-9)
+
+
+def _system(api, ctx, V, F, n, seed, integrator, sigma, submesh, range_, dt, T):
+    rng = np.random.default_rng(seed)
+    f, b = ms.area_weighted_positions(V, F, n, rng)
+    vel = ms.tangent_velocities(V, F, f, T if T > 0 else 0.1, rng)
+    M = api.Mesh(V, F)
+    p = api.make_params(integrator, "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=range_, submesh=submesh,
+                        max_dist=sigma, cutoff=sigma, dt=dt, temperature=T)
+    S = api.System(ctx, M, n, p)
+    S.set_state(f, b, vel, np.zeros((n, 3)))
+    return S, f, b, vel
+
+
+def test_nve_all_to_all_matches_oracle(gpu, oracle_mod):
+    """Icosphere-4, N=100, sigma=0.2, all-to-all, velocity Verlet dt=0.005, 100 steps: positions within 1e-5."""
+    api, ctx = gpu
+    V, F = ms.icosphere(4)
+    n, sigma, dt = 100, 0.2, 0.005
+    S, f, b, vel = _system(api, ctx, V, F, n, 1, "nve", sigma, False, 0.0, dt, 0.1)
+    S.step(100, graph=True)
+    bits, cnt = S.check()
+    assert bits == 0, cnt
+    fg, bg, vg, _ = S.get_state()
+    OM = oracle_mod.OracleMesh(V, F)
+    prm = OM.params(0, k=1.0 / sigma ** 2, sigma=sigma, rng=0.0, submesh=0, max_dist=sigma, cutoff=sigma, dt=dt)
+    fo, bo, vo, _, _, err, _ = OM.simulate(0, 100, f, b, vel, np.zeros((n, 3)), prm)
+    assert err == 0
+    err = np.linalg.norm(OM.r3(fg, bg) - OM.r3(fo, bo), axis=1)
+    assert err.max() < 1e-5, err.max()
+    np.testing.assert_allclose(vg, vo, atol=1e-5)
+
+
+def test_nvt_patch_matches_oracle(gpu, oracle_mod):
+    """Torus 200x100, N=2000, sigma=cutoff=0.3, patches, Nose-Hoover T=0.05 dt=0.002: 20 steps."""
+    api, ctx = gpu
+    V, F = ms.torus(200, 100)
+    n, sigma, dt, T = 2000, 0.3, 0.002, 0.05
+    S, f, b, vel = _system(api, ctx, V, F, n, 2, "nvt", sigma, True, sigma, dt, T)
+    S.step(20, graph=True)
+    bits, cnt = S.check()
+    assert bits == 0, cnt
+    fg, bg, vg, _ = S.get_state()
+    OM = oracle_mod.OracleMesh(V, F)
+    prm = OM.params(0, k=1.0 / sigma ** 2, sigma=sigma, rng=sigma, submesh=1, max_dist=sigma, cutoff=sigma, dt=dt,
+                    T=T)
+    fo, bo, vo, _, ch, err, _ = OM.simulate(1, 20, f, b, vel, np.zeros((n, 3)), prm)
+    assert err == 0
+    pe = np.linalg.norm(OM.r3(fg, bg) - OM.r3(fo, bo), axis=1)
+    assert pe.max() < 1e-7, pe.max()
+    np.testing.assert_allclose(vg, vo, atol=1e-7)
+    np.testing.assert_allclose(S.chain(), ch, rtol=1e-9, atol=1e-12)
+
+
+def test_pair_sets_identical(gpu, oracle_mod):
+    api, ctx = gpu
+    V, F = ms.torus(200, 100)
+    n, sigma = 2000, 0.3
+    S, f, b, vel = _system(api, ctx, V, F, n, 3, "nvt", sigma, True, sigma, 0.002, 0.05)
+    S.enable_pairs()
+    S.compute_forces()
+    i, j, d, t = S.pairs()
+    OM = oracle_mod.OracleMesh(V, F)
+    off, idx, mc = OM.candidates(f, b, sigma)
+    do, tso, _ = OM.neighbor_distances(f, b, off, idx, mc, 1, sigma, sigma)
+    gpu_pairs = {(a, c) for a, c, x in zip(i, j, d) if x <= sigma}
+    src = np.repeat(np.arange(n), np.diff(off))
+    ora_pairs = {(a, c) for a, c, x in zip(src, idx, do) if x <= sigma}
+    assert gpu_pairs == ora_pairs
+    gd = {(a, c): x for a, c, x in zip(i, j, d)}
+    for a, c, x in zip(src, idx, do):
+        if np.isfinite(x):
+            assert abs(gd[(a, c)] - x) <= 1e-12 * max(1, x)
+    # forces against the oracle's force evaluation
+    _, _, _, fg = S.get_state()
+    prm = OM.params(0, k=1.0 / sigma ** 2, sigma=sigma, rng=sigma, submesh=1, max_dist=sigma, cutoff=sigma)
+    fo, _, _ = OM.forces(f, b, prm)
+    np.testing.assert_allclose(fg, fo, atol=1e-11)
