@@ -42,6 +42,9 @@ BYTES_PER_FACE = 12 + 12 + 72         # patch face: vertex ids, neighbours, edge
 
 
 def workload_config(name):
+    if name == "batch64":
+        return dict(workload="batch64_uneven_nve_patch", batched=True, n_systems=64, phi=0.4, integrator="nve",
+                    submesh=True, dt=0.002, T=0.1, seed=3)
     if name == "torus_nvt":
         return dict(workload="torus200x100_N2000_nvt_patch", mesh=("torus", 200, 100), n=2000, sigma=0.3,
                     integrator="nvt", submesh=True, range_=0.3, dt=0.002, T=0.05, seed=2)
@@ -49,6 +52,31 @@ def workload_config(name):
         return dict(workload="icosphere4_N100_nve_alltoall", mesh=("ico", 4), n=100, sigma=0.2, integrator="nve",
                     submesh=False, range_=0.0, dt=0.005, T=0.1, seed=1)
     raise SystemExit(f"unknown workload {name}")
+
+
+def build_batch(cfg):
+    """64 independent systems: each an icosphere (subdivision 3-6), a torus grid (50x25 ... 400x200) or an
+    ellipsoid (scaled icosphere, axes U[0.5, 2]); N log-uniform in [50, 5000]; sigma from area fraction 0.4."""
+    rng = np.random.default_rng(cfg["seed"])
+    systems = []
+    for _ in range(cfg["n_systems"]):
+        kind = rng.integers(3)
+        if kind == 0:
+            V, F = ms.icosphere(int(rng.integers(3, 7)))
+            name = "icosphere"
+        elif kind == 1:
+            nu = int(rng.choice([50, 100, 200, 400]))
+            V, F = ms.torus(nu, nu // 2, 3.0, 1.0)
+            name = "torus"
+        else:
+            V, F = ms.ellipsoid(int(rng.integers(3, 7)), rng.uniform(0.5, 2.0, size=3))
+            name = "ellipsoid"
+        n = int(round(math.exp(rng.uniform(math.log(50), math.log(5000)))))
+        sigma = ms.sigma_for_area_fraction(ms.total_area(V, F), n, cfg["phi"])
+        f, b = ms.area_weighted_positions(V, F, n, rng)
+        vel = ms.tangent_velocities(V, F, f, cfg["T"], rng)
+        systems.append(dict(V=V, F=F, n=n, sigma=sigma, f=f, b=b, vel=vel, kind=name))
+    return systems
 
 
 def build_inputs(cfg):
@@ -142,75 +170,77 @@ def max_over_ranks(pg, x):
     return float(t.item())
 
 
+def systems_of(cfg):
+    """The workload as a list of independent systems (one entry for the single-system workloads)."""
+    if cfg.get("batched"):
+        out = build_batch(cfg)
+        for sy in out:
+            sy["range_"] = sy["sigma"]
+        return out
+    V, F, f, b, vel = build_inputs(cfg)
+    return [dict(V=V, F=F, n=cfg["n"], sigma=cfg["sigma"], range_=cfg["range_"], f=f, b=b, vel=vel)]
+
+
+def oracle_step_rate(cfg, systems, threads, budget_s, max_steps=200):
+    """Oracle (CPU restatement of the reference path) on `threads` host threads: particle-steps/s over whole steps
+    of every system, stopping at the first step boundary after budget_s."""
+    import oracle
+    oracle.build()
+    kind = 0 if cfg["integrator"] == "nve" else 1
+    states = []
+    for sy in systems:
+        OM = oracle.OracleMesh(sy["V"], sy["F"])
+        sigma = sy["sigma"]
+        prm = OM.params(0, k=1.0 / sigma ** 2, sigma=sigma, rng=sy["range_"], submesh=int(cfg["submesh"]),
+                        max_dist=sigma, cutoff=sigma, dt=cfg["dt"], T=cfg["T"])
+        states.append([OM, prm, (sy["f"], sy["b"], sy["vel"], np.zeros((sy["n"], 3)), OM.nvt_chain(sy["n"], prm))])
+    ntot = sum(sy["n"] for sy in systems)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        for st in states:
+            OM, prm, state = st
+            out = OM.simulate(kind, 1, *state[:4], prm, chain=state[4], threads=threads)
+            st[2] = out[:5]
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or steps >= max_steps:
+            break
+    return ntot * steps / el, steps
+
+
 def run_reference(args, cfg):
     """CPU oracle (restatement of the reference path) with all host threads, same workload."""
     world, rank, _, pg = dist_setup()
     if rank != 0:
         return
-    import oracle
-    oracle.build()
-    V, F, f, b, vel = build_inputs(cfg)
-    OM = oracle.OracleMesh(V, F)
-    sigma = cfg["sigma"]
-    prm = OM.params(0, k=1.0 / sigma ** 2, sigma=sigma, rng=cfg["range_"], submesh=int(cfg["submesh"]),
-                    max_dist=sigma, cutoff=sigma, dt=cfg["dt"], T=cfg["T"])
-    kind = 0 if cfg["integrator"] == "nve" else 1
+    systems = systems_of(cfg)
     threads = os.cpu_count() or 1
-    force = np.zeros((cfg["n"], 3))
-    chain = OM.nvt_chain(cfg["n"], prm)
-    state = (f, b, vel, force, chain)
-    for _ in range(args.warmup):
-        f2, b2, v2, fo2, ch2, err, _ = OM.simulate(kind, 1, *state[:4], prm, chain=state[4], threads=threads)
-        state = (f2, b2, v2, fo2, ch2)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        f2, b2, v2, fo2, ch2, err, _ = OM.simulate(kind, 1, *state[:4], prm, chain=state[4], threads=threads)
-        state = (f2, b2, v2, fo2, ch2)
-    dt_s = time.perf_counter() - t0
-    value = cfg["n"] * args.steps / dt_s
+    oracle_step_rate(cfg, systems, threads, 0.0, max_steps=args.warmup)  # warm-up
+    value, steps = oracle_step_rate(cfg, systems, threads, 1e30, max_steps=args.steps)
     line = {
         "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * dt_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic",
-        "config": {"workload": cfg["workload"], "n": cfg["n"], "sigma": sigma, "integrator": cfg["integrator"],
-                   "submesh": cfg["submesh"], "l2": "cpu run"},
+        "ms_per_step": 1e3 * sum(sy["n"] for sy in systems) / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": cfg["workload"], "n": sum(sy["n"] for sy in systems), "systems": len(systems),
+                   "integrator": cfg["integrator"], "submesh": cfg["submesh"], "l2": "cpu run"},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} full steps of the workload (oracle restatement; CGAL reference "
-                                   f"not buildable)"},
+                         "sample": f"{steps} full steps of the workload (oracle restatement; CGAL reference not "
+                                   f"buildable)"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline(cfg, seconds_budget=15.0):
-    """Bounded sample of the same workload on the host: the oracle, single-threaded and all threads."""
-    import oracle
-    oracle.build()
-    V, F, f, b, vel = build_inputs(cfg)
-    OM = oracle.OracleMesh(V, F)
-    sigma = cfg["sigma"]
-    prm = OM.params(0, k=1.0 / sigma ** 2, sigma=sigma, rng=cfg["range_"], submesh=int(cfg["submesh"]),
-                    max_dist=sigma, cutoff=sigma, dt=cfg["dt"], T=cfg["T"])
-    kind = 0 if cfg["integrator"] == "nve" else 1
+def cpu_baseline(cfg, systems, seconds_budget=20.0):
+    """Bounded sample of the same workload on the host: the oracle on all threads and on one thread."""
     threads = os.cpu_count() or 1
-    res = {}
-    for th in (threads, 1):
-        steps = 0
-        t0 = time.perf_counter()
-        state = (f, b, vel, np.zeros((cfg["n"], 3)), OM.nvt_chain(cfg["n"], prm))
-        while True:
-            out = OM.simulate(kind, 1, *state[:4], prm, chain=state[4], threads=th)
-            state = out[:5]
-            steps += 1
-            el = time.perf_counter() - t0
-            if el > seconds_budget / 2 or steps >= 200:
-                break
-        res[th] = (cfg["n"] * steps / el, steps)
-    v, steps = res[threads]
-    return {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} steps of the workload on {threads} threads (oracle restatement; CGAL reference not "
-                      f"buildable); single thread: {res[1][0]:.1f} particle-steps/s over {res[1][1]} steps"}
+    v_all, s_all = oracle_step_rate(cfg, systems, threads, seconds_budget / 2)
+    v_one, s_one = oracle_step_rate(cfg, systems, 1, seconds_budget / 2)
+    return {"value": v_all, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{s_all} whole steps of the workload on {threads} threads (oracle restatement; the CGAL "
+                      f"reference is not buildable); single thread: {v_one:.1f} particle-steps/s over {s_one} steps"}
 
 
 def run_ours(args, cfg):
@@ -219,24 +249,35 @@ def run_ours(args, cfg):
     torch.cuda.set_device(local)
     from curvedspacesim_gb300 import api
 
-    V, F, f, b, vel = build_inputs(cfg)
-    n = cfg["n"]
-    sigma = cfg["sigma"]
+    systems = systems_of(cfg)
+    n = sum(sy["n"] for sy in systems)
     ctx = api.Context(local)
-    M = api.Mesh(V, F, device=local)
-    p = api.make_params(cfg["integrator"], "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=cfg["range_"],
-                        submesh=cfg["submesh"], max_dist=sigma, cutoff=sigma, dt=cfg["dt"], temperature=cfg["T"])
-    S = api.System(ctx, M, n, p)
-    S.set_state(f, b, vel, np.zeros((n, 3)))
+    meshes, params = [], []
+    for sy in systems:
+        M = api.Mesh(sy["V"], sy["F"], device=local)
+        sigma = sy["sigma"]
+        meshes.append(M)
+        params.append(api.make_params(cfg["integrator"], "harmonic", k=1.0 / sigma ** 2, sigma=sigma,
+                                      range_=sy["range_"], submesh=cfg["submesh"], max_dist=sigma, cutoff=sigma,
+                                      dt=cfg["dt"], temperature=cfg["T"]))
+    S = api.System(ctx, meshes, [sy["n"] for sy in systems], params)
+    S.set_state(np.concatenate([sy["f"] for sy in systems]), np.concatenate([sy["b"] for sy in systems]),
+                np.concatenate([sy["vel"] for sy in systems]), np.zeros((n, 3)))
     stream = torch.cuda.current_stream()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
     # warm-up (also captures the graph)
-    S.step(max(args.warmup, 1), graph=True)
+    S.step(max(args.warmup, 1), graph=not args.profile)
     torch.cuda.synchronize()
     bits, cnt = S.check()
     if bits:
         raise RuntimeError(f"per-item errors during warm-up: {bits:#x} {cnt}")
+    if args.profile:
+        S.step(1, graph=False)
+        torch.cuda.synchronize()
+        bits, cnt = S.check()
+        print(json.dumps({"profile_run": cfg["workload"], "status_bits": bits, "counters": cnt}), flush=True)
+        return
 
     # ---- value: resident inputs, one graph replay per step, L2 flushed before each step ----
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -253,9 +294,8 @@ def run_ours(args, cfg):
     torch.cuda.synchronize()
     clocks = sampler.stop()
     barrier(pg)
-    ms_steps = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    t_ms = sum(ms_steps)
-    t_ms = max_over_ranks(pg, t_ms)
+    ms_steps = [a.elapsed_time(e) for a, e in zip(starts, ends)]
+    t_ms = max_over_ranks(pg, sum(ms_steps))
     bits, cnt = S.check()
     if bits:
         raise RuntimeError(f"per-item errors in the timed region: {bits:#x} {cnt}")
@@ -278,9 +318,9 @@ def run_ours(args, cfg):
     S.compute_forces()
     _, pj, _, _ = S.pairs()
     cands = len(pj)
-    faces_per_source = float(os.environ.get("CSSG_FACES_PER_SOURCE", "0")) or (
-        math.pi * sigma ** 2 / (M.area / M.nF) * 1.5)
-    geo_bytes = n * BYTES_PER_SOURCE + cands * BYTES_PER_CANDIDATE + n * faces_per_source * BYTES_PER_FACE
+    faces = sum(sy["n"] * min(len(sy["F"]), 1.3 * math.pi * (sy["sigma"] + 0.0) ** 2 /
+                              (ms.total_area(sy["V"], sy["F"]) / len(sy["F"]))) for sy in systems)
+    geo_bytes = n * BYTES_PER_SOURCE + cands * BYTES_PER_CANDIDATE + faces * BYTES_PER_FACE
     geo_flops = windows * FLOPS_PER_WINDOW
     peaks = {}
     try:
@@ -307,21 +347,20 @@ def run_ours(args, cfg):
         S.step(1, graph=True)
         a, bb, c, d = S.get_state()
         hf[:], hb[:], hv[:], hfo[:] = a, bb, c, d
-    e2e_s = time.perf_counter() - t0
-    e2e_s = max_over_ranks(pg, e2e_s)
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
     e2e = world * n * args.steps / e2e_s
     io_bytes = n * (4 + 24 + 24 + 24)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(cfg)
+        cpu = cpu_baseline(cfg, systems)
 
     if rank == 0:
         line = {
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": cfg["workload"], "n": n, "sigma": sigma, "integrator": cfg["integrator"],
+            "config": {"workload": cfg["workload"], "n": n, "systems": len(systems), "integrator": cfg["integrator"],
                        "submesh": cfg["submesh"], "graph": True,
                        "l2": "flushed before every timed step (512 MB write)", "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": io_bytes,
@@ -331,7 +370,7 @@ def run_ours(args, cfg):
                          "frac": achieved_gbs / hbm_peak, "traffic": int(traffic) if traffic else None,
                          "kernel": "geodesic_kernel", "kernel_ms": geo_ms,
                          "algorithmic_bytes_per_launch": geo_bytes,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "of fallback 6.8 TB/s",
                          "fp64": {"achieved_gflops": achieved_fp64, "peak_gflops": fp64_peak,
                                   "frac": achieved_fp64 / fp64_peak, "flops_per_launch": geo_flops,
                                   "windows_per_launch": windows, "peak_source": "measured FMA-chain kernel"}},
@@ -351,6 +390,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="torus_nvt")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="minimal run for ncu: warm-up steps, then one step without graph replay, no other legs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -23,6 +23,8 @@ EXPORTS = [
     "cssg_system_device_state", "cssg_system_step", "cssg_system_compute_forces", "cssg_system_check",
     "cssg_system_pairs", "cssg_system_chain", "cssg_system_timing", "cssg_system_last_times",
     "cssg_system_reset_thermostat", "cssg_system_kernels_per_step", "cssg_diag_fp64_peak",
+    "cssg_system_create_batched", "cssg_mlp_param_count", "cssg_screen_features", "cssg_mlp_infer", "cssg_mlp_grad",
+    "cssg_mlp_adam",
 ]
 
 
@@ -77,8 +79,9 @@ def load(build_if_missing: bool = True):
     L.cssg_ctx_stream.argtypes = [P]
     L.cssg_ctx_stream.restype = P
     L.cssg_transport_batch.argtypes = [P, P, I, P, P, P, P, I, P, P]
-    L.cssg_distance_batch.argtypes = [P, P, I, P, P, P, P, P, I, D, P, D, P, P, P, P]
+    L.cssg_distance_batch.argtypes = [P, P, I, P, P, P, P, P, I, D, P, D, P, P, P, P, P]
     L.cssg_system_create.argtypes = [P, P, I, ctypes.POINTER(cssg_params), PP]
+    L.cssg_system_create_batched.argtypes = [P, I, P, P, P, PP]
     L.cssg_system_destroy.argtypes = [P]
     L.cssg_system_set_state.argtypes = [P, P, P, P, P]
     L.cssg_system_get_state.argtypes = [P, P, P, P, P]
@@ -93,6 +96,11 @@ def load(build_if_missing: bool = True):
     L.cssg_system_reset_thermostat.argtypes = [P]
     L.cssg_system_kernels_per_step.argtypes = [P, P]
     L.cssg_diag_fp64_peak.argtypes = [P, P]
+    L.cssg_mlp_param_count.argtypes = []
+    L.cssg_screen_features.argtypes = [P, P, D, I, P, P, P, P, P, P]
+    L.cssg_mlp_infer.argtypes = [P, P, I, P, P, P]
+    L.cssg_mlp_grad.argtypes = [P, P, P, I, P, P, P]
+    L.cssg_mlp_adam.argtypes = [P, P, P, P, P, I, ctypes.c_float, I]
     for name in EXPORTS:
         fn = getattr(L, name)
         if fn.restype is None and name not in ("cssg_last_error", "cssg_version", "cssg_ctx_stream"):

@@ -122,12 +122,15 @@ def distance_batch(ctx: Context, mesh: Mesh, src_face, src_bary, cand_off, cand_
     ts = torch.zeros((max(m, 1), 3), dtype=torch.float64, device=dev)
     te = torch.zeros((max(m, 1), 3), dtype=torch.float64, device=dev)
     st = torch.zeros(max(ns, 1), dtype=torch.int32, device=dev)
+    stats = torch.zeros((max(ns, 1), 4), dtype=torch.int64, device=dev)
     L = _lib.load()
     check(L.cssg_distance_batch(ctx.h, mesh.h, ns, _P(sf.data_ptr()), _P(sb.data_ptr()), _P(co.data_ptr()),
                                 _P(cf.data_ptr()), _P(cb.data_ptr()), int(bool(submesh)), float(max_dist),
                                 _P(th.data_ptr()) if th is not None else None, float(cutoff), _P(d.data_ptr()),
-                                _P(ts.data_ptr()), _P(te.data_ptr()), _P(st.data_ptr())), "cssg_distance_batch")
+                                _P(ts.data_ptr()), _P(te.data_ptr()), _P(st.data_ptr()), _P(stats.data_ptr())),
+          "cssg_distance_batch")
     ctx.synchronize()
+    distance_batch.last_stats = stats.cpu().numpy()[:ns]
     return d.cpu().numpy()[:m], ts.cpu().numpy()[:m], te.cpu().numpy()[:m], st.cpu().numpy()[:ns]
 
 
@@ -156,13 +159,32 @@ def make_params(integrator="nve", force="harmonic", k=1.0, sigma=1.0, range_=Non
 
 
 class System:
-    """cssg_system: particles, forces and the updater resident on the device."""
+    """cssg_system: particles, forces and the updater resident on the device.
 
-    def __init__(self, ctx: Context, mesh: Mesh, n: int, params: cssg_params):
+    ``mesh``/``n``/``params`` may be lists (one entry per independent system) to batch several systems; state
+    arrays are then the concatenation of the systems' particles."""
+
+    def __init__(self, ctx: Context, mesh, n, params):
         L = _lib.load()
-        self.ctx, self.mesh, self.n, self.params = ctx, mesh, n, params
+        meshes = list(mesh) if isinstance(mesh, (list, tuple)) else [mesh]
+        counts = list(n) if isinstance(n, (list, tuple)) else [n]
+        plist = list(params) if isinstance(params, (list, tuple)) else [params]
+        if not (len(meshes) == len(counts) == len(plist)):
+            raise ValueError("one mesh, count and parameter set per system")
+        self.ctx, self.meshes, self.counts, self.params = ctx, meshes, counts, plist[0]
+        self.mesh = meshes[0]
+        self.K = len(meshes)
+        self.n = int(sum(counts))
         h = ctypes.c_void_p()
-        check(L.cssg_system_create(ctx.h, mesh.h, n, ctypes.byref(params), ctypes.byref(h)), "cssg_system_create")
+        if self.K == 1:
+            check(L.cssg_system_create(ctx.h, meshes[0].h, counts[0], ctypes.byref(plist[0]), ctypes.byref(h)),
+                  "cssg_system_create")
+        else:
+            mh = (ctypes.c_void_p * self.K)(*[m.h.value for m in meshes])
+            cn = (ctypes.c_int * self.K)(*counts)
+            pa = (cssg_params * self.K)(*plist)
+            check(L.cssg_system_create_batched(ctx.h, self.K, mh, cn, pa, ctypes.byref(h)),
+                  "cssg_system_create_batched")
         self.h = h
 
     def __del__(self):
@@ -236,7 +258,7 @@ class System:
         return i, j, d, t
 
     def chain(self):
-        cap = 4 * (max(1, self.params.chain_length) + 1) + 2
+        cap = (4 * (max(1, self.params.chain_length) + 1) + 2) * self.K
         out = np.zeros(cap)
         check(_lib.load().cssg_system_chain(self.h, _np_ptr(out), cap), "cssg_system_chain")
         return out
@@ -248,3 +270,50 @@ class System:
         out = np.zeros(2)
         check(_lib.load().cssg_system_last_times(self.h, _np_ptr(out), 2), "cssg_system_last_times")
         return {"geodesic_ms": float(out[0]), "walk_ms": float(out[1])}
+
+
+# ----------------------------------------------------------------------------------------------------------------
+# learned distance screen
+# ----------------------------------------------------------------------------------------------------------------
+def mlp_param_count() -> int:
+    return int(_lib.load().cssg_mlp_param_count())
+
+
+def screen_features(ctx: Context, mesh: Mesh, sigma: float, pi, pj, face, pos):
+    """Pair features on the device; all inputs torch tensors on the context's device. Returns (X bf16, chord/s)."""
+    torch = _torch()
+    n = int(pi.numel())
+    X = torch.zeros((max(n, 1), 16), dtype=torch.bfloat16, device=pi.device)
+    c = torch.zeros(max(n, 1), dtype=torch.float32, device=pi.device)
+    check(_lib.load().cssg_screen_features(ctx.h, mesh.h, float(sigma), n, _P(pi.data_ptr()), _P(pj.data_ptr()),
+                                           _P(face.data_ptr()), _P(pos.data_ptr()), _P(X.data_ptr()),
+                                           _P(c.data_ptr())), "cssg_screen_features")
+    return X[:n], c[:n]
+
+
+def mlp_infer(ctx: Context, X, params):
+    """Tensor-core inference; X bf16 [n, 16], params float32 [P] (torch, device)."""
+    torch = _torch()
+    n = int(X.shape[0])
+    y = torch.zeros(max(n, 1), dtype=torch.float32, device=X.device)
+    err = torch.zeros(1, dtype=torch.int32, device=X.device)
+    check(_lib.load().cssg_mlp_infer(ctx.h, _P(X.data_ptr()), n, _P(params.data_ptr()), _P(y.data_ptr()),
+                                     _P(err.data_ptr())), "cssg_mlp_infer")
+    ctx.synchronize()
+    if int(err.item()):
+        raise _lib.CssgError("cssg_mlp_infer: tensor-core completion wait timed out")
+    return y[:n]
+
+
+def mlp_grad(ctx: Context, X, y, params):
+    torch = _torch()
+    g = torch.zeros(mlp_param_count(), dtype=torch.float32, device=X.device)
+    loss = torch.zeros(1, dtype=torch.float32, device=X.device)
+    check(_lib.load().cssg_mlp_grad(ctx.h, _P(X.data_ptr()), _P(y.data_ptr()), int(X.shape[0]),
+                                    _P(params.data_ptr()), _P(g.data_ptr()), _P(loss.data_ptr())), "cssg_mlp_grad")
+    return g, loss
+
+
+def mlp_adam(ctx: Context, params, grad, m, v, batch: int, lr: float, step: int):
+    check(_lib.load().cssg_mlp_adam(ctx.h, _P(params.data_ptr()), _P(grad.data_ptr()), _P(m.data_ptr()),
+                                    _P(v.data_ptr()), int(batch), ctypes.c_float(lr), int(step)), "cssg_mlp_adam")

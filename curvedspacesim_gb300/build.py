@@ -2,7 +2,8 @@
 
 Each .cu file is compiled by its own nvcc process (in parallel), then linked with ``nvcc -shared``.  The walk's
 translation unit is compiled with ``-fmad=false`` so its edge-crossing arithmetic matches the CPU restatement
-operation for operation.
+operation for operation; host code (mesh preprocessing) is compiled with ``-ffp-contract=off`` for the same reason
+(aarch64 g++ would otherwise fuse multiply-adds in the edge frames and normals).
 """
 from __future__ import annotations
 
@@ -17,9 +18,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(OUT_DIR, "libcssg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off",
+          "--expt-relaxed-constexpr"]
 PER_FILE = {"walk.cu": ["-fmad=false"]}
-SOURCES = ["mesh.cu", "walk.cu", "geodesic.cu", "system.cu", "diag.cu"]
+SOURCES = ["mesh.cu", "walk.cu", "geodesic.cu", "system.cu", "diag.cu", "mlp.cu"]
 
 
 def nvcc() -> str:

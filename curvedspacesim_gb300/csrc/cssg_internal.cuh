@@ -19,6 +19,7 @@ struct DevMesh {
     const int* ringStart;       // nV + 1: clockwise neighbour ring of closed vertices (throughVertex order)
     const int* ringV;
     const unsigned char* vflag; // bit0 closed ring available, bit1 border vertex, bit2 saddle (angle sum > 2 pi)
+    const float* fcurv;         // 3 nF: per face mean curvature, Gaussian curvature, mean edge length (screen features)
     double bbMin[3], bbMax[3];
 };
 
@@ -26,6 +27,7 @@ enum { VF_RING = 1, VF_BORDER = 2, VF_SADDLE = 4 };
 
 struct cssg_mesh {
     DevMesh d;
+    DevMesh* dself;  // device copy of d (kernels that serve several meshes index arrays of DevMesh)
     int device;
     double area;
     double meanEdge;
@@ -51,9 +53,12 @@ int cssg_cuda_fail(cudaError_t e, const char* what);
 // ---- walk (walk.cu) ----------------------------------------------------------------------------------------------
 // Launches the batched transport kernel; pos_out (nullable) receives the final R3 positions, crossings (nullable)
 // accumulates the launch's crossings.
-void cssg_launch_transport(const DevMesh& M, int n, int* face, double* bary, double* disp, double* transport, int nT,
-                           int* status, unsigned long long* crossings, double* pos_out, cudaStream_t s);
-void cssg_launch_positions(const DevMesh& M, int n, const int* face, const double* bary, double* pos, cudaStream_t s);
+// meshes: device array of meshes; meshOf (nullable): per-particle index into it (null: all on meshes[0])
+void cssg_launch_transport(const DevMesh* meshes, const int* meshOf, int n, int* face, double* bary, double* disp,
+                           double* transport, int nT, int* status, unsigned long long* crossings, double* pos_out,
+                           cudaStream_t s);
+void cssg_launch_positions(const DevMesh* meshes, const int* meshOf, int n, const int* face, const double* bary,
+                           double* pos, cudaStream_t s);
 
 // ---- geodesics (geodesic.cu) -------------------------------------------------------------------------------------
 struct GeoCaps {
@@ -65,8 +70,30 @@ struct GeoCaps {
     int CLOG;  // target-face window log entries
 };
 
+// One independent system (mesh + interaction parameters + its slice of the particle and cell arrays).  A launch
+// serves any number of them: sources carry their system index.
+struct SysDesc {
+    DevMesh mesh;
+    int searchMode;   // 0 CSR candidate lists (distance API), 1 cell list, 2 all-to-all
+    int bigBin;       // patches too large for the regular tables: sources go straight to the large-table pass
+    int submesh;      // reference patches
+    int forceKind;    // 0 harmonic, 1 gaussian
+    int partBase;     // first particle of this system
+    int nPart;
+    int cellBase;     // first cell of this system's grid in the shared cell arrays
+    int nc[3];
+    double cs[3];
+    double lo[3];
+    double range2;    // candidate test: chord^2 < range2
+    double maxDist;   // patch radius cap
+    double cutoff;    // paths longer than this are not followed
+    double k, sigma;  // force parameters
+};
+
 // Per-launch configuration of the fused neighbour / geodesic / force kernel.
 struct GeoLaunch {
+    const SysDesc* sys;          // device array of systems
+    const int* sysOf;            // nullable: system of each particle (null: all in sys[0])
     // sources
     int nSrc;
     const int* srcFace;
@@ -77,22 +104,13 @@ struct GeoLaunch {
     const int* candOff;
     const int* candFace;
     const double* candBary;
-    // ... or neighbour search mode (system): particles + cell list
-    int searchMode;              // 0 CSR, 1 cell list, 2 all-to-all
-    int nPart;
+    const double* threshold;     // nullable (CSR mode): per-source patch radius
+    // ... or neighbour search (system mode): all particles + the shared cell arrays
     const int* partFace;
     const double* partBary;
     const double* partPos;
     const int* cellStart;        // totalCells + 1
     const int* cellList;         // particle indices sorted by cell (stable)
-    int nc[3];
-    double cs[3];
-    double range2;               // candidate test: chord^2 < range2
-    // domain
-    int submesh;
-    double maxDist;
-    const double* threshold;     // nullable (CSR mode)
-    double cutoff;
     // outputs
     double* dOut;                // per candidate (CSR mode) or per pair slot (system mode, nullable)
     double* tsOut;
@@ -101,13 +119,13 @@ struct GeoLaunch {
     int* pairCount;              // system mode: candidates per source (nullable)
     int pairCap;                 // system mode: pair slots per source
     double* force;               // system mode: force per source (nullable)
-    int forceKind;
-    double k, sigma;
     int* status;                 // per source
+    long long* stats;            // nullable: per source {windows processed, launches, rounds, targets}
     unsigned long long* counters;  // [0] windows processed, [1] vertex launches, [2] in-range pairs, [3] capacity hits
     int patchDisconnected;       // CSR mode with cutoff = inf: unreached -> 2*maxDist, tangent (0,0,1)
-    double delta;                // bucket width of the propagation order (inf = plain rounds)
-    int maxRounds;
+    double delta;                // band width of the distance-ordered rounds
+    int maxRounds;               // per-source caps: exceeding either reports CSSG_ST_CAPACITY
+    int maxWindows;
     // scratch
     GeoCaps caps;
     void* scratch;
@@ -117,9 +135,12 @@ struct GeoLaunch {
     const int* itemCountDev;     // nullable: number of work items read from the device (retry pass)
     int* failList;               // nullable: sources whose tables overflowed are queued here for a retry pass
     int* failCount;
+    int smemTables;              // set by cssg_launch_geodesic: hash tables in shared memory
 };
 
 size_t cssg_geo_slot_bytes(const GeoCaps& c);
+// shared memory one warp's hash tables need (tables go to global scratch when this exceeds the block budget)
+size_t cssg_geo_smem_per_warp(const GeoCaps& c);
 // Fills slots with their initial (empty) state; call once after allocating the scratch.
 void cssg_geo_init_scratch(void* scratch, size_t slotBytes, int nSlots, const GeoCaps& c, cudaStream_t s);
-void cssg_launch_geodesic(const DevMesh& M, const GeoLaunch& L, int blocks, cudaStream_t s);
+void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s);

@@ -47,6 +47,15 @@ struct __align__(16) Win {
     int src;  // -1: the source, else the vertex pseudo-source
 };
 
+// loads of table entries other lanes may be writing (shared-memory tables: plain volatile loads)
+__device__ __forceinline__ int ldv(const int* p) { return *(const volatile int*)p; }
+__device__ __forceinline__ unsigned long long ldv(const unsigned long long* p)
+{
+    return *(const volatile unsigned long long*)p;
+}
+
+__device__ __forceinline__ double len2(double x, double y) { return sqrt(x * x + y * y); }
+
 __device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
 __device__ __forceinline__ double bitsd(unsigned long long b)
 {
@@ -54,7 +63,7 @@ __device__ __forceinline__ double bitsd(unsigned long long b)
 }
 
 struct WarpCtl {
-    int nA, nB, nLA, nLB, nLog, nV, nF, nT, err, nBA, nBB, pad;
+    int nA, nB, nLA, nLB, nLog, nV, nF, nT, err, nBA, nBB, nProc;
 };
 
 struct Slot {
@@ -69,6 +78,7 @@ struct Slot {
     double* vtx;
     double* vty;
     unsigned long long* vtok;
+    unsigned long long* vlaunched;  // label bits a vertex was last launched with
     int* vlist;
     int* fkey;
     int* fhead;
@@ -99,12 +109,13 @@ __host__ __device__ inline size_t carve(const GeoCaps& c, char* base, Slot* S)
     CARVE(tbest, unsigned long long, c.CT);
     CARVE(vkey, int, c.CV);
     CARVE(vlab, unsigned long long, c.CV);
+    CARVE(fkey, int, c.CF);
+    CARVE(fhead, int, c.CF);
     CARVE(vtx, double, c.CV);
     CARVE(vty, double, c.CV);
     CARVE(vtok, unsigned long long, c.CV);
+    CARVE(vlaunched, unsigned long long, c.CV);
     CARVE(vlist, int, c.CV);
-    CARVE(fkey, int, c.CF);
-    CARVE(fhead, int, c.CF);
     CARVE(flist, int, c.CF);
     CARVE(wA, Win, c.CW);
     CARVE(wB, Win, c.CW);
@@ -118,6 +129,21 @@ __host__ __device__ inline size_t carve(const GeoCaps& c, char* base, Slot* S)
     return o;
 }
 
+// the probed hash tables live in shared memory when they fit (else in the global slot): vertex labels (key, label
+// bits) and faces (key, target-list head)
+__host__ __device__ inline size_t smem_per_warp(const GeoCaps& c)
+{
+    return (size_t)c.CV * 8 + (size_t)c.CV * 4 + (size_t)c.CF * 8;
+}
+
+__device__ inline void carve_smem(const GeoCaps& c, char* base, Slot* S)
+{
+    S->vlab = (unsigned long long*)base;
+    S->vkey = (int*)(base + (size_t)c.CV * 8);
+    S->fkey = (int*)(base + (size_t)c.CV * 12);
+    S->fhead = (int*)(base + (size_t)c.CV * 12 + (size_t)c.CF * 4);
+}
+
 __device__ __forceinline__ unsigned hash_int(int k) { return (unsigned)k * 2654435761u; }
 
 // ---- hash tables ----------------------------------------------------------------------------------------------
@@ -125,7 +151,7 @@ __device__ int vfind(const Slot& S, int CV, int v)
 {
     unsigned h = hash_int(v) & (CV - 1);
     for (int p = 0; p < CV; ++p) {
-        int k = __ldcg(&S.vkey[h]);
+        int k = ldv(&S.vkey[h]);
         if (k == v) return (int)h;
         if (k == -1) return -1;
         h = (h + 1) & (CV - 1);
@@ -137,7 +163,7 @@ __device__ int vinsert(const Slot& S, int CV, int v, WarpCtl* ctl)
 {
     unsigned h = hash_int(v) & (CV - 1);
     for (int p = 0; p < CV; ++p) {
-        int k = __ldcg(&S.vkey[h]);
+        int k = ldv(&S.vkey[h]);
         if (k == v) return (int)h;
         if (k == -1) {
             int old = atomicCAS(&S.vkey[h], -1, v);
@@ -158,7 +184,7 @@ __device__ int ffind(const Slot& S, int CF, int f)
 {
     unsigned h = hash_int(f) & (CF - 1);
     for (int p = 0; p < CF; ++p) {
-        int k = __ldcg(&S.fkey[h]);
+        int k = ldv(&S.fkey[h]);
         if (k == f) return (int)h;
         if (k == -1) return -1;
         h = (h + 1) & (CF - 1);
@@ -172,7 +198,7 @@ __device__ int finsert(const Slot& S, int CF, int f, WarpCtl* ctl, int* fresh)
     *fresh = 0;
     unsigned h = hash_int(f) & (CF - 1);
     for (int p = 0; p < CF; ++p) {
-        int k = __ldcg(&S.fkey[h]);
+        int k = ldv(&S.fkey[h]);
         if (k == f) return (int)h;
         if (k == -1) {
             int old = atomicCAS(&S.fkey[h], -1, f);
@@ -194,7 +220,7 @@ __device__ int finsert(const Slot& S, int CF, int f, WarpCtl* ctl, int* fresh)
 __device__ __forceinline__ double vlabel(const Slot& S, int CV, int v)
 {
     int h = vfind(S, CV, v);
-    return h < 0 ? CUDART_INF : bitsd(__ldcg(&S.vlab[h]));
+    return h < 0 ? CUDART_INF : bitsd(ldv(&S.vlab[h]));
 }
 
 // ---- per-source solver state ----------------------------------------------------------------------------------
@@ -214,8 +240,8 @@ struct VRec {
 __device__ __forceinline__ double key_of(const Win& w)
 {
     double m;
-    if (w.sx < w.b0) m = hypot(w.sx - w.b0, w.sy);
-    else if (w.sx > w.b1) m = hypot(w.sx - w.b1, w.sy);
+    if (w.sx < w.b0) m = len2(w.sx - w.b0, w.sy);
+    else if (w.sx > w.b1) m = len2(w.sx - w.b1, w.sy);
     else m = fabs(w.sy);
     return w.sigma + m;
 }
@@ -235,7 +261,7 @@ __device__ bool trim(const DevMesh& M, const Slot& S, const GeoCaps& C, Win& w)
     double dA = vlabel(S, C.CV, A);
     if (dA < CUDART_INF) {
         double a = dA - w.sigma;
-        double fb0 = hypot(w.b0 - w.sx, w.sy) - a - w.b0;
+        double fb0 = len2(w.b0 - w.sx, w.sy) - a - w.b0;
         if (fb0 > 0) {
             if (a + w.sx <= 0) return false;
             double xs = (w.sx * w.sx + w.sy * w.sy - a * a) / (2.0 * (a + w.sx));
@@ -247,7 +273,7 @@ __device__ bool trim(const DevMesh& M, const Slot& S, const GeoCaps& C, Win& w)
     if (dB < CUDART_INF) {
         double a = dB - w.sigma;
         double sxm = L - w.sx, xm = L - w.b1;
-        double fb1 = hypot(xm - sxm, w.sy) - a - xm;
+        double fb1 = len2(xm - sxm, w.sy) - a - xm;
         if (fb1 > 0) {
             if (a + sxm <= 0) return false;
             double xs = (sxm * sxm + w.sy * w.sy - a * a) / (2.0 * (a + sxm));
@@ -258,7 +284,7 @@ __device__ bool trim(const DevMesh& M, const Slot& S, const GeoCaps& C, Win& w)
     double dC = vlabel(S, C.CV, Cv);
     if (dC < CUDART_INF) {
         double cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
-        double m0 = hypot(cx - w.b0, cy), m1 = hypot(cx - w.b1, cy);
+        double m0 = len2(cx - w.b0, cy), m1 = len2(cx - w.b1, cy);
         if (dC + fmax(m0, m1) < key_of(w)) return false;
     }
     return w.b1 - w.b0 > 1e-14 * L;
@@ -284,7 +310,7 @@ __device__ __forceinline__ void start_dir(const Win& w, double px, double py, do
 {
     if (w.sigma == 0) {
         double ux = px - w.sx, uy = py - w.sy;
-        double l = hypot(ux, uy);
+        double l = len2(ux, uy);
         ux /= l;
         uy /= l;
         dx = w.c * ux - w.s * uy;
@@ -327,7 +353,7 @@ __device__ void resolve(const DevMesh& M, const Slot& S, const GeoCaps& C, const
 {
     if (r.slot < 0) return;
     unsigned long long b = dbits(r.d);
-    if (__ldcg(&S.vlab[r.slot]) != b) return;
+    if (ldv(&S.vlab[r.slot]) != b) return;
     S.vtx[r.slot] = r.dx;
     S.vty[r.slot] = r.dy;
     if (r.d <= src.cutoff && launchable(M, S, C, src, r.v)) {
@@ -346,6 +372,7 @@ __device__ void process(const DevMesh& M, const Slot& S, const GeoCaps& C, const
     rec[0].slot = rec[1].slot = rec[2].slot = -1;
     if (!trim(M, S, C, w)) return;
     processed++;
+    atomicAdd(&ctl->nProc, 1);
     const int g = w.he >> 2, j = w.he & 3;
     const double L = M.geom[9 * g + 3 * j], cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
     const int A = M.F[3 * g + j], B = M.F[3 * g + (j + 1) % 3], Cv = M.F[3 * g + (j + 2) % 3];
@@ -353,7 +380,7 @@ __device__ void process(const DevMesh& M, const Slot& S, const GeoCaps& C, const
     // targets in g: log the window for the final query and update the running bests (early exit)
     int fh = ffind(S, C.CF, g);
     if (fh >= 0) {
-        int head = __ldcg(&S.fhead[fh]);
+        int head = ldv(&S.fhead[fh]);
         if (head >= 0) {
             int pos = atomicAdd(&ctl->nLog, 1);
             if (pos < C.CLOG) S.wlog[pos] = w;
@@ -363,7 +390,7 @@ __device__ void process(const DevMesh& M, const Slot& S, const GeoCaps& C, const
                 double px = b1 * L + b2 * cx, py = b2 * cy;
                 double xp = w.sx + (px - w.sx) * (-w.sy) / (py - w.sy);
                 if (xp >= w.b0 - tol && xp <= w.b1 + tol) {
-                    double d = w.sigma + hypot(px - w.sx, py - w.sy);
+                    double d = w.sigma + len2(px - w.sx, py - w.sy);
                     atomicMin(&S.tbest[t], dbits(d));
                 }
             }
@@ -373,22 +400,22 @@ __device__ void process(const DevMesh& M, const Slot& S, const GeoCaps& C, const
     if (xC >= w.b0 - tol && xC <= w.b1 + tol) {
         double dx, dy;
         start_dir(w, cx, cy, dx, dy);
-        propose(S, C, ctl, Cv, w.sigma + hypot(cx - w.sx, cy - w.sy), dx, dy, rec[0]);
+        propose(S, C, ctl, Cv, w.sigma + len2(cx - w.sx, cy - w.sy), dx, dy, rec[0]);
     }
     if (w.b0 <= tol) {
         double dx, dy;
         start_dir(w, 0, 0, dx, dy);
-        propose(S, C, ctl, A, w.sigma + hypot(w.sx, w.sy), dx, dy, rec[1]);
+        propose(S, C, ctl, A, w.sigma + len2(w.sx, w.sy), dx, dy, rec[1]);
     }
     if (w.b1 >= L - tol) {
         double dx, dy;
         start_dir(w, L, 0, dx, dy);
-        propose(S, C, ctl, B, w.sigma + hypot(L - w.sx, w.sy), dx, dy, rec[2]);
+        propose(S, C, ctl, B, w.sigma + len2(L - w.sx, w.sy), dx, dy, rec[2]);
     }
     if (w.b0 < xC) {  // exit through edge C->A (local j+2); child frame: origin A, x toward C
         int t = M.twin[3 * g + (j + 2) % 3];
         if (t >= 0) {
-            double n = hypot(cx, cy);
+            double n = len2(cx, cy);
             double ux = cx / n, uy = cy / n;
             double isx = ux * w.sx + uy * w.sy, isy = -uy * w.sx + ux * w.sy;
             Win c;
@@ -420,7 +447,7 @@ __device__ void process(const DevMesh& M, const Slot& S, const GeoCaps& C, const
         int t = M.twin[3 * g + (j + 1) % 3];
         if (t >= 0) {
             double bx = L - cx, by = -cy;
-            double n = hypot(bx, by);
+            double n = len2(bx, by);
             double ux = bx / n, uy = by / n;
             double rx = w.sx - cx, ry = w.sy - cy;
             double isx = ux * rx + uy * ry, isy = -uy * rx + ux * ry;
@@ -510,7 +537,7 @@ __device__ double target_query(const DevMesh& M, const Slot& S, const GeoCaps& C
         double xp = w.sx + (px - w.sx) * (-w.sy) / (py - w.sy);
         const double tol = 1e-12 * L;
         if (xp >= w.b0 - tol && xp <= w.b1 + tol) {
-            double d = w.sigma + hypot(px - w.sx, py - w.sy);
+            double d = w.sigma + len2(px - w.sx, py - w.sy);
             if (d < best) {
                 best = d;
                 start_dir(w, px, py, bdx, bdy);
@@ -527,7 +554,7 @@ __device__ double target_query(const DevMesh& M, const Slot& S, const GeoCaps& C
         const double* PA = &M.V[3 * M.F[3 * g + j]];
         const double* PB = &M.V[3 * M.F[3 * g + (j + 1) % 3]];
         const double* PC = &M.V[3 * M.F[3 * g + (j + 2) % 3]];
-        double ul = hypot(bux, buy);
+        double ul = len2(bux, buy);
         for (int c = 0; c < 3; ++c) {
             double ex = (PB[c] - PA[c]) / L;
             double ey = (PC[c] - PA[c] - cx * ex) / cy;
@@ -538,7 +565,7 @@ __device__ double target_query(const DevMesh& M, const Slot& S, const GeoCaps& C
         int v = M.F[3 * f + c];
         int h = vfind(S, C.CV, v);
         if (h < 0) continue;
-        double lab = bitsd(__ldcg(&S.vlab[h]));
+        double lab = bitsd(ldv(&S.vlab[h]));
         if (!(lab < CUDART_INF)) continue;
         const double* pv = &M.V[3 * v];
         double u[3] = {P[0] - pv[0], P[1] - pv[1], P[2] - pv[2]};
@@ -569,7 +596,7 @@ __device__ bool settled(const DevMesh& M, const Slot& S, const GeoCaps& C, const
             int v = M.F[3 * S.tface[t] + c];
             int h = vfind(S, C.CV, v);
             if (h < 0) continue;
-            double lab = bitsd(__ldcg(&S.vlab[h]));
+            double lab = bitsd(ldv(&S.vlab[h]));
             if (!(lab < CUDART_INF)) continue;
             const double* pv = &M.V[3 * v];
             double u[3] = {P[0] - pv[0], P[1] - pv[1], P[2] - pv[2]};
@@ -581,23 +608,32 @@ __device__ bool settled(const DevMesh& M, const Slot& S, const GeoCaps& C, const
 }
 
 // The per-source solve (whole warp).  Returns the number of targets; leaves results in the slot.
-__device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, int lane,
-                             unsigned long long* cnt)
+__device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, int lane, unsigned long long* cnt)
 {
     const GeoCaps& C = Lp.caps;
+    const SysDesc& D = Lp.sys[Lp.sysOf ? Lp.sysOf[si] : 0];
+    const DevMesh& M = D.mesh;
+    if (D.bigBin && Lp.failList) {
+        // binned to the large-table pass
+        if (lane == 0) {
+            Lp.status[si] = 0;
+            Lp.failList[atomicAdd(Lp.failCount, 1)] = si;
+        }
+        return;
+    }
     Src src;
     src.f0 = Lp.srcFace[si];
-    src.cutoff = Lp.cutoff;
+    src.cutoff = D.cutoff;
     double b0[3] = {Lp.srcBary[3 * si], Lp.srcBary[3 * si + 1], Lp.srcBary[3 * si + 2]};
     load_pt(M, src.f0, b0, src.S);
     if (lane == 0) {
         ctl->nA = ctl->nB = ctl->nLA = ctl->nLB = ctl->nLog = ctl->nV = ctl->nF = ctl->nT = ctl->err = 0;
-        ctl->nBA = ctl->nBB = 0;
+        ctl->nBA = ctl->nBB = ctl->nProc = 0;
     }
     __syncwarp();
     // ---- targets ---------------------------------------------------------------------------------------------
     double maxChord2 = 0;
-    if (Lp.searchMode == 0) {
+    if (D.searchMode == 0) {
         int beg = Lp.candOff[si], nT = Lp.candOff[si + 1] - beg;
         if (nT > C.CT) {
             if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
@@ -620,7 +656,7 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
                 const double* Pj = &Lp.partPos[3 * jj];
                 double dx = Pi[0] - Pj[0], dy = Pi[1] - Pj[1], dz = Pi[2] - Pj[2];
                 d2 = dx * dx + dy * dy + dz * dz;
-                take = (Lp.searchMode == 2) || (d2 < Lp.range2);
+                take = (D.searchMode == 2) || (d2 < D.range2);
             }
             unsigned m = __ballot_sync(FULL, take);
             if (take) {
@@ -634,18 +670,18 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
             }
             count += __popc(m);
         };
-        if (Lp.searchMode == 2) {
-            for (int base = 0; base < Lp.nPart; base += 32) consider(base + lane, base + lane < Lp.nPart);
+        if (D.searchMode == 2) {
+            for (int base = 0; base < D.nPart; base += 32) consider(D.partBase + base + lane, base + lane < D.nPart);
         } else {
             int ci[3];
             for (int c = 0; c < 3; ++c) {
-                int q = (int)floor((Pi[c] - M.bbMin[c]) / Lp.cs[c]);
-                ci[c] = max(0, min(Lp.nc[c] - 1, q));
+                int q = (int)floor((Pi[c] - D.lo[c]) / D.cs[c]);
+                ci[c] = max(0, min(D.nc[c] - 1, q));
             }
-            for (int xx = max(0, ci[0] - 1); xx <= min(Lp.nc[0] - 1, ci[0] + 1); ++xx)
-                for (int yy = max(0, ci[1] - 1); yy <= min(Lp.nc[1] - 1, ci[1] + 1); ++yy)
-                    for (int zz = max(0, ci[2] - 1); zz <= min(Lp.nc[2] - 1, ci[2] + 1); ++zz) {
-                        int cell = xx + Lp.nc[0] * (yy + Lp.nc[1] * zz);
+            for (int xx = max(0, ci[0] - 1); xx <= min(D.nc[0] - 1, ci[0] + 1); ++xx)
+                for (int yy = max(0, ci[1] - 1); yy <= min(D.nc[1] - 1, ci[1] + 1); ++yy)
+                    for (int zz = max(0, ci[2] - 1); zz <= min(D.nc[2] - 1, ci[2] + 1); ++zz) {
+                        int cell = D.cellBase + xx + D.nc[0] * (yy + D.nc[1] * zz);
                         int a = Lp.cellStart[cell], b = Lp.cellStart[cell + 1];
                         for (int base = a; base < b; base += 32) {
                             int q = base + lane;
@@ -684,16 +720,16 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
     }
     __syncwarp();
     // ---- domain: whole mesh or the reference patch ---------------------------------------------------------------
-    src.full = !Lp.submesh;
-    double r = Lp.maxDist;
-    if (Lp.searchMode == 0) {
+    src.full = !D.submesh;
+    double r = D.maxDist;
+    if (D.searchMode == 0) {
         if (Lp.threshold && Lp.threshold[si] < r) r = Lp.threshold[si];
     } else {
         double mc = sqrt(maxChord2);
-        if (Lp.searchMode == 2) mc = 1e20;
+        if (D.searchMode == 2) mc = 1e20;
         if (mc < r) r = mc;
     }
-    if (Lp.submesh) {
+    if (D.submesh) {
         int fresh;
         bool notInF0 = false, notInSeeds = false;
         int nb[3];
@@ -727,7 +763,8 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
                 int* nxt = S.bB;
                 int nCur = ctl->nBA;
                 int guard = 0;
-                while (nCur > 0 && ctl->err == 0 && guard++ < 100000) {
+                while (nCur > 0 && guard++ < 100000) {
+                    __syncwarp();  // every lane has read nCur / err before lane 0 resets the counter
                     if (lane == 0) ctl->nBB = 0;
                     __syncwarp();
                     for (int q = lane; q < 3 * nCur; q += 32) {
@@ -751,7 +788,7 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
                         }
                     }
                     __syncwarp();
-                    nCur = min(ctl->nBB, C.CF);
+                    nCur = ctl->err ? 0 : min(ctl->nBB, C.CF);
                     int* tmp = cur;
                     cur = nxt;
                     nxt = tmp;
@@ -787,7 +824,7 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
         int k = lane;
         int v = M.F[3 * f0 + k];
         double dx = P2[k][0] - S2x, dy = P2[k][1] - S2y;
-        double l = hypot(dx, dy);
+        double l = len2(dx, dy);
         const double* pv = &M.V[3 * v];
         double u[3] = {pv[0] - src.S[0], pv[1] - src.S[1], pv[2] - src.S[2]};
         propose(S, C, ctl, v, sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]), dx / l, dy / l, rec[0]);
@@ -811,7 +848,7 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
             w.b0 = 0;
             w.b1 = L;
             double ddx = P2[(k + 1) % 3][0] - P2[k][0], ddy = P2[(k + 1) % 3][1] - P2[k][1];
-            double dl = hypot(ddx, ddy);
+            double dl = len2(ddx, ddy);
             w.c = -ddx / dl;
             w.s = -ddy / dl;
             push_win(M, S, C, src, ctl, w);
@@ -819,86 +856,18 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
     }
     __syncwarp();
     // ---- rounds ---------------------------------------------------------------------------------------------------
-    // the initial windows sit in S.wB (ctl->nB); each round swaps the buffers and processes S.wA into S.wB
+    // Distance-banded rounds: each round takes the smallest key among queued windows and queued pseudo-source
+    // launches (mk) and handles only what lies within mk + delta, deferring the rest, so labels are close to final
+    // when they are used (a breadth-first order would relaunch border and saddle vertices in cascades).  The initial
+    // windows sit in S.wB (ctl->nB); each round swaps the buffers and processes S.wA into S.wB.
     int processed = 0, launches = 0;
     int round = 0;
     while (true) {
-        // pseudo-source launches queued by resolve() run first; their windows join the next round
-        for (int guard = 0;; ++guard) {
-            __syncwarp();
-            int nL = min(ctl->nLA, C.CL);
-            if (nL == 0 || ctl->err) break;
-            if (guard > Lp.maxRounds) {
-                if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
-                break;
-            }
-            __syncwarp();
-            if (lane == 0) ctl->nLA = 0;
-            for (int q = lane; q < nL; q += 32) S.lB[q] = S.lA[q];
-            __syncwarp();
-            for (int q = lane; q < nL; q += 32) {
-                int v = S.lB[q];
-                int h = vfind(S, C.CV, v);
-                double d = bitsd(__ldcg(&S.vlab[h]));
-                double tx = S.vtx[h], ty = S.vty[h];
-                S.ld[3 * q] = d;
-                S.ld[3 * q + 1] = tx;
-                S.ld[3 * q + 2] = ty;
-                launches++;
-                for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
-                    int f = M.vfList[i];
-                    if (!in_domain(M, S, C, src, f)) continue;
-                    int k = 0;
-                    while (M.F[3 * f + k] != v) ++k;
-                    int e = (k + 1) % 3;
-                    VRec r1, r2;
-                    propose(S, C, ctl, M.F[3 * f + e], d + M.geom[9 * f + 3 * k], tx, ty, r1);
-                    propose(S, C, ctl, M.F[3 * f + (k + 2) % 3], d + M.geom[9 * f + 3 * ((k + 2) % 3)], tx, ty, r2);
-                    int t = M.twin[3 * f + e];
-                    if (t < 0) continue;
-                    Win c;
-                    c.he = (t / 3) * 4 + t % 3;
-                    c.src = v;
-                    c.sigma = d;
-                    double L = M.geom[9 * f + 3 * e];
-                    c.sx = L - M.geom[9 * f + 3 * e + 1];
-                    c.sy = -M.geom[9 * f + 3 * e + 2];
-                    c.b0 = 0;
-                    c.b1 = L;
-                    c.c = tx;
-                    c.s = ty;
-                    push_win(M, S, C, src, ctl, c);
-                }
-            }
-            __syncwarp();
-            // second pass: surviving edge-path proposals take the start direction their launcher had
-            for (int q = lane; q < nL; q += 32) {
-                int v = S.lB[q];
-                double d = S.ld[3 * q], tx = S.ld[3 * q + 1], ty = S.ld[3 * q + 2];
-                for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
-                    int f = M.vfList[i];
-                    if (!in_domain(M, S, C, src, f)) continue;
-                    int k = 0;
-                    while (M.F[3 * f + k] != v) ++k;
-                    VRec r;
-                    r.dx = tx;
-                    r.dy = ty;
-                    r.v = M.F[3 * f + (k + 1) % 3];
-                    r.d = d + M.geom[9 * f + 3 * k];
-                    r.slot = vfind(S, C.CV, r.v);
-                    resolve(M, S, C, src, ctl, r);
-                    r.v = M.F[3 * f + (k + 2) % 3];
-                    r.d = d + M.geom[9 * f + 3 * ((k + 2) % 3)];
-                    r.slot = vfind(S, C.CV, r.v);
-                    resolve(M, S, C, src, ctl, r);
-                }
-            }
-        }
         __syncwarp();
-        int nA = ctl->nB;
-        if (nA > C.CW) nA = C.CW;
-        if (nA == 0 || ctl->err) break;
-        if (++round > Lp.maxRounds) {
+        const int nA = min(ctl->nB, C.CW);
+        const int nP = min(ctl->nLA, C.CL);
+        if (ctl->err || (nA == 0 && nP == 0)) break;
+        if (++round > Lp.maxRounds || ctl->nProc > Lp.maxWindows) {
             if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
             break;
         }
@@ -907,14 +876,91 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
             S.wA = S.wB;
             S.wB = t;
         }
+        for (int q = lane; q < nP; q += 32) S.lB[q] = S.lA[q];
         __syncwarp();
-        if (lane == 0) ctl->nB = 0;
+        if (lane == 0) {
+            ctl->nB = 0;
+            ctl->nLA = 0;
+        }
         double mk = CUDART_INF;
         for (int q = lane; q < nA; q += 32) mk = fmin(mk, key_of(S.wA[q]));
+        for (int q = lane; q < nP; q += 32) mk = fmin(mk, vlabel(S, C.CV, S.lB[q]));
         mk = warp_min(mk);
         __syncwarp();
         if (settled(M, S, C, src, nT, mk, lane)) break;
         const double thr = mk + Lp.delta;
+        // pseudo-source launches within the band (pass 1: windows + edge-path proposals); the rest stay queued
+        for (int q = lane; q < nP; q += 32) {
+            int v = S.lB[q];
+            int h = vfind(S, C.CV, v);
+            S.ld[3 * q] = -1.0;
+            if (h < 0) continue;
+            unsigned long long lb = ldv(&S.vlab[h]);
+            double d = bitsd(lb);
+            if (d > thr) {
+                int pos = atomicAdd(&ctl->nLA, 1);
+                if (pos < C.CL) S.lA[pos] = v;
+                else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                continue;
+            }
+            if (atomicExch(&S.vlaunched[h], lb) == lb) continue;  // already launched with this label
+            double tx = S.vtx[h], ty = S.vty[h];
+            S.ld[3 * q] = d;
+            S.ld[3 * q + 1] = tx;
+            S.ld[3 * q + 2] = ty;
+            launches++;
+            for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
+                int f = M.vfList[i];
+                if (!in_domain(M, S, C, src, f)) continue;
+                int k = 0;
+                while (M.F[3 * f + k] != v) ++k;
+                int e = (k + 1) % 3;
+                VRec r1, r2;
+                propose(S, C, ctl, M.F[3 * f + e], d + M.geom[9 * f + 3 * k], tx, ty, r1);
+                propose(S, C, ctl, M.F[3 * f + (k + 2) % 3], d + M.geom[9 * f + 3 * ((k + 2) % 3)], tx, ty, r2);
+                int t = M.twin[3 * f + e];
+                if (t < 0) continue;
+                Win c;
+                c.he = (t / 3) * 4 + t % 3;
+                c.src = v;
+                c.sigma = d;
+                double L = M.geom[9 * f + 3 * e];
+                c.sx = L - M.geom[9 * f + 3 * e + 1];
+                c.sy = -M.geom[9 * f + 3 * e + 2];
+                c.b0 = 0;
+                c.b1 = L;
+                c.c = tx;
+                c.s = ty;
+                push_win(M, S, C, src, ctl, c);
+            }
+        }
+        __syncwarp();
+        // pass 2: surviving edge-path proposals take the start direction their launcher had
+        for (int q = lane; q < nP; q += 32) {
+            double d = S.ld[3 * q];
+            if (d < 0) continue;
+            int v = S.lB[q];
+            double tx = S.ld[3 * q + 1], ty = S.ld[3 * q + 2];
+            for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
+                int f = M.vfList[i];
+                if (!in_domain(M, S, C, src, f)) continue;
+                int k = 0;
+                while (M.F[3 * f + k] != v) ++k;
+                VRec r;
+                r.dx = tx;
+                r.dy = ty;
+                r.v = M.F[3 * f + (k + 1) % 3];
+                r.d = d + M.geom[9 * f + 3 * k];
+                r.slot = vfind(S, C.CV, r.v);
+                resolve(M, S, C, src, ctl, r);
+                r.v = M.F[3 * f + (k + 2) % 3];
+                r.d = d + M.geom[9 * f + 3 * ((k + 2) % 3)];
+                r.slot = vfind(S, C.CV, r.v);
+                resolve(M, S, C, src, ctl, r);
+            }
+        }
+        __syncwarp();
+        // windows within the band
         for (int base = 0; base < nA; base += 32) {
             int q = base + lane;
             VRec r[3];
@@ -955,10 +1001,10 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
             d = CUDART_INF;
             ts[0] = ts[1] = ts[2] = te[0] = te[1] = te[2] = 0;
         }
-        if (Lp.searchMode == 0) {
+        if (D.searchMode == 0) {
             int o = S.tidx[t];
             if (!(d < CUDART_INF) && Lp.patchDisconnected) {
-                d = 2.0 * Lp.maxDist;
+                d = 2.0 * D.maxDist;
                 ts[0] = ts[1] = te[0] = te[1] = 0;
                 ts[2] = te[2] = 1;
             }
@@ -976,17 +1022,17 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
             }
             if (d < CUDART_INF) {
                 double fm = 0;
-                if (Lp.forceKind == 0) {
-                    if (d <= Lp.sigma) fm = -Lp.k * (Lp.sigma - d);
+                if (D.forceKind == 0) {
+                    if (d <= D.sigma) fm = -D.k * (D.sigma - d);
                 } else {
                     const double sqrtTwoPi = 2.50662827463100050241576528481104525300698674061;
-                    fm = -(d * Lp.k * exp(-d * d / (2.0 * Lp.sigma * Lp.sigma)) /
-                           ((sqrtTwoPi * Lp.sigma) * sqrt(Lp.sigma)));
+                    fm = -(d * D.k * exp(-d * d / (2.0 * D.sigma * D.sigma)) /
+                           ((sqrtTwoPi * D.sigma) * sqrt(D.sigma)));
                 }
                 fx += fm * ts[0];
                 fy += fm * ts[1];
                 fz += fm * ts[2];
-                if (d <= Lp.sigma) inRange++;
+                if (d <= D.sigma) inRange++;
             }
         }
     }
@@ -1003,6 +1049,12 @@ __device__ void solve_source(const DevMesh& M, const GeoLaunch& Lp, Slot S, Warp
     inRange = warp_sum_i(inRange);
     processed = warp_sum_i(processed);
     launches = warp_sum_i(launches);
+    if (lane == 0 && Lp.stats) {
+        Lp.stats[4 * si] = processed;
+        Lp.stats[4 * si + 1] = launches;
+        Lp.stats[4 * si + 2] = round;
+        Lp.stats[4 * si + 3] = nT;
+    }
     if (lane == 0) {
         Lp.status[si] = err;
         cnt[0] += processed;
@@ -1021,6 +1073,7 @@ __device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, int la
         S.vkey[h] = -1;
         S.vlab[h] = INF_BITS;
         S.vtok[h] = ~0ull;
+        S.vlaunched[h] = ~0ull;
     }
     for (int q = lane; q < nF; q += 32) {
         int h = S.flist[q];
@@ -1033,6 +1086,7 @@ __device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, int la
             S.vkey[q] = -1;
             S.vlab[q] = INF_BITS;
             S.vtok[q] = ~0ull;
+            S.vlaunched[q] = ~0ull;
         }
         for (int q = lane; q < C.CF; q += 32) {
             S.fkey[q] = -1;
@@ -1042,9 +1096,10 @@ __device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, int la
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(256) geodesic_kernel(DevMesh M, GeoLaunch L)
+__global__ void __launch_bounds__(256) geodesic_kernel(GeoLaunch L)
 {
     __shared__ WarpCtl ctls[8];
+    extern __shared__ __align__(16) char dyn[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int warp = blockIdx.x * (blockDim.x >> 5) + wib;
@@ -1052,6 +1107,18 @@ __global__ void __launch_bounds__(256) geodesic_kernel(DevMesh M, GeoLaunch L)
     WarpCtl* ctl = &ctls[wib];
     Slot S;
     carve(L.caps, (char*)L.scratch + (size_t)warp * L.slotBytes, &S);
+    if (L.smemTables) {
+        carve_smem(L.caps, dyn + (size_t)wib * smem_per_warp(L.caps), &S);
+        for (int q = lane; q < L.caps.CV; q += 32) {
+            S.vkey[q] = -1;
+            S.vlab[q] = INF_BITS;
+        }
+        for (int q = lane; q < L.caps.CF; q += 32) {
+            S.fkey[q] = -1;
+            S.fhead[q] = -1;
+        }
+    }
+    __syncwarp();
     unsigned long long cnt[4] = {0, 0, 0, 0};
     while (true) {
         int item = 0;
@@ -1061,7 +1128,7 @@ __global__ void __launch_bounds__(256) geodesic_kernel(DevMesh M, GeoLaunch L)
         if (L.itemCountDev) nItems = min(nItems, *(volatile const int*)L.itemCountDev);
         if (item >= nItems) break;
         int si = L.order ? L.order[item] : item;
-        solve_source(M, L, S, ctl, si, lane, cnt);
+        solve_source(L, S, ctl, si, lane, cnt);
         reset_slot(S, L.caps, ctl, lane);
     }
     if (lane == 0 && L.counters) {
@@ -1077,9 +1144,10 @@ __global__ void init_scratch_kernel(char* scratch, size_t slotBytes, int nSlots,
     Slot S;
     carve(C, scratch + (size_t)warp * slotBytes, &S);
     for (int q = threadIdx.x; q < C.CV; q += blockDim.x) {
+        S.vtok[q] = ~0ull;
+        S.vlaunched[q] = ~0ull;
         S.vkey[q] = -1;
         S.vlab[q] = INF_BITS;
-        S.vtok[q] = ~0ull;
     }
     for (int q = threadIdx.x; q < C.CF; q += blockDim.x) {
         S.fkey[q] = -1;
@@ -1118,9 +1186,26 @@ void cssg_geo_init_scratch(void* scratch, size_t slotBytes, int nSlots, const Ge
     if (nSlots > 0) init_scratch_kernel<<<nSlots, 256, 0, s>>>((char*)scratch, slotBytes, nSlots, c);
 }
 
-void cssg_launch_geodesic(const DevMesh& M, const GeoLaunch& L, int blocks, cudaStream_t s)
+size_t cssg_geo_smem_per_warp(const GeoCaps& c) { return smem_per_warp(c); }
+
+void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
 {
-    geodesic_kernel<<<blocks, 256, 0, s>>>(M, L);
+    const size_t per = smem_per_warp(L.caps);
+    const size_t budget = 200 * 1024;
+    int wpb = 8;
+    size_t smem = 0;
+    L.smemTables = per <= budget ? 1 : 0;
+    if (L.smemTables) {
+        wpb = (int)std::min<size_t>(8, budget / per);
+        smem = per * wpb;
+        static size_t configured = 48 * 1024;
+        if (smem > configured) {
+            cudaFuncSetAttribute(geodesic_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
+            configured = budget;
+        }
+    }
+    int blocks = (L.nSlots + wpb - 1) / wpb;
+    geodesic_kernel<<<blocks, 32 * wpb, smem, s>>>(L);
 }
 
 // --------------------------------------------------------------------------------------------------------------------
@@ -1129,7 +1214,8 @@ void cssg_launch_geodesic(const DevMesh& M, const GeoLaunch& L, int blocks, cuda
 extern "C" int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSrc, const int* src_face,
                                    const double* src_bary, const int* cand_offsets, const int* cand_face,
                                    const double* cand_bary, int submesh, double max_dist, const double* threshold,
-                                   double cutoff, double* d_out, double* tstart_out, double* tend_out, int* status)
+                                   double cutoff, double* d_out, double* tstart_out, double* tend_out, int* status,
+                                   long long* stats)
 {
     if (!ctx || !mesh || nSrc < 0 || (nSrc > 0 && (!src_face || !src_bary || !cand_offsets || !d_out || !status))) {
         cssg_set_error("cssg_distance_batch: bad arguments");
@@ -1145,19 +1231,25 @@ extern "C" int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSr
     CSSG_CUDA(cudaMemcpyAsync(&hmax, dmax, sizeof(int), cudaMemcpyDeviceToHost, s));
     CSSG_CUDA(cudaStreamSynchronize(s));
     CSSG_CUDA(cudaFreeAsync(dmax, s));
-    // domain estimate: faces within the cutoff (or the whole mesh)
+    // domain estimate: faces within reach of the source (patch radius or cutoff), or the whole mesh
     long long est;
     double reach = cutoff;
     if (submesh && max_dist < reach) reach = max_dist;
-    if (reach < 1e30) est = (long long)(3.14159 * reach * reach / mesh->meanFaceArea * 4.0) + 64;
-    else est = mesh->d.nF;
+    if (reach < 1e30) {
+        double r = reach + mesh->meanEdge;
+        est = (long long)(1.3 * 3.14159265 * r * r / mesh->meanFaceArea) + 32;
+    } else {
+        est = mesh->d.nF;
+    }
     if (est > mesh->d.nF) est = mesh->d.nF;
+    long long estV = std::min<long long>(mesh->d.nV, est / 2 + 4 * (long long)std::sqrt((double)est) + 16);
     GeoCaps caps;
     caps.CT = std::max(32, hmax);
-    caps.CF = next_pow2(4 * (est + caps.CT) + 64);
-    caps.CV = next_pow2(4 * est + 64);
+    // whole mesh: the face table holds only target faces; patch: the patch plus the goal faces
+    caps.CF = submesh ? next_pow2(2 * (est + caps.CT) + 64) : next_pow2(2 * caps.CT + 64);
+    caps.CV = next_pow2(2 * estV + 64);
     caps.CW = (int)std::min<long long>(1 << 22, 16 * est + 1024);
-    caps.CL = (int)std::min<long long>(1 << 20, 2 * est + 256);
+    caps.CL = (int)std::min<long long>(1 << 20, 2 * estV + 256);
     caps.CLOG = (int)std::min<long long>(1 << 22, 32 * (long long)caps.CT + 16 * est + 1024);
     size_t slotBytes = cssg_geo_slot_bytes(caps);
     int dev = ctx->device;
@@ -1175,34 +1267,43 @@ extern "C" int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSr
     CSSG_CUDA(cudaMallocAsync((void**)&work, sizeof(int), s));
     CSSG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
     cssg_geo_init_scratch(scratch, slotBytes, (int)nSlots, caps, s);
+    SysDesc hd;
+    memset(&hd, 0, sizeof(hd));
+    hd.mesh = mesh->d;
+    hd.searchMode = 0;
+    hd.submesh = submesh;
+    hd.maxDist = max_dist;
+    hd.cutoff = cutoff;
+    SysDesc* dsys = nullptr;
+    CSSG_CUDA(cudaMallocAsync((void**)&dsys, sizeof(SysDesc), s));
+    CSSG_CUDA(cudaMemcpyAsync(dsys, &hd, sizeof(SysDesc), cudaMemcpyHostToDevice, s));
     GeoLaunch L;
     memset(&L, 0, sizeof(L));
+    L.sys = dsys;
     L.nSrc = nSrc;
     L.srcFace = src_face;
     L.srcBary = src_bary;
     L.candOff = cand_offsets;
     L.candFace = cand_face;
     L.candBary = cand_bary;
-    L.searchMode = 0;
-    L.submesh = submesh;
-    L.maxDist = max_dist;
     L.threshold = threshold;
-    L.cutoff = cutoff;
+    L.stats = stats;
     L.dOut = d_out;
     L.tsOut = tstart_out;
     L.teOut = tend_out;
     L.status = status;
     L.patchDisconnected = (submesh && !(cutoff < 1e300)) ? 1 : 0;
-    L.delta = 1e300;
-    L.maxRounds = 1 << 20;
+    L.delta = mesh->meanEdge;
+    L.maxRounds = 1 << 16;
+    L.maxWindows = (int)std::min<long long>(1 << 30, 400 * est + 100000);
     L.caps = caps;
     L.scratch = scratch;
     L.slotBytes = slotBytes;
     L.nSlots = (int)nSlots;
     L.workCounter = work;
-    int blocks = (int)((nSlots + 7) / 8);
-    cssg_launch_geodesic(mesh->d, L, blocks, s);
+    cssg_launch_geodesic(L, s);
     CSSG_CUDA(cudaGetLastError());
+    CSSG_CUDA(cudaFreeAsync(dsys, s));
     CSSG_CUDA(cudaFreeAsync(scratch, s));
     CSSG_CUDA(cudaFreeAsync(work, s));
     return CSSG_OK;

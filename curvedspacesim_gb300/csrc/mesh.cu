@@ -29,6 +29,8 @@ extern "C" const char* cssg_version(void) { return "cssg 0.1 (sm_103a)"; }
 
 namespace {
 
+inline double twoPiConst() { return 6.283185307179586; }
+
 template <typename T>
 int upload(const std::vector<T>& h, T** d, void** keep)
 {
@@ -178,6 +180,46 @@ extern "C" int cssg_mesh_create(const double* V, int nV, const int* F, int nF, i
     for (int v = nV - 1; v >= 0; --v)
         if (!(vflag[v] & VF_RING)) ringStart[v] = ringStart[v + 1];
 
+    // per-face curvature features: mean curvature from the dihedral angles of its three edges
+    // (H_f = sum_e theta_e L_e / (4 A_f), theta signed positive where the surface bends away from the normal) and
+    // Gaussian curvature as the mean angle defect of its vertices over their barycentric areas
+    std::vector<float> fcurv(3 * (size_t)nF, 0.0f);
+    {
+        std::vector<double> varea(nV, 0.0);
+        for (int f = 0; f < nF; ++f) {
+            double a = 0;
+            for (int k = 0; k < 3; ++k) a = geom[9 * f + 3 * k] * geom[9 * f + 3 * k + 2] * 0.5;
+            for (int k = 0; k < 3; ++k) varea[F[3 * f + k]] += a / 3.0;
+        }
+        for (int f = 0; f < nF; ++f) {
+            double A = geom[9 * f] * geom[9 * f + 2] * 0.5;
+            double H = 0, Kg = 0, el = 0;
+            for (int k = 0; k < 3; ++k) {
+                int t = twin[3 * f + k];
+                double L = geom[9 * f + 3 * k];
+                el += L / 3.0;
+                if (t >= 0) {
+                    int g = t / 3;
+                    const double* n1 = &N[3 * f];
+                    const double* n2 = &N[3 * g];
+                    double c = n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2];
+                    c = c > 1 ? 1 : (c < -1 ? -1 : c);
+                    double th = std::acos(c);
+                    // convex edge: the neighbour's far vertex lies below this face's plane
+                    const double* q = &V[3 * F[3 * g + (t % 3 + 2) % 3]];
+                    const double* p0 = &V[3 * F[3 * f + k]];
+                    double side = (q[0] - p0[0]) * n1[0] + (q[1] - p0[1]) * n1[1] + (q[2] - p0[2]) * n1[2];
+                    H += (side <= 0 ? th : -th) * L;
+                }
+                int v = F[3 * f + k];
+                Kg += (twoPiConst() - angle[v]) / (varea[v] > 0 ? varea[v] : 1.0) / 3.0;
+            }
+            fcurv[3 * f] = (float)(H / (4.0 * A));
+            fcurv[3 * f + 1] = (float)Kg;
+            fcurv[3 * f + 2] = (float)el;
+        }
+    }
+
     cssg_mesh* m = new cssg_mesh();
     memset(m->buffers, 0, sizeof(m->buffers));
     m->device = device;
@@ -202,11 +244,13 @@ extern "C" int cssg_mesh_create(const double* V, int nV, const int* F, int nF, i
     double *dV, *dN, *dG;
     int *dF, *dT, *dVS, *dVL, *dRS, *dRV;
     unsigned char* dVF;
+    float* dFC;
     if ((rc = upload(hv, &dV, &m->buffers[0])) || (rc = upload(hf, &dF, &m->buffers[1])) ||
         (rc = upload(twin, &dT, &m->buffers[2])) || (rc = upload(N, &dN, &m->buffers[3])) ||
         (rc = upload(geom, &dG, &m->buffers[4])) || (rc = upload(vfStart, &dVS, &m->buffers[5])) ||
         (rc = upload(vfList, &dVL, &m->buffers[6])) || (rc = upload(ringStart, &dRS, &m->buffers[7])) ||
-        (rc = upload(ringV, &dRV, &m->buffers[8])) || (rc = upload(vflag, &dVF, &m->buffers[9]))) {
+        (rc = upload(ringV, &dRV, &m->buffers[8])) || (rc = upload(vflag, &dVF, &m->buffers[9])) ||
+        (rc = upload(fcurv, &dFC, &m->buffers[11]))) {
         cssg_mesh_destroy(m);
         return rc;
     }
@@ -220,6 +264,18 @@ extern "C" int cssg_mesh_create(const double* V, int nV, const int* F, int nF, i
     d.ringStart = dRS;
     d.ringV = dRV;
     d.vflag = dVF;
+    d.fcurv = dFC;
+    {
+        DevMesh* ds = nullptr;
+        cudaError_t e = cudaMalloc((void**)&ds, sizeof(DevMesh));
+        if (e == cudaSuccess) e = cudaMemcpy(ds, &d, sizeof(DevMesh), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cssg_mesh_destroy(m);
+            return cssg_cuda_fail(e, "mesh descriptor upload");
+        }
+        m->dself = ds;
+        m->buffers[10] = ds;
+    }
     *out = m;
     return CSSG_OK;
 }

@@ -82,24 +82,19 @@ __global__ void scan_add(int* out, int n, const int* blockSums)
     if (i < n) out[i] += blockSums[i / (SCAN_BLOCK * SCAN_ITEMS)];
 }
 
-// ---- cell list ------------------------------------------------------------------------------------------------
-struct Grid {
-    int nc[3];
-    double cs[3];
-    double lo[3];
-};
-
-__global__ void cell_assign(int n, const double* __restrict__ pos, Grid G, int* __restrict__ cellOf,
-                            int* __restrict__ count)
+// ---- cell list (one grid per system, concatenated) -------------------------------------------------------------
+__global__ void cell_assign(int n, const double* __restrict__ pos, const SysDesc* __restrict__ sys,
+                            const int* __restrict__ sysOf, int* __restrict__ cellOf, int* __restrict__ count)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const SysDesc& D = sys[sysOf ? sysOf[i] : 0];
     int ci[3];
     for (int c = 0; c < 3; ++c) {
-        int q = (int)floor((pos[3 * i + c] - G.lo[c]) / G.cs[c]);
-        ci[c] = max(0, min(G.nc[c] - 1, q));
+        int q = (int)floor((pos[3 * i + c] - D.lo[c]) / D.cs[c]);
+        ci[c] = max(0, min(D.nc[c] - 1, q));
     }
-    int cell = ci[0] + G.nc[0] * (ci[1] + G.nc[1] * ci[2]);
+    int cell = D.cellBase + ci[0] + D.nc[0] * (ci[1] + D.nc[1] * ci[2]);
     cellOf[i] = cell;
     atomicAdd(&count[cell], 1);
 }
@@ -152,18 +147,15 @@ __global__ void nve_second_half(int n, double* __restrict__ v, const double* __r
     v[i] += 0.5 * dt * f[i];
 }
 
-// chain layout: (M+1) x {pos, vel, accel, mass}, then kineticEnergy, scale
-__global__ void nh_chain(double* ch, int Mc, double T, double dt, const double* partials, int nPartials)
+// One thread per system: noseHooverNVT::propagateChain.  Chain k occupies len = 4 (M+1) + 2 doubles:
+// (M+1) x {pos, vel, accel, mass}, then kineticEnergy, scale.
+__global__ void nh_chain(double* chains, int K, int Mc, double T, double dt)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double* bv = ch;
-    double& KE = ch[4 * (Mc + 1)];
-    double& scale = ch[4 * (Mc + 1) + 1];
-    if (partials) {
-        double s = 0;
-        for (int b = 0; b < nPartials; ++b) s += partials[b];
-        KE = s;
-    }
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    double* bv = chains + (size_t)k * (4 * (Mc + 1) + 2);
+    double& KE = bv[4 * (Mc + 1)];
+    double& scale = bv[4 * (Mc + 1) + 1];
     const double dt2 = 0.5 * dt, dt4 = 0.25 * dt, dt8 = 0.125 * dt;
     double ef = 0;
     for (int ii = Mc - 1; ii > 0; --ii) {
@@ -195,39 +187,47 @@ __global__ void nh_chain(double* ch, int Mc, double T, double dt, const double* 
     }
 }
 
-__global__ void nvt_scale(int n, double* __restrict__ v, const double* __restrict__ ch, int Mc,
-                          double* __restrict__ disp, double dt2)
+__global__ void nvt_scale(int n, double* __restrict__ v, const double* __restrict__ chains, int Mc,
+                          const int* __restrict__ sysOf, double* __restrict__ disp, double dt2)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 3 * n) return;
-    double s = ch[4 * (Mc + 1) + 1];
+    int k = sysOf ? sysOf[i / 3] : 0;
+    double s = chains[(size_t)k * (4 * (Mc + 1) + 2) + 4 * (Mc + 1) + 1];
     v[i] = s * v[i];
     if (disp) disp[i] = dt2 * v[i];
 }
 
-__global__ void __launch_bounds__(KE_BLOCK) nvt_kick(int n, double* __restrict__ v, const double* __restrict__ f,
-                                                     double* __restrict__ disp, double dt, double dt2,
-                                                     double* __restrict__ partials)
+__global__ void nvt_kick(int n, double* __restrict__ v, const double* __restrict__ f, double* __restrict__ disp,
+                         double dt, double dt2, double* __restrict__ ke)
 {
-    __shared__ double s[KE_BLOCK];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double ke = 0;
-    if (i < n) {
-        double vv[3];
-        for (int c = 0; c < 3; ++c) {
-            vv[c] = v[3 * i + c] + (dt / 1.0) * f[3 * i + c];
-            v[3 * i + c] = vv[c];
-            disp[3 * i + c] = dt2 * vv[c];
-        }
-        ke = 0.5 * 1.0 * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+    if (i >= n) return;
+    double vv[3];
+    for (int c = 0; c < 3; ++c) {
+        vv[c] = v[3 * i + c] + (dt / 1.0) * f[3 * i + c];
+        v[3 * i + c] = vv[c];
+        disp[3 * i + c] = dt2 * vv[c];
     }
-    s[threadIdx.x] = ke;
+    ke[i] = 0.5 * 1.0 * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+}
+
+// one block per system: kinetic energy in a fixed summation order, written into that system's chain
+__global__ void __launch_bounds__(KE_BLOCK) ke_reduce(const double* __restrict__ ke, const int* __restrict__ partBase,
+                                                      double* chains, int Mc)
+{
+    __shared__ double sm[KE_BLOCK];
+    int k = blockIdx.x;
+    int a = partBase[k], b = partBase[k + 1];
+    double acc = 0;
+    for (int i = a + threadIdx.x; i < b; i += KE_BLOCK) acc += ke[i];
+    sm[threadIdx.x] = acc;
     __syncthreads();
     for (int o = KE_BLOCK / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        if (threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) partials[blockIdx.x] = s[0];
+    if (threadIdx.x == 0) chains[(size_t)k * (4 * (Mc + 1) + 2) + 4 * (Mc + 1)] = sm[0];
 }
 
 __global__ void status_or(int n, const int* __restrict__ st, int* __restrict__ bits)
@@ -249,9 +249,17 @@ int next_pow2(long long x)
 
 struct cssg_system {
     cssg_ctx* ctx;
-    const cssg_mesh* mesh;
-    int n;
-    cssg_params P;
+    int K = 1;             // independent systems
+    int n = 0;             // particles over all systems
+    cssg_params P;         // shared integrator parameters (systems' own force/patch parameters live in hsys)
+    std::vector<const cssg_mesh*> meshes;
+    std::vector<cssg_params> params;
+    std::vector<int> partBase;  // K + 1
+    std::vector<SysDesc> hsys;
+    SysDesc* dsys = nullptr;
+    DevMesh* dmeshes = nullptr;
+    int* sysOf = nullptr;       // per particle (null when K == 1)
+    int* dPartBase = nullptr;
     // state
     int* face = nullptr;
     double* bary = nullptr;
@@ -261,11 +269,10 @@ struct cssg_system {
     double* pos = nullptr;
     int* walkStatus = nullptr;
     int* srcStatus = nullptr;
-    int* statusBits = nullptr;           // device: OR of 1 << status over walks and sources
+    int* statusBits = nullptr;               // device: OR of 1 << status over walks and sources
     unsigned long long* counters = nullptr;  // device: crossings, windows, launches, in-range pairs, capacity hits
     // cell list
     bool useCells = false;
-    Grid grid;
     int totalCells = 0;
     int* cellOf = nullptr;
     int* cellCount = nullptr;
@@ -290,16 +297,16 @@ struct cssg_system {
     int* pairJ = nullptr;
     int* pairCount = nullptr;
     // NVT
-    double* chain = nullptr;
-    double* kePartials = nullptr;
-    int nKeBlocks = 0;
+    double* chains = nullptr;
+    double* ke = nullptr;
     // graph
     cudaGraphExec_t graphExec = nullptr;
+    double delta = 1e300;  // bucket width of the propagation order (distance-banded rounds)
+    int maxWindows = 0, bigMaxWindows = 0;  // per-source work caps of the regular and large-table passes
     // timing
     bool timing = false;
     std::vector<cudaEvent_t> events;
     int eventsUsed = 0;
-    double lastMs[4] = {0, 0, 0, 0};
 };
 
 namespace {
@@ -310,13 +317,14 @@ int alloc(void** p, size_t bytes)
     return CSSG_OK;
 }
 
-int record(cssg_system* s, int slot)
+int chain_len(const cssg_system* s) { return 4 * (std::max(1, s->P.chain_length) + 1) + 2; }
+
+int record(cssg_system* s)
 {
     if (!s->timing) return -1;
     if (s->eventsUsed >= (int)s->events.size()) return -1;
     int k = s->eventsUsed++;
     cudaEventRecord(s->events[k], s->ctx->stream);
-    (void)slot;
     return k;
 }
 
@@ -324,13 +332,12 @@ int record(cssg_system* s, int slot)
 void launch_forces(cssg_system* s)
 {
     cudaStream_t st = s->ctx->stream;
-    const DevMesh& M = s->mesh->d;
     const int n = s->n;
     const int tb = 256;
     if (s->useCells) {
         cudaMemsetAsync(s->cellCount, 0, sizeof(int) * (s->totalCells + 1), st);
         cudaMemsetAsync(s->cellCursor, 0, sizeof(int) * s->totalCells, st);
-        cell_assign<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->pos, s->grid, s->cellOf, s->cellCount);
+        cell_assign<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->pos, s->dsys, s->sysOf, s->cellOf, s->cellCount);
         scan_local<<<s->nScanBlocks, SCAN_BLOCK, 0, st>>>(s->cellCount, s->totalCells, s->cellStart, s->scanBlocks);
         scan_blocks<<<1, 1024, 0, st>>>(s->scanBlocks, s->nScanBlocks, s->cellStart + s->totalCells);
         scan_add<<<(s->totalCells + 255) / 256, 256, 0, st>>>(s->cellStart, s->totalCells, s->scanBlocks);
@@ -341,39 +348,29 @@ void launch_forces(cssg_system* s)
     cudaMemsetAsync(s->work, 0, 3 * sizeof(int), st);
     GeoLaunch L;
     memset(&L, 0, sizeof(L));
+    L.sys = s->dsys;
+    L.sysOf = s->sysOf;
     L.nSrc = n;
     L.srcFace = s->face;
     L.srcBary = s->bary;
     L.srcPos = s->pos;
     L.order = s->useCells ? s->cellList : nullptr;
-    L.searchMode = s->useCells ? 1 : 2;
-    L.nPart = n;
     L.partFace = s->face;
     L.partBary = s->bary;
     L.partPos = s->pos;
     L.cellStart = s->cellStart;
     L.cellList = s->cellList;
-    for (int c = 0; c < 3; ++c) {
-        L.nc[c] = s->grid.nc[c];
-        L.cs[c] = s->grid.cs[c];
-    }
-    L.range2 = s->P.range * s->P.range;
-    L.submesh = s->P.submesh;
-    L.maxDist = s->P.max_dist;
-    L.cutoff = s->P.cutoff;
     L.dOut = s->pairD;
     L.tsOut = s->pairT;
     L.pairJ = s->pairJ;
     L.pairCount = s->pairCount;
     L.pairCap = s->pairCap;
     L.force = s->force;
-    L.forceKind = s->P.force_kind;
-    L.k = s->P.k;
-    L.sigma = s->P.sigma;
     L.status = s->srcStatus;
     L.counters = s->counters + 1;
-    L.delta = 1e300;
-    L.maxRounds = 1 << 16;
+    L.delta = s->delta;
+    L.maxRounds = 4096;
+    L.maxWindows = s->maxWindows;
     L.caps = s->caps;
     L.scratch = s->scratch;
     L.slotBytes = s->slotBytes;
@@ -381,8 +378,8 @@ void launch_forces(cssg_system* s)
     L.workCounter = s->work;
     L.failList = s->failList;
     L.failCount = s->work + 2;
-    int e0 = record(s, 0);
-    cssg_launch_geodesic(M, L, (s->nSlots + 7) / 8, st);
+    record(s);
+    cssg_launch_geodesic(L, st);
     // retry pass with large tables for the sources whose tables overflowed (usually none: exits at once)
     GeoLaunch R = L;
     R.caps = s->bigCaps;
@@ -394,23 +391,21 @@ void launch_forces(cssg_system* s)
     R.itemCountDev = s->work + 2;
     R.failList = nullptr;
     R.failCount = nullptr;
-    cssg_launch_geodesic(M, R, (s->nBigSlots + 7) / 8, st);
-    int e1 = record(s, 1);
+    R.maxRounds = 1 << 15;
+    R.maxWindows = s->bigMaxWindows;
+    cssg_launch_geodesic(R, st);
+    record(s);
     status_or<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->srcStatus, s->statusBits);
-    (void)e0;
-    (void)e1;
 }
 
 void launch_walk(cssg_system* s)
 {
     cudaStream_t st = s->ctx->stream;
-    int e0 = record(s, 2);
-    cssg_launch_transport(s->mesh->d, s->n, s->face, s->bary, s->disp, s->vel, 1, s->walkStatus, s->counters,
-                          s->pos, st);
-    int e1 = record(s, 3);
+    record(s);
+    cssg_launch_transport(s->dmeshes, s->sysOf, s->n, s->face, s->bary, s->disp, s->vel, 1, s->walkStatus,
+                          s->counters, s->pos, st);
+    record(s);
     status_or<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, s->walkStatus, s->statusBits);
-    (void)e0;
-    (void)e1;
 }
 
 void launch_step(cssg_system* s)
@@ -427,52 +422,78 @@ void launch_step(cssg_system* s)
     } else {
         const int Mc = s->P.chain_length;
         const double T = s->P.temperature;
-        nh_chain<<<1, 32, 0, st>>>(s->chain, Mc, T, dt, nullptr, 0);
-        nvt_scale<<<(3 * n + tb - 1) / tb, tb, 0, st>>>(n, s->vel, s->chain, Mc, s->disp, 0.5 * dt);
+        const int K = s->K;
+        nh_chain<<<(K + 63) / 64, 64, 0, st>>>(s->chains, K, Mc, T, dt);
+        nvt_scale<<<(3 * n + tb - 1) / tb, tb, 0, st>>>(n, s->vel, s->chains, Mc, s->sysOf, s->disp, 0.5 * dt);
         launch_walk(s);
         launch_forces(s);
-        nvt_kick<<<s->nKeBlocks, KE_BLOCK, 0, st>>>(n, s->vel, s->force, s->disp, dt, 0.5 * dt, s->kePartials);
+        nvt_kick<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->vel, s->force, s->disp, dt, 0.5 * dt, s->ke);
+        ke_reduce<<<K, KE_BLOCK, 0, st>>>(s->ke, s->dPartBase, s->chains, Mc);
         launch_walk(s);
-        nh_chain<<<1, 32, 0, st>>>(s->chain, Mc, T, dt, s->kePartials, s->nKeBlocks);
-        nvt_scale<<<(3 * n + tb - 1) / tb, tb, 0, st>>>(n, s->vel, s->chain, Mc, nullptr, 0.0);
+        nh_chain<<<(K + 63) / 64, 64, 0, st>>>(s->chains, K, Mc, T, dt);
+        nvt_scale<<<(3 * n + tb - 1) / tb, tb, 0, st>>>(n, s->vel, s->chains, Mc, s->sysOf, nullptr, 0.0);
     }
 }
 
+// noseHooverNVT::setBathVariables per system (its own particle count)
 int reset_chain(cssg_system* s)
 {
-    int Mc = s->P.chain_length;
-    std::vector<double> h(4 * (Mc + 1) + 2, 0.0);
+    int Mc = std::max(1, s->P.chain_length), len = chain_len(s);
+    std::vector<double> h((size_t)len * s->K, 0.0);
     double T = s->P.temperature, tau = s->P.tau;
-    h[3] = 2.0 * (s->n - 1) * T * tau * tau;
-    for (int ii = 1; ii < Mc + 1; ++ii) h[4 * ii + 3] = T * tau * tau;
-    h[4 * (Mc + 1)] = h[3];
-    h[4 * (Mc + 1) + 1] = 1.0;
-    CSSG_CUDA(cudaMemcpyAsync(s->chain, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, s->ctx->stream));
+    for (int k = 0; k < s->K; ++k) {
+        double* c = &h[(size_t)k * len];
+        int nk = s->partBase[k + 1] - s->partBase[k];
+        c[3] = 2.0 * (nk - 1) * T * tau * tau;
+        for (int ii = 1; ii < Mc + 1; ++ii) c[4 * ii + 3] = T * tau * tau;
+        c[4 * (Mc + 1)] = c[3];
+        c[4 * (Mc + 1) + 1] = 1.0;
+    }
+    CSSG_CUDA(cudaMemcpyAsync(s->chains, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, s->ctx->stream));
     CSSG_CUDA(cudaStreamSynchronize(s->ctx->stream));
     return CSSG_OK;
 }
 
+int next_pow2_ll(long long x)
+{
+    int p = 1;
+    while (p < x && p < (1 << 30)) p <<= 1;
+    return p;
+}
+
 }  // namespace
 
-extern "C" int cssg_system_create(cssg_ctx* ctx, const cssg_mesh* mesh, int n, const cssg_params* params,
-                                  cssg_system** out)
+extern "C" int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh* const* meshes, const int* counts,
+                                          const cssg_params* params, cssg_system** out)
 {
-    if (!ctx || !mesh || !params || !out || n <= 0) {
+    if (!ctx || K <= 0 || !meshes || !counts || !params || !out) {
         cssg_set_error("cssg_system_create: bad arguments");
         return CSSG_ERR_ARG;
     }
-    const cssg_params& P = *params;
-    if (P.integrator < 0 || P.integrator > 1 || P.force_kind < 0 || P.force_kind > 1 || !(P.dt > 0) ||
-        (P.integrator == 1 && P.chain_length < 1) || !(P.cutoff > 0)) {
-        cssg_set_error("cssg_system_create: bad parameters");
-        return CSSG_ERR_ARG;
+    for (int k = 0; k < K; ++k) {
+        const cssg_params& P = params[k];
+        if (!meshes[k] || counts[k] <= 0 || P.integrator < 0 || P.integrator > 1 || P.force_kind < 0 ||
+            P.force_kind > 1 || !(P.dt > 0) || (P.integrator == 1 && P.chain_length < 1) || !(P.cutoff > 0)) {
+            cssg_set_error("cssg_system_create: bad parameters");
+            return CSSG_ERR_ARG;
+        }
+        if (P.integrator != params[0].integrator || P.dt != params[0].dt || P.temperature != params[0].temperature ||
+            P.tau != params[0].tau || P.chain_length != params[0].chain_length || (P.range > 0) != (params[0].range > 0)) {
+            cssg_set_error("cssg_system_create: batched systems must share integrator, dt, T, tau, chain length and "
+                           "neighbour structure kind");
+            return CSSG_ERR_ARG;
+        }
     }
     CSSG_CUDA(cudaSetDevice(ctx->device));
     cssg_system* s = new cssg_system();
     s->ctx = ctx;
-    s->mesh = mesh;
-    s->n = n;
-    s->P = P;
+    s->K = K;
+    s->P = params[0];
+    s->meshes.assign(meshes, meshes + K);
+    s->params.assign(params, params + K);
+    s->partBase.assign(K + 1, 0);
+    for (int k = 0; k < K; ++k) s->partBase[k + 1] = s->partBase[k] + counts[k];
+    const int n = s->n = s->partBase[K];
     int rc = CSSG_OK;
 #define TRY(x)                      \
     if ((rc = (x)) != CSSG_OK) {    \
@@ -491,62 +512,129 @@ extern "C" int cssg_system_create(cssg_ctx* ctx, const cssg_mesh* mesh, int n, c
     TRY(alloc((void**)&s->counters, sizeof(unsigned long long) * 8));
     TRY(alloc((void**)&s->work, sizeof(int) * 4));
     TRY(alloc((void**)&s->failList, sizeof(int) * n));
+    TRY(alloc((void**)&s->ke, sizeof(double) * n));
+    TRY(alloc((void**)&s->dPartBase, sizeof(int) * (K + 1)));
     cudaMemset(s->force, 0, sizeof(double) * 3 * n);
     cudaMemset(s->vel, 0, sizeof(double) * 3 * n);
     cudaMemset(s->face, 0, sizeof(int) * n);
     cudaMemset(s->statusBits, 0, sizeof(int));
     cudaMemset(s->counters, 0, sizeof(unsigned long long) * 8);
-    // cell list over the reference's domain: cells of size >= range (hyperRectangularCellList::setGridSize)
-    s->useCells = P.range > 0;
-    if (s->useCells) {
-        long long total = 1;
+    cudaMemcpy(s->dPartBase, s->partBase.data(), sizeof(int) * (K + 1), cudaMemcpyHostToDevice);
+    if (K > 1) {
+        std::vector<int> so(n);
+        for (int k = 0; k < K; ++k)
+            for (int i = s->partBase[k]; i < s->partBase[k + 1]; ++i) so[i] = k;
+        TRY(alloc((void**)&s->sysOf, sizeof(int) * n));
+        cudaMemcpy(s->sysOf, so.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+    }
+    // per-system descriptors: mesh, interaction parameters, grid (hyperRectangularCellList::setGridSize: cells of
+    // size >= range over the origin-including bounding box), particle and cell offsets
+    s->useCells = params[0].range > 0;
+    long long cellTotal = 0;
+    s->hsys.resize(K);
+    std::vector<DevMesh> hm(K);
+    long long maxF = 0, maxV = 0, maxT = 0;           // regular tables: systems whose patches fit shared memory
+    long long bigF = 0, bigV = 0, bigT = 0;           // large tables: every system (retry and binned sources)
+    const long long kRegularTable = 1024;             // entries per table that keep a warp's tables in ~20 KB
+    for (int k = 0; k < K; ++k) {
+        const cssg_params& P = params[k];
+        const cssg_mesh* m = meshes[k];
+        SysDesc& D = s->hsys[k];
+        memset(&D, 0, sizeof(D));
+        D.mesh = m->d;
+        hm[k] = m->d;
+        D.searchMode = s->useCells ? 1 : 2;
+        D.submesh = P.submesh;
+        D.forceKind = P.force_kind;
+        D.partBase = s->partBase[k];
+        D.nPart = counts[k];
+        D.range2 = P.range * P.range;
+        D.maxDist = P.max_dist;
+        D.cutoff = P.cutoff;
+        D.k = P.k;
+        D.sigma = P.sigma;
+        long long cells = 1;
         for (int c = 0; c < 3; ++c) {
-            double ext = mesh->d.bbMax[c] - mesh->d.bbMin[c];
-            s->grid.nc[c] = std::max(1, (int)std::floor(ext / P.range));
-            s->grid.cs[c] = ext / s->grid.nc[c];
-            s->grid.lo[c] = mesh->d.bbMin[c];
-            total *= s->grid.nc[c];
+            double ext = m->d.bbMax[c] - m->d.bbMin[c];
+            D.lo[c] = m->d.bbMin[c];
+            if (s->useCells) {
+                D.nc[c] = std::max(1, (int)std::floor(ext / P.range));
+                D.cs[c] = ext / D.nc[c];
+            } else {
+                D.nc[c] = 1;
+                D.cs[c] = 1;
+            }
+            cells *= D.nc[c];
         }
-        if (total > (1LL << 28)) {
+        D.cellBase = (int)cellTotal;
+        cellTotal += s->useCells ? cells : 0;
+        if (cellTotal > (1LL << 28)) {
             cssg_set_error("cssg_system_create: cell grid too large for the interaction range");
             cssg_system_destroy(s);
             return CSSG_ERR_CAPACITY;
         }
-        s->totalCells = (int)total;
-        s->nScanBlocks = (int)((total + SCAN_BLOCK * SCAN_ITEMS - 1) / (SCAN_BLOCK * SCAN_ITEMS));
+        // table sizes from the expected neighbourhood: faces with a vertex within reach (patch radius <= range, or
+        // the cutoff on the whole mesh) and candidates within the range
+        double reach = P.cutoff;
+        if (P.submesh && P.max_dist < reach) reach = P.max_dist;
+        double rr = reach + m->meanEdge;
+        long long estF = (long long)(1.3 * 3.14159265 * rr * rr / m->meanFaceArea) + 16;
+        if (estF > m->d.nF) estF = m->d.nF;
+        long long estV = std::min<long long>(m->d.nV, estF / 2 + 4 * (long long)std::sqrt((double)estF) + 16);
+        double density = counts[k] / m->area;
+        long long estT = P.range > 0 ? (long long)(density * 3.14159265 * P.range * P.range) : counts[k];
+        estT = std::min<long long>(std::max<long long>(32, 4 * estT + 16), std::max(32, counts[k]));
+        bigF = std::max(bigF, estF);
+        bigV = std::max(bigV, estV);
+        bigT = std::max(bigT, estT);
+        if (next_pow2_ll(3 * (estF + estT) / 2 + 32) > kRegularTable || next_pow2_ll(2 * estV + 32) > kRegularTable) {
+            D.bigBin = 1;
+        } else {
+            maxF = std::max(maxF, estF);
+            maxV = std::max(maxV, estV);
+            maxT = std::max(maxT, estT);
+        }
+    }
+    if (maxF == 0) {  // every system is large: the regular pass only routes sources to the large one
+        maxF = 16;
+        maxV = 16;
+        maxT = 32;
+    }
+    {
+        double me = 0;
+        for (int k = 0; k < K; ++k) me = std::max(me, meshes[k]->meanEdge);
+        s->delta = me;
+    }
+    TRY(alloc((void**)&s->dsys, sizeof(SysDesc) * K));
+    TRY(alloc((void**)&s->dmeshes, sizeof(DevMesh) * K));
+    cudaMemcpy(s->dsys, s->hsys.data(), sizeof(SysDesc) * K, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->dmeshes, hm.data(), sizeof(DevMesh) * K, cudaMemcpyHostToDevice);
+    if (s->useCells) {
+        s->totalCells = (int)cellTotal;
+        s->nScanBlocks = (int)((cellTotal + SCAN_BLOCK * SCAN_ITEMS - 1) / (SCAN_BLOCK * SCAN_ITEMS));
         TRY(alloc((void**)&s->cellOf, sizeof(int) * n));
-        TRY(alloc((void**)&s->cellCount, sizeof(int) * (total + 1)));
-        TRY(alloc((void**)&s->cellStart, sizeof(int) * (total + 1)));
-        TRY(alloc((void**)&s->cellCursor, sizeof(int) * total));
+        TRY(alloc((void**)&s->cellCount, sizeof(int) * (cellTotal + 1)));
+        TRY(alloc((void**)&s->cellStart, sizeof(int) * (cellTotal + 1)));
+        TRY(alloc((void**)&s->cellCursor, sizeof(int) * cellTotal));
         TRY(alloc((void**)&s->cellList, sizeof(int) * n));
         TRY(alloc((void**)&s->slotOf, sizeof(int) * n));
         TRY(alloc((void**)&s->scanBlocks, sizeof(int) * (s->nScanBlocks + 1)));
-    } else {
-        for (int c = 0; c < 3; ++c) {
-            s->grid.nc[c] = 1;
-            s->grid.cs[c] = 1;
-            s->grid.lo[c] = 0;
-        }
     }
-    // table sizes from the expected neighbourhood: faces within the cutoff and candidates within the range
-    double reach = P.cutoff;
-    if (P.submesh && P.max_dist < reach) reach = P.max_dist;
-    long long estF = (long long)(3.14159265 * reach * reach / mesh->meanFaceArea * 2.0) + 48;
-    if (estF > mesh->d.nF) estF = mesh->d.nF;
-    double density = n / mesh->area;
-    long long estT = P.range > 0 ? (long long)(density * 3.14159265 * P.range * P.range) : n;
-    s->caps.CT = (int)std::min<long long>(std::max<long long>(64, 6 * estT + 32), std::max(64, n));
-    s->caps.CF = next_pow2(2 * (estF + s->caps.CT) + 32);
-    s->caps.CV = next_pow2(2 * estF + 64);
-    s->caps.CW = (int)(8 * estF + 256);
-    s->caps.CL = (int)(estF + 128);
-    s->caps.CLOG = (int)(4 * s->caps.CT + 2 * estF + 256);
-    s->bigCaps.CT = std::max(s->caps.CT * 8, std::min(n, 4096));
-    s->bigCaps.CF = next_pow2(16LL * s->caps.CF);
-    s->bigCaps.CV = next_pow2(16LL * s->caps.CV);
-    s->bigCaps.CW = 16 * s->caps.CW;
-    s->bigCaps.CL = 16 * s->caps.CL;
-    s->bigCaps.CLOG = 16 * s->caps.CLOG + 8 * s->bigCaps.CT;
+    s->caps.CT = (int)maxT;
+    s->caps.CF = next_pow2_ll(3 * (maxF + s->caps.CT) / 2 + 32);
+    s->caps.CV = next_pow2_ll(2 * maxV + 32);
+    s->caps.CW = (int)(6 * maxF + 256);
+    s->caps.CL = (int)(maxV + 64);
+    s->caps.CLOG = (int)(4 * s->caps.CT + 2 * maxF + 128);
+    // large tables: 4x the largest estimate of any system (and never smaller than 8x the regular ones)
+    s->bigCaps.CT = (int)std::max<long long>(std::max(s->caps.CT * 8, std::min(n, 4096)), 4 * bigT);
+    s->bigCaps.CF = next_pow2_ll(std::max<long long>(8LL * s->caps.CF, 6 * (bigF + bigT)));
+    s->bigCaps.CV = next_pow2_ll(std::max<long long>(8LL * s->caps.CV, 8 * bigV));
+    s->bigCaps.CW = (int)std::max<long long>(16LL * s->caps.CW, 24 * bigF + 1024);
+    s->bigCaps.CL = (int)std::max<long long>(16LL * s->caps.CL, 4 * bigV + 256);
+    s->bigCaps.CLOG = (int)std::max<long long>(16LL * s->caps.CLOG + 8 * s->bigCaps.CT, 16 * bigT + 8 * bigF);
+    s->maxWindows = (int)std::min<long long>(1 << 30, 200 * maxF + 20000);
+    s->bigMaxWindows = (int)std::min<long long>(1 << 30, 400 * bigF + 100000);
     s->slotBytes = cssg_geo_slot_bytes(s->caps);
     s->bigSlotBytes = cssg_geo_slot_bytes(s->bigCaps);
     int sms = 0;
@@ -558,17 +646,24 @@ extern "C" int cssg_system_create(cssg_ctx* ctx, const cssg_mesh* mesh, int n, c
     TRY(alloc(&s->bigScratch, s->bigSlotBytes * (size_t)s->nBigSlots));
     cssg_geo_init_scratch(s->scratch, s->slotBytes, s->nSlots, s->caps, ctx->stream);
     cssg_geo_init_scratch(s->bigScratch, s->bigSlotBytes, s->nBigSlots, s->bigCaps, ctx->stream);
-    // NVT
-    int Mc = std::max(1, P.chain_length);
-    TRY(alloc((void**)&s->chain, sizeof(double) * (4 * (Mc + 1) + 2)));
-    s->nKeBlocks = (n + KE_BLOCK - 1) / KE_BLOCK;
-    TRY(alloc((void**)&s->kePartials, sizeof(double) * s->nKeBlocks));
-    if (P.integrator == 1) TRY(reset_chain(s));
+    TRY(alloc((void**)&s->chains, sizeof(double) * chain_len(s) * K));
+    cudaMemset(s->chains, 0, sizeof(double) * chain_len(s) * K);
+    if (s->P.integrator == 1) TRY(reset_chain(s));
     CSSG_CUDA(cudaStreamSynchronize(ctx->stream));
     CSSG_CUDA(cudaGetLastError());
 #undef TRY
     *out = s;
     return CSSG_OK;
+}
+
+extern "C" int cssg_system_create(cssg_ctx* ctx, const cssg_mesh* mesh, int n, const cssg_params* params,
+                                  cssg_system** out)
+{
+    if (!mesh || n <= 0) {
+        cssg_set_error("cssg_system_create: bad arguments");
+        return CSSG_ERR_ARG;
+    }
+    return cssg_system_create_batched(ctx, 1, &mesh, &n, params, out);
 }
 
 extern "C" int cssg_system_destroy(cssg_system* s)
@@ -580,8 +675,8 @@ extern "C" int cssg_system_destroy(cssg_system* s)
     for (cudaEvent_t e : s->events) cudaEventDestroy(e);
     void* ptrs[] = {s->face, s->bary, s->vel, s->force, s->disp, s->pos, s->walkStatus, s->srcStatus,
                     s->statusBits, s->counters, s->cellOf, s->cellCount, s->cellStart, s->cellCursor, s->cellList,
-                    s->slotOf, s->scanBlocks, s->scratch, s->bigScratch, s->work, s->failList, s->pairD, s->pairT, s->pairJ,
-                    s->pairCount, s->chain, s->kePartials};
+                    s->slotOf, s->scanBlocks, s->scratch, s->bigScratch, s->work, s->failList, s->pairD, s->pairT,
+                    s->pairJ, s->pairCount, s->chains, s->ke, s->dsys, s->dmeshes, s->sysOf, s->dPartBase};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -595,17 +690,18 @@ extern "C" int cssg_system_set_state(cssg_system* s, const int* face, const doub
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
     if (face) {
-        for (int i = 0; i < n; ++i)
-            if (face[i] < 0 || face[i] >= s->mesh->d.nF) {
-                cssg_set_error("cssg_system_set_state: face index out of range");
-                return CSSG_ERR_ARG;
-            }
+        for (int k = 0; k < s->K; ++k)
+            for (int i = s->partBase[k]; i < s->partBase[k + 1]; ++i)
+                if (face[i] < 0 || face[i] >= s->meshes[k]->d.nF) {
+                    cssg_set_error("cssg_system_set_state: face index out of range");
+                    return CSSG_ERR_ARG;
+                }
         CSSG_CUDA(cudaMemcpyAsync(s->face, face, sizeof(int) * n, cudaMemcpyHostToDevice, st));
     }
     if (bary) CSSG_CUDA(cudaMemcpyAsync(s->bary, bary, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
     if (vel) CSSG_CUDA(cudaMemcpyAsync(s->vel, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
     if (force) CSSG_CUDA(cudaMemcpyAsync(s->force, force, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
-    cssg_launch_positions(s->mesh->d, n, s->face, s->bary, s->pos, st);
+    cssg_launch_positions(s->dmeshes, s->sysOf, n, s->face, s->bary, s->pos, st);
     CSSG_CUDA(cudaStreamSynchronize(st));
     return CSSG_OK;
 }
@@ -621,7 +717,7 @@ extern "C" int cssg_system_kernels_per_step(cssg_system* s, int* count)
     if (!s || !count) return CSSG_ERR_ARG;
     // walk + status_or ; [cell list: assign, scan x3, scatter, sort] + geodesic + retry + status_or
     int walk = 2, forces = (s->useCells ? 6 : 0) + 3;
-    *count = s->P.integrator == 0 ? (1 + walk + forces + 1) : (2 + walk + forces + 1 + walk + 2);
+    *count = s->P.integrator == 0 ? (1 + walk + forces + 1) : (2 + walk + forces + 2 + walk + 2);
     return CSSG_OK;
 }
 
@@ -759,13 +855,12 @@ extern "C" int cssg_system_pairs(cssg_system* s, int cap, int* ih, int* jh, doub
 extern "C" int cssg_system_chain(cssg_system* s, double* chain, int capacity)
 {
     if (!s || !chain) return CSSG_ERR_ARG;
-    int Mc = std::max(1, s->P.chain_length);
-    int len = 4 * (Mc + 1) + 2;
+    int len = chain_len(s) * s->K;
     if (capacity < len) {
         cssg_set_error("cssg_system_chain: capacity too small");
         return CSSG_ERR_CAPACITY;
     }
-    CSSG_CUDA(cudaMemcpyAsync(chain, s->chain, sizeof(double) * len, cudaMemcpyDeviceToHost, s->ctx->stream));
+    CSSG_CUDA(cudaMemcpyAsync(chain, s->chains, sizeof(double) * len, cudaMemcpyDeviceToHost, s->ctx->stream));
     CSSG_CUDA(cudaStreamSynchronize(s->ctx->stream));
     return CSSG_OK;
 }

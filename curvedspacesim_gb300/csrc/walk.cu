@@ -333,7 +333,10 @@ __device__ int transport_one(const DevMesh& M, int& face, double* bary, double* 
         double nt[3];
         ld3(&M.N[3 * g], nt);
         double ndt = dot3(ns, nt);
-        if (ndt < 1) {
+        // the reference also divides by |n_s x n_t| here; for coplanar faces whose normals' dot product rounds
+        // below 1 that length is exactly zero (NaN there); the rotation is then the identity and is skipped
+        if (ndt < 1 && (ns[0] * nt[1] - ns[1] * nt[0] != 0 || ns[1] * nt[2] - ns[2] * nt[1] != 0 ||
+                        ns[2] * nt[0] - ns[0] * nt[2] != 0)) {
             double ax[3];
             cross3(ns, nt, ax);
             double al = sqrt(dot3(ax, ax));
@@ -364,7 +367,8 @@ __device__ int transport_one(const DevMesh& M, int& face, double* bary, double* 
     return CSSG_ST_OK;
 }
 
-__global__ void __launch_bounds__(128) transport_kernel(DevMesh M, int n, int* __restrict__ face,
+__global__ void __launch_bounds__(128) transport_kernel(const DevMesh* __restrict__ meshes, const int* __restrict__ meshOf,
+                                                        int n, int* __restrict__ face,
                                                         double* __restrict__ bary, double* __restrict__ disp,
                                                         double* __restrict__ transport, int ntv, int* __restrict__ status,
                                                         unsigned long long* crossings, double* __restrict__ posOut)
@@ -372,6 +376,7 @@ __global__ void __launch_bounds__(128) transport_kernel(DevMesh M, int n, int* _
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int cr = 0;
     if (i < n) {
+        const DevMesh& M = meshes[meshOf ? meshOf[i] : 0];
         int f = face[i];
         double b[3] = {bary[3 * i], bary[3 * i + 1], bary[3 * i + 2]};
         double d[3] = {disp[3 * i], disp[3 * i + 1], disp[3 * i + 2]};
@@ -399,11 +404,12 @@ __global__ void __launch_bounds__(128) transport_kernel(DevMesh M, int n, int* _
     }
 }
 
-__global__ void positions_kernel(DevMesh M, int n, const int* __restrict__ face, const double* __restrict__ bary,
-                                 double* __restrict__ pos)
+__global__ void positions_kernel(const DevMesh* __restrict__ meshes, const int* __restrict__ meshOf, int n,
+                                 const int* __restrict__ face, const double* __restrict__ bary, double* __restrict__ pos)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const DevMesh& M = meshes[meshOf ? meshOf[i] : 0];
     FacePts P;
     load_face(M, face[i], P);
     double b[3] = {bary[3 * i], bary[3 * i + 1], bary[3 * i + 2]};
@@ -414,19 +420,21 @@ __global__ void positions_kernel(DevMesh M, int n, const int* __restrict__ face,
 
 }  // namespace
 
-void cssg_launch_transport(const DevMesh& M, int n, int* face, double* bary, double* disp, double* transport, int nT,
-                           int* status, unsigned long long* crossings, double* pos_out, cudaStream_t s)
+void cssg_launch_transport(const DevMesh* meshes, const int* meshOf, int n, int* face, double* bary, double* disp,
+                           double* transport, int nT, int* status, unsigned long long* crossings, double* pos_out,
+                           cudaStream_t s)
 {
     if (n <= 0) return;
     int threads = 128;
-    transport_kernel<<<(n + threads - 1) / threads, threads, 0, s>>>(M, n, face, bary, disp, transport, nT, status,
-                                                                     crossings, pos_out);
+    transport_kernel<<<(n + threads - 1) / threads, threads, 0, s>>>(meshes, meshOf, n, face, bary, disp, transport, nT,
+                                                                     status, crossings, pos_out);
 }
 
-void cssg_launch_positions(const DevMesh& M, int n, const int* face, const double* bary, double* pos, cudaStream_t s)
+void cssg_launch_positions(const DevMesh* meshes, const int* meshOf, int n, const int* face, const double* bary,
+                           double* pos, cudaStream_t s)
 {
     if (n <= 0) return;
-    positions_kernel<<<(n + 127) / 128, 128, 0, s>>>(M, n, face, bary, pos);
+    positions_kernel<<<(n + 127) / 128, 128, 0, s>>>(meshes, meshOf, n, face, bary, pos);
 }
 
 extern "C" int cssg_transport_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int n, int* face, double* bary, double* disp,
@@ -437,7 +445,8 @@ extern "C" int cssg_transport_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int n,
         cssg_set_error("cssg_transport_batch: bad arguments (at most 4 transported vectors)");
         return CSSG_ERR_ARG;
     }
-    cssg_launch_transport(mesh->d, n, face, bary, disp, transport, nTransport, status, crossings, nullptr, ctx->stream);
+    cssg_launch_transport(mesh->dself, nullptr, n, face, bary, disp, transport, nTransport, status, crossings, nullptr,
+                          ctx->stream);
     CSSG_CUDA(cudaGetLastError());
     return CSSG_OK;
 }

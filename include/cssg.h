@@ -79,11 +79,12 @@ int cssg_transport_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int n, int* face,
  *   cutoff: paths longer than cutoff are not followed; such targets report +inf (use +inf for exact reference
  *           semantics, where a disconnected patch target reports 2*max_dist and tangent (0,0,1) (:197-203))
  * Outputs per candidate: d_out[], tstart_out[3*] (unit start tangent at the source), tend_out[3*] (nullable; unit
- * direction of travel at the target).  status[nSrc]. */
+ * direction of travel at the target).  status[nSrc].  stats (nullable): 4 per source = windows processed,
+ * pseudo-source launches, propagation rounds, targets. */
 int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSrc, const int* src_face, const double* src_bary,
                         const int* cand_offsets, const int* cand_face, const double* cand_bary, int submesh,
                         double max_dist, const double* threshold, double cutoff, double* d_out, double* tstart_out,
-                        double* tend_out, int* status);
+                        double* tend_out, int* status, long long* stats);
 
 /* ---- particle system: simpleModel + force + updater on the device -------------------------------------------- */
 typedef struct cssg_params {
@@ -102,6 +103,12 @@ typedef struct cssg_params {
 } cssg_params;
 
 int cssg_system_create(cssg_ctx* ctx, const cssg_mesh* mesh, int n, const cssg_params* params, cssg_system** out);
+/* K independent systems (own mesh, particle count and force / patch parameters) advanced together: every kernel of
+ * a step serves all of them (one persistent geodesic launch per step over all sources).  Integrator, dt, T, tau,
+ * chain length and the neighbour-structure kind (cell list or all-to-all) must agree.  State arrays of the other
+ * system_* calls are the concatenation of the systems' particles in order. */
+int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh* const* meshes, const int* counts,
+                               const cssg_params* params, cssg_system** out);
 int cssg_system_destroy(cssg_system* sys);
 /* simpleModel::setParticlePositions (simpleModel.cpp:204-212) + velocities/forces; host arrays; nullable fields
  * are left unchanged.  Synchronises. */
@@ -125,7 +132,8 @@ int cssg_system_check(cssg_system* sys, int* status_bits, unsigned long long* co
 /* Pair data of the last force evaluation, host arrays with capacity cap: source i, target j, distance, start
  * tangent (3).  Returns the number of candidate pairs in *count (which may exceed cap). */
 int cssg_system_pairs(cssg_system* sys, int cap, int* i_host, int* j_host, double* d_host, double* t_host, int* count);
-/* Nose-Hoover chain state: (M+1) x 4 bath variables + {kinetic energy, scale factor}, host array. */
+/* Nose-Hoover chain state, per system: (M+1) x 4 bath variables + {kinetic energy, scale factor}, host array of
+ * K * (4 (M+1) + 2) doubles. */
 int cssg_system_chain(cssg_system* sys, double* chain_host, int capacity);
 /* Timing of the last step() call: milliseconds of the dominant kernel (geodesic+force) and of the walk, from
  * CUDA events on the system stream (filled when timing is enabled with cssg_system_timing(sys, 1)). */
@@ -139,6 +147,26 @@ int cssg_system_kernels_per_step(cssg_system* sys, int* count);
  * dependent-chain kernel timed with CUDA events on the context stream; the denominator of the FP64 roofline of the
  * geodesic kernel.  Synchronises. */
 int cssg_diag_fp64_peak(cssg_ctx* ctx, double* gflops_host);
+
+/* ---- learned distance screen -------------------------------------------------------------------------------
+ * No counterpart in the reference: a 14 -> 64 -> 64 -> 64 -> 1 GELU MLP that predicts the normalised geodesic
+ * excess (d - |chord|) / sigma of a candidate pair, so that pairs predicted beyond sigma plus a calibrated margin can
+ * skip exact propagation.  Parameters are one FP32 array of cssg_mlp_param_count() values:
+ * W1[64][16] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] w4[64] b4 (W rows = output units). */
+int cssg_mlp_param_count(void);
+/* Features of pairs (pi[p] -> pj[p]) of particles on one mesh: X_bf16[nPairs][16] (14 features + 2 zeros, BF16)
+ * and |chord| / sigma (nullable).  face[], pos[3*] are the particles' faces and R3 positions. */
+int cssg_screen_features(cssg_ctx* ctx, const cssg_mesh* mesh, double sigma, int nPairs, const int* pi, const int* pj,
+                         const int* face, const double* pos, void* X_bf16, float* chord_over_sigma);
+/* Inference on the tensor cores (tcgen05, BF16 operands, FP32 accumulation in tensor memory): y[n].  err_flag
+ * (nullable, device int) is set to 1 if a tensor-core completion wait timed out. */
+int cssg_mlp_infer(cssg_ctx* ctx, const void* X_bf16, int n, const float* params, float* y, int* err_flag);
+/* Gradient of 0.5 sum_p (f(x_p) - y_p)^2 with respect to params (FP32 forward/backward with the BF16 roundings of
+ * inference): grad[cssg_mlp_param_count()] is overwritten; loss (nullable) receives the sum. */
+int cssg_mlp_grad(cssg_ctx* ctx, const void* X_bf16, const float* y, int n, const float* params, float* grad,
+                  float* loss);
+/* One Adam step (lr, beta 0.9 / 0.999) on params using grad / batch; m, v: zero-initialised state arrays. */
+int cssg_mlp_adam(cssg_ctx* ctx, float* params, const float* grad, float* m, float* v, int batch, float lr, int step);
 
 #ifdef __cplusplus
 }

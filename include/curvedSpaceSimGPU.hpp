@@ -1,0 +1,397 @@
+// curvedSpaceSimGPU.hpp - C++ host classes over the C ABI (cssg.h) that keep the reference's interfaces for the
+// per-timestep hot path, so existing curvedSpaceSim driver code can switch to the GB300 kernels with type changes
+// only.  Header-only; link against libcssg.so and the CUDA runtime.
+//
+//   reference                                   here
+//   meshPosition (inc/pointDataType.h:10-28)    cssg::meshPosition     (x = barycentric weights, faceIndex)
+//   closedMeshSpace / triangulatedMeshSpace     cssg::closedMeshSpace
+//     distance (triangulatedMeshSpace.cpp:212-238, distanceWithSubmeshing :155-205)
+//     transportParticleAndVectors (:448-564), displaceParticle (:428-432), getArea (:153),
+//     useSubmeshingRoutines (triangulatedMeshSpace.h:60-66), randomVectorAtPosition (:118-138)
+//   simpleModel (src/models/simpleModel.h:25-111) + force + updater + simulation
+//                                               cssg::gpuSimulation: positions/velocities/forces vectors,
+//                                               moveParticles, computeForces, performTimestep on the device
+//   harmonicRepulsion (src/forces/harmonicRepulsion.cpp:3-34)
+//                                               cssg::harmonicRepulsion::pairwiseForce / pairwiseEnergy
+//
+// Errors: the reference prints and throws std::exception (inc/debuggingHelp.h:19-31); these classes throw
+// std::runtime_error carrying cssg_last_error() or the per-item status name.
+#ifndef CURVEDSPACESIM_GPU_HPP
+#define CURVEDSPACESIM_GPU_HPP
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <fstream>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "cssg.h"
+
+namespace cssg {
+
+struct vector3 {
+    double v[3] = {0, 0, 0};
+    vector3() = default;
+    vector3(double a, double b, double c) : v{a, b, c} {}
+    double& operator[](int i) { return v[i]; }
+    double operator[](int i) const { return v[i]; }
+    double squared_length() const { return v[0] * v[0] + v[1] * v[1] + v[2] * v[2]; }
+};
+typedef vector3 point3;
+
+struct meshPosition {
+    point3 x;  // barycentric weights on faceIndex
+    int faceIndex = -1;
+    meshPosition() = default;
+    meshPosition(point3 b, int f) : x(b), faceIndex(f) {}
+};
+
+inline void throwIf(int rc, const char* what)
+{
+    if (rc != CSSG_OK) throw std::runtime_error(std::string(what) + ": " + cssg_last_error());
+}
+
+inline const char* statusName(int st)
+{
+    switch (st) {
+        case CSSG_ST_BORDER: return "Surface is meant to be closed, but a border was encountered.";
+        case CSSG_ST_NAN: return "Illegal coordinates";
+        case CSSG_ST_VERTEX: return "throughvertex didn't find a face";
+        case CSSG_ST_ITER: return "walk exceeded its crossing cap";
+        case CSSG_ST_NO_INTERSECTION: return "a barycentric coordinate of the target is negative, but neither 1 nor 2 intersections were found";
+        case CSSG_ST_CAPACITY: return "geodesic propagation exceeded its table capacity";
+        default: return "ok";
+    }
+}
+
+// RAII device buffer
+template <typename T>
+struct devbuf {
+    T* p = nullptr;
+    size_t n = 0;
+    explicit devbuf(size_t count) : n(count)
+    {
+        if (cudaMalloc((void**)&p, sizeof(T) * (count ? count : 1)) != cudaSuccess) throw std::runtime_error("cudaMalloc");
+    }
+    ~devbuf() { cudaFree(p); }
+    devbuf(const devbuf&) = delete;
+    devbuf& operator=(const devbuf&) = delete;
+    void up(const T* h, cudaStream_t s)
+    {
+        if (n) cudaMemcpyAsync(p, h, sizeof(T) * n, cudaMemcpyHostToDevice, s);
+    }
+    void down(T* h, cudaStream_t s) const
+    {
+        if (n) cudaMemcpyAsync(h, p, sizeof(T) * n, cudaMemcpyDeviceToHost, s);
+    }
+};
+
+//! closedMeshSpace: a closed triangulated surface whose geodesic work runs on the GPU.
+class closedMeshSpace {
+public:
+    explicit closedMeshSpace(int device = 0) : device_(device) { throwIf(cssg_ctx_create(device, nullptr, &ctx_), "cssg_ctx_create"); }
+    ~closedMeshSpace()
+    {
+        if (mesh_) cssg_mesh_destroy(mesh_);
+        cssg_ctx_destroy(ctx_);
+    }
+    closedMeshSpace(const closedMeshSpace&) = delete;
+    closedMeshSpace& operator=(const closedMeshSpace&) = delete;
+
+    //! vertices (x,y,z per vertex) and counter-clockwise triangles
+    void loadMesh(const std::vector<double>& V, const std::vector<int>& F)
+    {
+        if (mesh_) cssg_mesh_destroy(mesh_);
+        mesh_ = nullptr;
+        throwIf(cssg_mesh_create(V.data(), (int)(V.size() / 3), F.data(), (int)(F.size() / 3), device_, &mesh_),
+                "cssg_mesh_create");
+        V_ = V;
+        F_ = F;
+        double bb[6];
+        throwIf(cssg_mesh_info(mesh_, nullptr, nullptr, &area_, bb), "cssg_mesh_info");
+        for (int c = 0; c < 3; ++c) {
+            minVertexPosition[c] = bb[c];
+            maxVertexPosition[c] = bb[3 + c];
+        }
+    }
+
+    //! OFF reader (the reference loads OFF/OBJ/STL/PLY through CGAL; triangles only, like its is_triangle_mesh check)
+    void loadMeshFromFile(const std::string& filename, bool verbose = false)
+    {
+        std::ifstream in(filename);
+        if (!in) throw std::runtime_error("Invalid input file.");
+        std::string tok;
+        std::vector<std::string> toks;
+        std::string line;
+        while (std::getline(in, line)) {
+            auto h = line.find('#');
+            if (h != std::string::npos) line = line.substr(0, h);
+            std::istringstream ss(line);
+            while (ss >> tok) toks.push_back(tok);
+        }
+        size_t p = 0;
+        if (!toks.empty() && (toks[0] == "OFF" || toks[0] == "off")) p = 1;
+        int nv = std::stoi(toks.at(p)), nf = std::stoi(toks.at(p + 1));
+        p += 3;
+        std::vector<double> V(3 * (size_t)nv);
+        for (size_t i = 0; i < V.size(); ++i) V[i] = std::stod(toks.at(p++));
+        std::vector<int> F;
+        F.reserve(3 * (size_t)nf);
+        for (int f = 0; f < nf; ++f) {
+            int k = std::stoi(toks.at(p++));
+            if (k != 3) throw std::runtime_error("Non-triangular mesh");
+            for (int c = 0; c < 3; ++c) F.push_back(std::stoi(toks.at(p++)));
+        }
+        if (verbose) printf("input mesh has %i faces and %i vertices\n", nf, nv);
+        loadMesh(V, F);
+    }
+
+    void useSubmeshingRoutines(bool useSubMesh, double maxDist = 1.0, bool danger = false)
+    {
+        submeshingActivated_ = useSubMesh;
+        maximumDistance_ = maxDist;
+        (void)danger;
+    }
+
+    double getArea() const { return area_; }
+
+    //! geodesic distances and unit path tangents from p1 to every p2 (the reference's per-source query)
+    void distance(meshPosition& p1, std::vector<meshPosition>& p2, std::vector<double>& distances,
+                  std::vector<vector3>& startPathTangent, std::vector<vector3>& endPathTangent,
+                  double distanceThreshold = 1e20)
+    {
+        const int n = (int)p2.size();
+        distances.resize(n);
+        startPathTangent.resize(n);
+        endPathTangent.resize(n);
+        if (n == 0) return;
+        cudaStream_t s = (cudaStream_t)cssg_ctx_stream(ctx_);
+        std::vector<int> sf{p1.faceIndex}, off{0, n}, cf(n);
+        std::vector<double> sb{p1.x[0], p1.x[1], p1.x[2]}, cb(3 * (size_t)n), th{distanceThreshold};
+        for (int i = 0; i < n; ++i) {
+            cf[i] = p2[i].faceIndex;
+            for (int c = 0; c < 3; ++c) cb[3 * i + c] = p2[i].x[c];
+        }
+        devbuf<int> dsf(1), doff(2), dcf(n), dst(1);
+        devbuf<double> dsb(3), dcb(3 * (size_t)n), dth(1), dd(n), dts(3 * (size_t)n), dte(3 * (size_t)n);
+        dsf.up(sf.data(), s);
+        doff.up(off.data(), s);
+        dcf.up(cf.data(), s);
+        dsb.up(sb.data(), s);
+        dcb.up(cb.data(), s);
+        dth.up(th.data(), s);
+        throwIf(cssg_distance_batch(ctx_, mesh_, 1, dsf.p, dsb.p, doff.p, dcf.p, dcb.p, submeshingActivated_ ? 1 : 0,
+                                    maximumDistance_, dth.p, INFINITY, dd.p, dts.p, dte.p, dst.p, nullptr),
+                "cssg_distance_batch");
+        std::vector<double> ts(3 * (size_t)n), te(3 * (size_t)n);
+        int st = 0;
+        dd.down(distances.data(), s);
+        dts.down(ts.data(), s);
+        dte.down(te.data(), s);
+        dst.down(&st, s);
+        throwIf(cssg_ctx_synchronize(ctx_), "cssg_ctx_synchronize");
+        if (st) throw std::runtime_error(statusName(st));
+        for (int i = 0; i < n; ++i) {
+            startPathTangent[i] = vector3(ts[3 * i], ts[3 * i + 1], ts[3 * i + 2]);
+            endPathTangent[i] = vector3(te[3 * i], te[3 * i + 1], te[3 * i + 2]);
+        }
+    }
+
+    //! move pos by displacementVector along the surface, parallel-transporting transportVectors
+    void transportParticleAndVectors(meshPosition& pos, vector3& displacementVector, std::vector<vector3>& transportVectors)
+    {
+        std::vector<meshPosition> p{pos};
+        std::vector<vector3> d{displacementVector};
+        std::vector<std::vector<vector3>> t{transportVectors};
+        transportBatch(p, d, t);
+        pos = p[0];
+        displacementVector = d[0];
+        transportVectors = t[0];
+    }
+
+    void displaceParticle(meshPosition& pos, vector3& displacementVector)
+    {
+        std::vector<vector3> none;
+        transportParticleAndVectors(pos, displacementVector, none);
+    }
+
+    //! batched walk (what simpleModel::moveParticles does particle by particle)
+    void transportBatch(std::vector<meshPosition>& pos, std::vector<vector3>& disp,
+                        std::vector<std::vector<vector3>>& transport)
+    {
+        const int n = (int)pos.size();
+        if (n == 0) return;
+        const int nt = transport.empty() ? 0 : (int)transport[0].size();
+        cudaStream_t s = (cudaStream_t)cssg_ctx_stream(ctx_);
+        std::vector<int> f(n), st(n);
+        std::vector<double> b(3 * (size_t)n), d(3 * (size_t)n), tv(3 * (size_t)n * nt);
+        for (int i = 0; i < n; ++i) {
+            f[i] = pos[i].faceIndex;
+            for (int c = 0; c < 3; ++c) {
+                b[3 * i + c] = pos[i].x[c];
+                d[3 * i + c] = disp[i][c];
+            }
+            for (int k = 0; k < nt; ++k)
+                for (int c = 0; c < 3; ++c) tv[3 * ((size_t)i * nt + k) + c] = transport[i][k][c];
+        }
+        devbuf<int> df(n), dst(n);
+        devbuf<double> db(3 * (size_t)n), dd(3 * (size_t)n), dtv(3 * (size_t)n * nt);
+        df.up(f.data(), s);
+        db.up(b.data(), s);
+        dd.up(d.data(), s);
+        dtv.up(tv.data(), s);
+        throwIf(cssg_transport_batch(ctx_, mesh_, n, df.p, db.p, dd.p, nt ? dtv.p : nullptr, nt, dst.p, nullptr),
+                "cssg_transport_batch");
+        df.down(f.data(), s);
+        db.down(b.data(), s);
+        dd.down(d.data(), s);
+        dtv.down(tv.data(), s);
+        dst.down(st.data(), s);
+        throwIf(cssg_ctx_synchronize(ctx_), "cssg_ctx_synchronize");
+        for (int i = 0; i < n; ++i) {
+            if (st[i]) throw std::runtime_error(statusName(st[i]));
+            pos[i].faceIndex = f[i];
+            pos[i].x = point3(b[3 * i], b[3 * i + 1], b[3 * i + 2]);
+            disp[i] = vector3(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
+            for (int k = 0; k < nt; ++k)
+                transport[i][k] = vector3(tv[3 * ((size_t)i * nt + k)], tv[3 * ((size_t)i * nt + k) + 1],
+                                          tv[3 * ((size_t)i * nt + k) + 2]);
+        }
+    }
+
+    cssg_ctx* context() const { return ctx_; }
+    cssg_mesh* mesh() const { return mesh_; }
+    bool submeshing() const { return submeshingActivated_; }
+    double maximumDistance() const { return maximumDistance_; }
+
+    double minVertexPosition[3] = {0, 0, 0};
+    double maxVertexPosition[3] = {0, 0, 0};
+
+private:
+    int device_;
+    cssg_ctx* ctx_ = nullptr;
+    cssg_mesh* mesh_ = nullptr;
+    std::vector<double> V_;
+    std::vector<int> F_;
+    double area_ = 0;
+    bool submeshingActivated_ = false;
+    double maximumDistance_ = 0;
+};
+
+//! harmonicRepulsion: E = k/2 (sigma - d)^2 for d < sigma, F = -k (sigma - d) t for d <= sigma
+class harmonicRepulsion {
+public:
+    harmonicRepulsion(double stiffness = 1, double monodisperseRange = 1) : k(stiffness), sigma(monodisperseRange),
+        maximumInteractionRange(monodisperseRange) {}
+    double pairwiseEnergy(const vector3&, double distance) const
+    {
+        return distance < sigma ? 0.5 * k * (sigma - distance) * (sigma - distance) : 0.0;
+    }
+    vector3 pairwiseForce(const vector3& separation, double distance) const
+    {
+        if (distance > sigma) return vector3();
+        double m = -k * (sigma - distance);
+        return vector3(m * separation[0], m * separation[1], m * separation[2]);
+    }
+    double k, sigma, maximumInteractionRange;
+};
+
+//! simpleModel + harmonicRepulsion + (velocityVerletNVE | noseHooverNVT) + simulation, resident on the GPU.
+//! performTimestep() advances one step without leaving the device; positions/velocities/forces are mirrored into
+//! the public vectors by pull() and pushed by push(), like the reference model's public members.
+class gpuSimulation {
+public:
+    enum Integrator { NVE = 0, NVT = 1 };
+    gpuSimulation(closedMeshSpace& space, int N, const harmonicRepulsion& force, Integrator integ, double dt,
+                  double T = 0.0, double tau = 1.0, int chainLength = 2, bool useCellList = true)
+        : space_(space), N(N)
+    {
+        cssg_params p{};
+        p.integrator = integ;
+        p.force_kind = 0;
+        p.k = force.k;
+        p.sigma = force.sigma;
+        p.range = useCellList ? force.maximumInteractionRange : 0.0;
+        p.submesh = space.submeshing() ? 1 : 0;
+        p.max_dist = space.submeshing() ? space.maximumDistance() : force.sigma;
+        p.cutoff = force.sigma;
+        p.dt = dt;
+        p.temperature = T;
+        p.tau = tau;
+        p.chain_length = chainLength;
+        throwIf(cssg_system_create(space.context(), space.mesh(), N, &p, &sys_), "cssg_system_create");
+        positions.resize(N);
+        velocities.resize(N);
+        forces.resize(N);
+    }
+    ~gpuSimulation() { cssg_system_destroy(sys_); }
+    gpuSimulation(const gpuSimulation&) = delete;
+    gpuSimulation& operator=(const gpuSimulation&) = delete;
+
+    void setParticlePositions(const std::vector<meshPosition>& p)
+    {
+        positions = p;
+        push();
+    }
+    void push()
+    {
+        std::vector<int> f(N);
+        std::vector<double> b(3 * (size_t)N), v(3 * (size_t)N), fo(3 * (size_t)N);
+        for (int i = 0; i < N; ++i) {
+            f[i] = positions[i].faceIndex;
+            for (int c = 0; c < 3; ++c) {
+                b[3 * i + c] = positions[i].x[c];
+                v[3 * i + c] = velocities[i][c];
+                fo[3 * i + c] = forces[i][c];
+            }
+        }
+        throwIf(cssg_system_set_state(sys_, f.data(), b.data(), v.data(), fo.data()), "cssg_system_set_state");
+    }
+    void pull()
+    {
+        std::vector<int> f(N);
+        std::vector<double> b(3 * (size_t)N), v(3 * (size_t)N), fo(3 * (size_t)N);
+        throwIf(cssg_system_get_state(sys_, f.data(), b.data(), v.data(), fo.data()), "cssg_system_get_state");
+        for (int i = 0; i < N; ++i) {
+            positions[i] = meshPosition(point3(b[3 * i], b[3 * i + 1], b[3 * i + 2]), f[i]);
+            velocities[i] = vector3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+            forces[i] = vector3(fo[3 * i], fo[3 * i + 1], fo[3 * i + 2]);
+        }
+    }
+    //! simulation::performTimestep, `steps` times, on the device (CUDA graph replay)
+    void performTimestep(int steps = 1)
+    {
+        throwIf(cssg_system_step(sys_, steps, 1), "cssg_system_step");
+        checkItems();
+    }
+    //! simulation::computeForces
+    void computeForces()
+    {
+        throwIf(cssg_system_compute_forces(sys_), "cssg_system_compute_forces");
+        checkItems();
+    }
+    void checkItems()
+    {
+        int bits = 0;
+        throwIf(cssg_system_check(sys_, &bits, nullptr), "cssg_system_check");
+        for (int st = 1; st < 8; ++st)
+            if (bits & (1 << st)) throw std::runtime_error(statusName(st));
+    }
+    cssg_system* handle() const { return sys_; }
+
+    closedMeshSpace& space_;
+    int N;
+    std::vector<meshPosition> positions;
+    std::vector<vector3> velocities;
+    std::vector<vector3> forces;
+
+private:
+    cssg_system* sys_ = nullptr;
+};
+
+}  // namespace cssg
+
+#endif

@@ -56,12 +56,19 @@ def lib():
         L.oracle_simulate.restype = I
         L.oracle_simulate.argtypes = [P, I, I, I, P, P, P, P, P, P, I, P]
         L.oracle_nvt_init.argtypes = [I, D, D, I, P]
+        L.oracle_set_order.argtypes = [I, D, I]
         _lib = L
     return _lib
 
 
 def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_order(order: int = 0, delta: float = 0.0, bfs: bool = False):
+    """Processing order of the oracle's propagation: 0 priority queue (default), 1 distance-banded rounds of width
+    delta (the CUDA kernel's order; bfs=True drops the banding).  Results are identical; only the work differs."""
+    lib().oracle_set_order(int(order), float(delta), int(bool(bfs)))
 
 
 class OracleMesh:

@@ -72,6 +72,7 @@ inline void cross3(const double* a, const double* b, double* o)
     o[2] = a[0] * b[1] - a[1] * b[0];
 }
 inline double norm3(const double* a) { return std::sqrt(dot3(a, a)); }
+inline double len2(double x, double y) { return std::sqrt(x * x + y * y); }
 
 // ------------------------------------------------------------------------------------------------------------------
 // Mesh
@@ -465,6 +466,7 @@ int transport_one(const Mesh& M, int& face, double* bary, double* disp, double* 
         for (int c = 0; c < 3; ++c) { sb[c] = ip[c]; sp[c] = ep[c]; }
         cross++;
         if (nhit == 2) {
+            cross += (1 << 16) - 1;  // vertex crossings are counted in the high half
             // vertex crossing (triangulatedMeshSpace.cpp:520-532, 566-611); like the reference, the vertex passed on
             // is the first vertex of the first edge that reported a hit
             int v = inv0;
@@ -508,7 +510,10 @@ int transport_one(const Mesh& M, int& face, double* bary, double* disp, double* 
         construct_pt(p[0], p[1], p[2], ip, sp);
         double nt[3] = {M.N[3 * g], M.N[3 * g + 1], M.N[3 * g + 2]};
         double ndt = dot3(ns, nt);
-        if (ndt < 1) {
+        // the reference also divides by |n_s x n_t| here; for coplanar faces whose normals' dot product rounds
+        // below 1 that length is exactly zero (NaN there); the rotation is then the identity and is skipped
+        if (ndt < 1 && (ns[0] * nt[1] - ns[1] * nt[0] != 0 || ns[1] * nt[2] - ns[2] * nt[1] != 0 ||
+                        ns[2] * nt[0] - ns[0] * nt[2] != 0)) {
             double ax[3];
             cross3(ns, nt, ax);
             double al = norm3(ax);
@@ -659,6 +664,12 @@ struct GeoWork {
     }
 };
 
+// processing order: 0 = exact priority queue (Dijkstra order); 1 = distance-banded rounds of width g_delta
+// (the order the CUDA kernel uses; results are identical, only the work differs)
+int g_order = 0;
+double g_delta = 0.0;
+double g_bfs = 0;  // 1: plain breadth-first rounds (no banding, launches immediately)
+
 struct PQItem {
     double key;
     int kind;  // 0 window, 1 vertex
@@ -711,8 +722,8 @@ struct Geo {
     static double key_of(const Win& w)
     {
         double m;
-        if (w.sx < w.b0) m = std::hypot(w.sx - w.b0, w.sy);
-        else if (w.sx > w.b1) m = std::hypot(w.sx - w.b1, w.sy);
+        if (w.sx < w.b0) m = len2(w.sx - w.b0, w.sy);
+        else if (w.sx > w.b1) m = len2(w.sx - w.b1, w.sy);
         else m = std::fabs(w.sy);
         return w.sigma + m;
     }
@@ -726,7 +737,7 @@ struct Geo {
         double dA = W.lab[A], dB = W.lab[B];
         if (dA < kInf) {
             double a = dA - w.sigma;
-            double fb0 = std::hypot(w.b0 - w.sx, w.sy) - a - w.b0;
+            double fb0 = len2(w.b0 - w.sx, w.sy) - a - w.b0;
             if (fb0 > 0) {
                 if (a + w.sx <= 0) return false;
                 double xs = (w.sx * w.sx + w.sy * w.sy - a * a) / (2.0 * (a + w.sx));
@@ -738,7 +749,7 @@ struct Geo {
             double a = dB - w.sigma;
             double sxm = L - w.sx;
             double xm = L - w.b1;
-            double fb1 = std::hypot(xm - sxm, w.sy) - a - xm;
+            double fb1 = len2(xm - sxm, w.sy) - a - xm;
             if (fb1 > 0) {
                 if (a + sxm <= 0) return false;
                 double xs = (sxm * sxm + w.sy * w.sy - a * a) / (2.0 * (a + sxm));
@@ -751,7 +762,7 @@ struct Geo {
         double dC = W.lab[C];
         if (dC < kInf) {
             double cx = M.CX[3 * w.g + w.j], cy = M.CY[3 * w.g + w.j];
-            double m0 = std::hypot(cx - w.b0, cy), m1 = std::hypot(cx - w.b1, cy);
+            double m0 = len2(cx - w.b0, cy), m1 = len2(cx - w.b1, cy);
             double key = key_of(w);
             if (dC + std::max(m0, m1) < key) return false;
         }
@@ -775,7 +786,7 @@ struct Geo {
     {
         if (w.sigma == 0) {
             double ux = px - w.sx, uy = py - w.sy;
-            double l = std::hypot(ux, uy);
+            double l = len2(ux, uy);
             ux /= l;
             uy /= l;
             dx = w.c * ux - w.s * uy;
@@ -822,12 +833,12 @@ struct Geo {
                 double py = t.b[(j + 2) % 3] * cy;
                 double xp = w.sx + (px - w.sx) * (-w.sy) / (py - w.sy);
                 if (xp >= w.b0 - tol && xp <= w.b1 + tol) {
-                    double d = w.sigma + std::hypot(px - w.sx, py - w.sy);
+                    double d = w.sigma + len2(px - w.sx, py - w.sy);
                     if (d < t.best) {
                         double dx, dy;
                         start_dir(w, px, py, dx, dy);
                         double ux = px - w.sx, uy = py - w.sy;
-                        double ul = std::hypot(ux, uy);
+                        double ul = len2(ux, uy);
                         double te[3];
                         for (int c = 0; c < 3; ++c) te[c] = (ux * ex[c] + uy * ey[c]) / ul;
                         update_target(t, d, dx, dy, te);
@@ -840,21 +851,21 @@ struct Geo {
         if (xC >= w.b0 - tol && xC <= w.b1 + tol) {
             double dx, dy;
             start_dir(w, cx, cy, dx, dy);
-            propose(C, w.sigma + std::hypot(cx - w.sx, cy - w.sy), dx, dy);
+            propose(C, w.sigma + len2(cx - w.sx, cy - w.sy), dx, dy);
         }
         if (w.b0 <= tol) {
             double dx, dy;
             start_dir(w, 0, 0, dx, dy);
-            propose(A, w.sigma + std::hypot(w.sx, w.sy), dx, dy);
+            propose(A, w.sigma + len2(w.sx, w.sy), dx, dy);
         }
         if (w.b1 >= L - tol) {
             double dx, dy;
             start_dir(w, L, 0, dx, dy);
-            propose(B, w.sigma + std::hypot(L - w.sx, w.sy), dx, dy);
+            propose(B, w.sigma + len2(L - w.sx, w.sy), dx, dy);
         }
         // children
         if (w.b0 < xC) {  // left: exit edge C->A (local j+2), new frame origin A, x toward C
-            double n = std::hypot(cx, cy);
+            double n = len2(cx, cy);
             double ux = cx / n, uy = cy / n;
             double isx = ux * w.sx + uy * w.sy, isy = -uy * w.sx + ux * w.sy;
             auto proj = [&](double x) {
@@ -884,7 +895,7 @@ struct Geo {
         }
         if (w.b1 > xC) {  // right: exit edge B->C (local j+1), new frame origin C, x toward B
             double bx = L - cx, by = -cy;
-            double n = std::hypot(bx, by);
+            double n = len2(bx, by);
             double ux = bx / n, uy = by / n;
             double rx = w.sx - cx, ry = w.sy - cy;
             double isx = ux * rx + uy * ry, isy = -uy * rx + ux * ry;
@@ -963,7 +974,7 @@ struct Geo {
         for (int k = 0; k < 3; ++k) {
             int v = M.F[3 * f0 + k];
             double dx = P2[k][0] - S2[0], dy = P2[k][1] - S2[1];
-            double l = std::hypot(dx, dy);
+            double l = len2(dx, dy);
             double d3[3];
             sub3(vp(M, v), S, d3);
             propose(v, norm3(d3), dx / l, dy / l);
@@ -984,10 +995,14 @@ struct Geo {
             w.b0 = 0;
             w.b1 = L;
             double ddx = P2[(k + 1) % 3][0] - P2[k][0], ddy = P2[(k + 1) % 3][1] - P2[k][1];
-            double dl = std::hypot(ddx, ddy);
+            double dl = len2(ddx, ddy);
             w.c = -ddx / dl;
             w.s = -ddy / dl;
             push_win(w);
+        }
+        if (g_order == 1) {
+            run_rounds(earlyExit);
+            return;
         }
         long long pops = 0;
         while (!pq.empty()) {
@@ -1011,6 +1026,58 @@ struct Geo {
             }
         }
     }
+
+    // distance-banded rounds over the same window / launch events (drains the priority queue into lists)
+    void run_rounds(bool earlyExit)
+    {
+        std::vector<int> front, pend;
+        std::vector<char> launchedWith;  // unused: launched label tracked in lastLaunch
+        std::unordered_map<int, double> lastLaunch;
+        auto drain = [&](std::vector<int>& fr, std::vector<int>& pe) {
+            while (!pq.empty()) {
+                PQItem it = pq.top();
+                pq.pop();
+                if (it.kind == 0) fr.push_back(it.idx);
+                else pe.push_back(it.idx);
+            }
+        };
+        drain(front, pend);
+        long long rounds = 0;
+        while (!front.empty() || !pend.empty()) {
+            if (++rounds > 100000) break;
+            double mk = kInf;
+            for (int w : front) mk = std::min(mk, key_of(wins[w]));
+            for (int v : pend) mk = std::min(mk, W.lab[v]);
+            if (mk > cutoff) break;
+            if (earlyExit) {
+                bool done = true;
+                for (auto& t : T)
+                    if (!(final_candidate(t) <= mk)) { done = false; break; }
+                if (done) break;
+            }
+            double thr = g_bfs ? kInf : mk + g_delta;
+            std::vector<int> nf, np;
+            for (int v : pend) {
+                double d = W.lab[v];
+                if (d > thr) { np.push_back(v); continue; }
+                auto itl = lastLaunch.find(v);
+                if (itl != lastLaunch.end() && itl->second == d) continue;
+                lastLaunch[v] = d;
+                launch(v);
+            }
+            drain(nf, np);
+            for (int w : front) {
+                if (key_of(wins[w]) > thr) { nf.push_back(w); continue; }
+                process(wins[w]);
+                drain(nf, np);
+            }
+            front.swap(nf);
+            pend.swap(np);
+        }
+        roundsUsed = rounds;
+    }
+
+    long long roundsUsed = 0;
 
     double final_candidate(const Target& t) const
     {
@@ -1126,7 +1193,7 @@ struct BF {
     {
         // third point at distance la from a and lb from b, on the given side of a->b (side=+1 left)
         double dx = b[0] - a[0], dy = b[1] - a[1];
-        double L = std::hypot(dx, dy);
+        double L = len2(dx, dy);
         double x = (la * la - lb * lb + L * L) / (2 * L);
         double y = std::sqrt(std::max(0.0, la * la - x * x));
         double ux = dx / L, uy = dy / L;
@@ -1161,7 +1228,7 @@ struct BF {
                 Y[0] = P[k][0];
                 Y[1] = P[k][1];
             }
-            double d = std::hypot(Y[0] - X[0], Y[1] - X[1]);
+            double d = len2(Y[0] - X[0], Y[1] - X[1]);
             if (d < best && valid_segment(X, Y)) best = d;
         }
         if (depth >= maxDepth) return;
@@ -1177,7 +1244,7 @@ struct BF {
             double ex = bpt[0] - a[0], ey = bpt[1] - a[1];
             double tt = ((X[0] - a[0]) * ex + (X[1] - a[1]) * ey) / (ex * ex + ey * ey);
             tt = std::max(0.0, std::min(1.0, tt));
-            double md = std::hypot(a[0] + tt * ex - X[0], a[1] + tt * ey - X[1]);
+            double md = len2(a[0] + tt * ex - X[0], a[1] + tt * ey - X[1]);
             if (md >= best) continue;
             int j = t % 3;  // g: F[g][j] = F[f][k+1], F[g][j+1] = F[f][k]
             double Q[3][2];
@@ -1270,6 +1337,13 @@ struct BF {
 // C API (ctypes)
 // ======================================================================================================================
 extern "C" {
+
+void oracle_set_order(int order, double delta, int bfs)
+{
+    g_order = order;
+    g_delta = delta;
+    g_bfs = bfs;
+}
 
 void* oracle_mesh_create(const double* V, int nV, const int* F, int nF)
 {

@@ -36,13 +36,21 @@ def test_walk_matches_oracle(gpu, oracle_mod, mesh, scale):
     vel = _tangent(V, F, f, rng, 1.0)
     fo, bo, do, to, so, co = OM.transport(f, b, disp, vel[:, None, :])
     fg, bg, dg, tg, sg, cg = api.transport_batch(ctx, M, f, b, disp, vel[:, None, :])
-    assert np.all(so == 0) and np.all(sg == 0)
-    assert cg == int(co.sum()) and cg > 0
-    assert np.array_equal(fg, fo)
-    # edge crossings use the same IEEE operations on both sides (no FMA contraction): bitwise equal
-    np.testing.assert_array_equal(bg, bo)
-    np.testing.assert_array_equal(tg[:, 0], to[:, 0])
-    np.testing.assert_array_equal(dg, do)
+    assert np.all(so == 0) and np.all(sg == 0), (np.unique(so), np.unique(sg))
+    vertex = co >> 16
+    edge = co & 0xFFFF
+    assert cg == int(edge.sum() + vertex.sum()) and cg > 0
+    mism = np.nonzero(fg != fo)[0]
+    assert len(mism) == 0, ("face mismatch", mism[:10], vertex[mism[:10]], edge[mism[:10]])
+    # walks with edge crossings only use the same IEEE operations on both sides (no FMA contraction): bitwise
+    # equal; vertex crossings evaluate acos/sin/cos (libm vs CUDA) and are compared with a tolerance
+    e = vertex == 0
+    np.testing.assert_array_equal(bg[e], bo[e])
+    np.testing.assert_array_equal(tg[e, 0], to[e, 0])
+    np.testing.assert_array_equal(dg[e], do[e])
+    if (~e).any():
+        np.testing.assert_allclose(bg[~e], bo[~e], atol=1e-9)
+        np.testing.assert_allclose(tg[~e, 0], to[~e, 0], atol=1e-9)
 
 
 def test_distances_full_mesh_match_oracle(gpu, oracle_mod):
@@ -87,7 +95,8 @@ def test_distances_patch_mode_match_oracle(gpu, oracle_mod, cutoff):
     off, idx, mc = OM.candidates(f, b, 0.3)
     d, ts, te, st = api.distance_batch(ctx, M, f, b, off, f[idx], b[idx], submesh=True, max_dist=0.3,
                                        threshold=mc, cutoff=cutoff)
-    assert np.all(st == 0)
+    stats = api.distance_batch.last_stats
+    assert np.all(st == 0), (np.nonzero(st)[0][:10], stats[st != 0][:5])
     do, tso, _ = OM.neighbor_distances(f, b, off, idx, mc, 1, 0.3, cutoff)
     if not math.isfinite(cutoff):
         do = np.where(np.isfinite(do), do, 0.6)
@@ -173,3 +182,39 @@ def test_pair_sets_identical(gpu, oracle_mod):
     prm = OM.params(0, k=1.0 / sigma ** 2, sigma=sigma, rng=sigma, submesh=1, max_dist=sigma, cutoff=sigma)
     fo, _, _ = OM.forces(f, b, prm)
     np.testing.assert_allclose(fg, fo, atol=1e-11)
+
+
+def test_batched_systems_match_oracle(gpu, oracle_mod):
+    """Three independent systems (different meshes, counts and ranges) in one system object: each must evolve
+    exactly as it does alone (velocity Verlet, cell lists, patches, 20 steps)."""
+    api, ctx = gpu
+    rng = np.random.default_rng(7)
+    specs = [ms.icosphere(3), ms.torus(50, 25, 3.0, 1.0), ms.ellipsoid(3, (1.5, 1.0, 0.7))]
+    counts = [60, 150, 40]
+    meshes, params, states = [], [], []
+    for (V, F), n in zip(specs, counts):
+        sigma = ms.sigma_for_area_fraction(ms.total_area(V, F), n, 0.4)
+        f, b = ms.area_weighted_positions(V, F, n, rng)
+        vel = ms.tangent_velocities(V, F, f, 0.05, rng)
+        meshes.append(api.Mesh(V, F))
+        params.append(api.make_params("nve", "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=sigma, submesh=True,
+                                      max_dist=sigma, cutoff=sigma, dt=0.002))
+        states.append((V, F, f, b, vel, sigma))
+    S = api.System(ctx, meshes, counts, params)
+    S.set_state(np.concatenate([s[2] for s in states]), np.concatenate([s[3] for s in states]),
+                np.concatenate([s[4] for s in states]), np.zeros((sum(counts), 3)))
+    S.step(20, graph=True)
+    bits, cnt = S.check()
+    assert bits == 0, cnt
+    fg, bg, vg, _ = S.get_state()
+    off = np.cumsum([0] + counts)
+    for k, (V, F, f, b, vel, sigma) in enumerate(states):
+        OM = oracle_mod.OracleMesh(V, F)
+        prm = OM.params(0, k=1.0 / sigma ** 2, sigma=sigma, rng=sigma, submesh=1, max_dist=sigma, cutoff=sigma,
+                        dt=0.002)
+        fo, bo, vo, _, _, err, _ = OM.simulate(0, 20, f, b, vel, np.zeros((len(f), 3)), prm)
+        assert err == 0
+        a, e = off[k], off[k + 1]
+        pe = np.linalg.norm(OM.r3(fg[a:e], bg[a:e]) - OM.r3(fo, bo), axis=1)
+        assert pe.max() < 1e-8, (k, pe.max())
+        np.testing.assert_allclose(vg[a:e], vo, atol=1e-8)
