@@ -24,7 +24,7 @@ EXPORTS = [
     "cssg_system_pairs", "cssg_system_chain", "cssg_system_timing", "cssg_system_last_times",
     "cssg_system_reset_thermostat", "cssg_system_kernels_per_step", "cssg_diag_fp64_peak",
     "cssg_system_create_batched", "cssg_mlp_param_count", "cssg_screen_features", "cssg_mlp_infer", "cssg_mlp_grad",
-    "cssg_mlp_adam",
+    "cssg_mlp_adam", "cssg_system_set_screen", "cssg_system_screen_counters",
 ]
 
 
@@ -97,6 +97,8 @@ def load(build_if_missing: bool = True):
     L.cssg_system_kernels_per_step.argtypes = [P, P]
     L.cssg_diag_fp64_peak.argtypes = [P, P]
     L.cssg_mlp_param_count.argtypes = []
+    L.cssg_system_set_screen.argtypes = [P, P, D, I]
+    L.cssg_system_screen_counters.argtypes = [P, P]
     L.cssg_screen_features.argtypes = [P, P, D, I, P, P, P, P, P, P]
     L.cssg_mlp_infer.argtypes = [P, P, I, P, P, P]
     L.cssg_mlp_grad.argtypes = [P, P, P, I, P, P, P]

@@ -29,18 +29,30 @@ def _torch():
 
 
 class Context:
-    """cssg_ctx: a CUDA stream (torch's current stream unless one is given)."""
+    """cssg_ctx: the CUDA stream the library launches on.
 
-    def __init__(self, device: int = 0, stream: int | None = None):
+    By default a dedicated torch stream is created and shared with the library (torch's default stream cannot be
+    used: it is the legacy NULL stream, which does not support graph capture), so torch copies and events issued
+    under ``with ctx.use():`` are ordered with the library's kernels."""
+
+    def __init__(self, device: int = 0, stream=None):
         L = _lib.load()
         torch = _torch()
-        if stream is None:
-            with torch.cuda.device(device):
-                stream = torch.cuda.current_stream().cuda_stream
         self.device = device
+        if stream is None:
+            self.tstream = torch.cuda.Stream(device=device)
+        elif isinstance(stream, int):
+            self.tstream = torch.cuda.ExternalStream(stream, device=device)
+        else:
+            self.tstream = stream
         h = ctypes.c_void_p()
-        check(L.cssg_ctx_create(device, ctypes.c_void_p(stream), ctypes.byref(h)), "cssg_ctx_create")
+        check(L.cssg_ctx_create(device, ctypes.c_void_p(self.tstream.cuda_stream), ctypes.byref(h)),
+              "cssg_ctx_create")
         self.h = h
+
+    def use(self):
+        """Context manager: make the library's stream torch's current stream."""
+        return _torch().cuda.stream(self.tstream)
 
     @property
     def stream(self):
@@ -82,6 +94,11 @@ class Mesh:
 
 def transport_batch(ctx: Context, mesh: Mesh, face, bary, disp, transport=None):
     """Batched transportParticleAndVectors on host arrays; returns (face, bary, disp, transport, status)."""
+    with ctx.use():
+        return _transport_batch(ctx, mesh, face, bary, disp, transport)
+
+
+def _transport_batch(ctx, mesh, face, bary, disp, transport):
     torch = _torch()
     dev = f"cuda:{ctx.device}"
     n = len(face)
@@ -108,6 +125,13 @@ def transport_batch(ctx: Context, mesh: Mesh, face, bary, disp, transport=None):
 def distance_batch(ctx: Context, mesh: Mesh, src_face, src_bary, cand_off, cand_face, cand_bary, submesh=False,
                    max_dist=1.0, threshold=None, cutoff=math.inf):
     """Batched triangulatedMeshSpace::distance over sources with CSR candidate lists (host arrays in and out)."""
+    with ctx.use():
+        return _distance_batch(ctx, mesh, src_face, src_bary, cand_off, cand_face, cand_bary, submesh, max_dist,
+                               threshold, cutoff)
+
+
+def _distance_batch(ctx, mesh, src_face, src_bary, cand_off, cand_face, cand_bary, submesh, max_dist, threshold,
+                    cutoff):
     torch = _torch()
     dev = f"cuda:{ctx.device}"
     ns = len(src_face)
@@ -263,6 +287,21 @@ class System:
         check(_lib.load().cssg_system_chain(self.h, _np_ptr(out), cap), "cssg_system_chain")
         return out
 
+    def set_screen(self, params=None, margin: float = 0.0, enable: bool = True):
+        """Learned screen: params = FP32 MLP parameters (host array); enable=False returns to the exact path."""
+        ptr = None
+        arr = None
+        if params is not None:
+            arr = np.ascontiguousarray(np.asarray(params, dtype=np.float32))
+            ptr = _np_ptr(arr)
+        check(_lib.load().cssg_system_set_screen(self.h, ptr, float(margin), int(bool(enable))),
+              "cssg_system_set_screen")
+
+    def screen_counters(self):
+        out = np.zeros(3, dtype=np.uint64)
+        check(_lib.load().cssg_system_screen_counters(self.h, _np_ptr(out)), "cssg_system_screen_counters")
+        return {"pairs": int(out[0]), "screened": int(out[1]), "tc_errors": int(out[2])}
+
     def timing(self, enable: bool):
         check(_lib.load().cssg_system_timing(self.h, int(bool(enable))), "cssg_system_timing")
 
@@ -283,11 +322,14 @@ def screen_features(ctx: Context, mesh: Mesh, sigma: float, pi, pj, face, pos):
     """Pair features on the device; all inputs torch tensors on the context's device. Returns (X bf16, chord/s)."""
     torch = _torch()
     n = int(pi.numel())
-    X = torch.zeros((max(n, 1), 16), dtype=torch.bfloat16, device=pi.device)
-    c = torch.zeros(max(n, 1), dtype=torch.float32, device=pi.device)
+    torch.cuda.current_stream(pi.device).synchronize()
+    with ctx.use():
+        X = torch.zeros((max(n, 1), 16), dtype=torch.bfloat16, device=pi.device)
+        c = torch.zeros(max(n, 1), dtype=torch.float32, device=pi.device)
     check(_lib.load().cssg_screen_features(ctx.h, mesh.h, float(sigma), n, _P(pi.data_ptr()), _P(pj.data_ptr()),
                                            _P(face.data_ptr()), _P(pos.data_ptr()), _P(X.data_ptr()),
                                            _P(c.data_ptr())), "cssg_screen_features")
+    ctx.synchronize()
     return X[:n], c[:n]
 
 
@@ -295,8 +337,10 @@ def mlp_infer(ctx: Context, X, params):
     """Tensor-core inference; X bf16 [n, 16], params float32 [P] (torch, device)."""
     torch = _torch()
     n = int(X.shape[0])
-    y = torch.zeros(max(n, 1), dtype=torch.float32, device=X.device)
-    err = torch.zeros(1, dtype=torch.int32, device=X.device)
+    torch.cuda.current_stream(X.device).synchronize()
+    with ctx.use():
+        y = torch.zeros(max(n, 1), dtype=torch.float32, device=X.device)
+        err = torch.zeros(1, dtype=torch.int32, device=X.device)
     check(_lib.load().cssg_mlp_infer(ctx.h, _P(X.data_ptr()), n, _P(params.data_ptr()), _P(y.data_ptr()),
                                      _P(err.data_ptr())), "cssg_mlp_infer")
     ctx.synchronize()
@@ -307,13 +351,17 @@ def mlp_infer(ctx: Context, X, params):
 
 def mlp_grad(ctx: Context, X, y, params):
     torch = _torch()
-    g = torch.zeros(mlp_param_count(), dtype=torch.float32, device=X.device)
-    loss = torch.zeros(1, dtype=torch.float32, device=X.device)
+    torch.cuda.current_stream(X.device).synchronize()
+    with ctx.use():
+        g = torch.zeros(mlp_param_count(), dtype=torch.float32, device=X.device)
+        loss = torch.zeros(1, dtype=torch.float32, device=X.device)
     check(_lib.load().cssg_mlp_grad(ctx.h, _P(X.data_ptr()), _P(y.data_ptr()), int(X.shape[0]),
                                     _P(params.data_ptr()), _P(g.data_ptr()), _P(loss.data_ptr())), "cssg_mlp_grad")
+    ctx.synchronize()
     return g, loss
 
 
 def mlp_adam(ctx: Context, params, grad, m, v, batch: int, lr: float, step: int):
     check(_lib.load().cssg_mlp_adam(ctx.h, _P(params.data_ptr()), _P(grad.data_ptr()), _P(m.data_ptr()),
                                     _P(v.data_ptr()), int(batch), ctypes.c_float(lr), int(step)), "cssg_mlp_adam")
+    ctx.synchronize()

@@ -14,6 +14,8 @@ struct DevMesh {
     const int* twin;            // 3 nF: face*3 + local edge of the neighbour across local edge k, -1 on a border
     const double* N;            // 3 nF unit face normals
     const double* geom;         // 9 nF: [9f + 3k + 0] edge length, [+1],[+2] third vertex in the edge frame
+    const double* exitu;        // 12 nF: entering through edge k, unit directions of the exit edges C->A and B->C in
+                                //        the edge-k frame: [12f + 4k + 0..1] (C - A)/|C - A|, [+2..3] (B - C)/|B - C|
     const int* vfStart;         // nV + 1: vertex -> incident faces (CSR)
     const int* vfList;
     const int* ringStart;       // nV + 1: clockwise neighbour ring of closed vertices (throughVertex order)
@@ -32,7 +34,7 @@ struct cssg_mesh {
     double area;
     double meanEdge;
     double meanFaceArea;
-    void* buffers[12];
+    void* buffers[14];
 };
 
 struct cssg_ctx {
@@ -74,7 +76,8 @@ struct GeoCaps {
 // serves any number of them: sources carry their system index.
 struct SysDesc {
     DevMesh mesh;
-    int searchMode;   // 0 CSR candidate lists (distance API), 1 cell list, 2 all-to-all
+    int searchMode;   // 0 CSR candidate lists (distance API), 1 cell list, 2 all-to-all,
+                      // 3 CSR of candidate particle indices with screen flags (learned-screen path)
     int bigBin;       // patches too large for the regular tables: sources go straight to the large-table pass
     int submesh;      // reference patches
     int forceKind;    // 0 harmonic, 1 gaussian
@@ -104,7 +107,9 @@ struct GeoLaunch {
     const int* candOff;
     const int* candFace;
     const double* candBary;
-    const double* threshold;     // nullable (CSR mode): per-source patch radius
+    const double* threshold;     // nullable (CSR modes): per-source patch radius
+    const int* candJ;            // mode 3: candidate particle index per CSR entry
+    const unsigned char* candSkip;  // mode 3: 1 = screened out (its face still completes the patch, not queried)
     // ... or neighbour search (system mode): all particles + the shared cell arrays
     const int* partFace;
     const double* partBary;
@@ -144,3 +149,15 @@ size_t cssg_geo_smem_per_warp(const GeoCaps& c);
 // Fills slots with their initial (empty) state; call once after allocating the scratch.
 void cssg_geo_init_scratch(void* scratch, size_t slotBytes, int nSlots, const GeoCaps& c, cudaStream_t s);
 void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s);
+// candidate lists for the learned-screen path: per source (warp) the cell-list candidates in reference order,
+// padded rows of `cap` entries; count[i] (> cap: overflow) and the largest candidate chord maxChord[i]
+void cssg_launch_candidates(const GeoLaunch& L, int n, int cap, int* candJ, int* count, double* maxChord,
+                            cudaStream_t s);
+
+// ---- learned screen (mlp.cu) ---------------------------------------------------------------------------------------
+// features + tensor-core MLP + decision for nPairs CSR pairs (pi -> pj): skip[p] = 1 when the predicted distance
+// |chord| + sigma * yhat exceeds sigma * (1 + margin).  X (nPairs x 16 BF16), chord, yhat are caller scratch.
+// maxPairs bounds the launch; the actual count is read from nPairsDev on the device
+void cssg_launch_screen(const SysDesc* sys, const int* sysOf, int maxPairs, const int* nPairsDev, const int* pi,
+                        const int* pj, const int* face, const double* pos, void* X, float* chord, const float* params,
+                        float* yhat, unsigned char* skip, double margin, int* errFlag, int sms, cudaStream_t s);

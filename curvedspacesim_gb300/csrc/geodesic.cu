@@ -43,8 +43,8 @@ constexpr unsigned FULL = 0xffffffffu;
 
 struct __align__(16) Win {
     double b0, b1, sx, sy, sigma, c, s;
-    int he;   // entered face * 4 + local edge
-    int src;  // -1: the source, else the vertex pseudo-source
+    int he;     // entered face * 4 + local edge
+    float key;  // smallest path length over the interval when queued (ordering and banding only)
 };
 
 // loads of table entries other lanes may be writing (shared-memory tables: plain volatile loads)
@@ -86,9 +86,12 @@ struct Slot {
     Win* wA;
     Win* wB;
     Win* wlog;
+    int* lognext;  // per log entry: next entry of the same face
+    int* flog;     // per face-table slot: first log entry of that face
     int* lA;
     int* lB;
     double* ld;  // per launch entry: label, start direction (x, y) it launched with
+    int* lpre;   // per launch entry: exclusive prefix of the launched vertices' face counts
     int* bA;
     int* bB;
 };
@@ -120,9 +123,12 @@ __host__ __device__ inline size_t carve(const GeoCaps& c, char* base, Slot* S)
     CARVE(wA, Win, c.CW);
     CARVE(wB, Win, c.CW);
     CARVE(wlog, Win, c.CLOG);
+    CARVE(lognext, int, c.CLOG);
+    CARVE(flog, int, c.CF);
     CARVE(lA, int, c.CL);
     CARVE(lB, int, c.CL);
     CARVE(ld, double, 3 * c.CL);
+    CARVE(lpre, int, c.CL + 1);
     CARVE(bA, int, c.CF);
     CARVE(bB, int, c.CF);
 #undef CARVE
@@ -253,18 +259,25 @@ __device__ __forceinline__ bool in_domain(const DevMesh& M, const Slot& S, const
     return ffind(S, C.CF, g) >= 0;
 }
 
-__device__ bool trim(const DevMesh& M, const Slot& S, const GeoCaps& C, Win& w)
+// Remove the parts of the window that a path through an endpoint vertex of its edge beats.  The excess of the
+// window's path over the vertex path is monotone along the edge, so the dominated part is an interval at that end,
+// bounded by the root of a linear equation.  The tests compare squared lengths (no square roots); the opposite
+// vertex can only discard the window as a whole and is tested in FP32 with a 1e-5 relative safety margin (it is a
+// pruning test: a conservative answer keeps the window).
+__device__ __noinline__ bool trim(const DevMesh& M, const Slot& S, const GeoCaps& C, Win& w)
 {
     const int g = w.he >> 2, j = w.he & 3;
     const double L = M.geom[9 * g + 3 * j];
     const int A = M.F[3 * g + j], B = M.F[3 * g + (j + 1) % 3], Cv = M.F[3 * g + (j + 2) % 3];
+    const double sy2 = w.sy * w.sy;
     double dA = vlabel(S, C.CV, A);
     if (dA < CUDART_INF) {
         double a = dA - w.sigma;
-        double fb0 = len2(w.b0 - w.sx, w.sy) - a - w.b0;
-        if (fb0 > 0) {
+        // dominated at b0 <=> |I - (b0,0)| > a + b0
+        double r = a + w.b0, dx = w.b0 - w.sx;
+        if (r < 0 || dx * dx + sy2 > r * r) {
             if (a + w.sx <= 0) return false;
-            double xs = (w.sx * w.sx + w.sy * w.sy - a * a) / (2.0 * (a + w.sx));
+            double xs = (w.sx * w.sx + sy2 - a * a) / (2.0 * (a + w.sx));
             if (xs >= w.b1) return false;
             w.b0 = fmax(w.b0, xs);
         }
@@ -273,31 +286,36 @@ __device__ bool trim(const DevMesh& M, const Slot& S, const GeoCaps& C, Win& w)
     if (dB < CUDART_INF) {
         double a = dB - w.sigma;
         double sxm = L - w.sx, xm = L - w.b1;
-        double fb1 = len2(xm - sxm, w.sy) - a - xm;
-        if (fb1 > 0) {
+        double r = a + xm, dx = xm - sxm;
+        if (r < 0 || dx * dx + sy2 > r * r) {
             if (a + sxm <= 0) return false;
-            double xs = (sxm * sxm + w.sy * w.sy - a * a) / (2.0 * (a + sxm));
+            double xs = (sxm * sxm + sy2 - a * a) / (2.0 * (a + sxm));
             if (L - xs <= w.b0) return false;
             w.b1 = fmin(w.b1, L - xs);
         }
     }
     double dC = vlabel(S, C.CV, Cv);
     if (dC < CUDART_INF) {
-        double cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
-        double m0 = len2(cx - w.b0, cy), m1 = len2(cx - w.b1, cy);
-        if (dC + fmax(m0, m1) < key_of(w)) return false;
+        float cx = (float)M.geom[9 * g + 3 * j + 1], cy = (float)M.geom[9 * g + 3 * j + 2];
+        float b0 = (float)w.b0, b1 = (float)w.b1, sx = (float)w.sx, sy = (float)w.sy;
+        float m = fmaxf(sqrtf((cx - b0) * (cx - b0) + cy * cy), sqrtf((cx - b1) * (cx - b1) + cy * cy));
+        float near = (sx < b0) ? sqrtf((sx - b0) * (sx - b0) + sy * sy)
+                                : (sx > b1 ? sqrtf((sx - b1) * (sx - b1) + sy * sy) : fabsf(sy));
+        if ((float)dC + m < ((float)w.sigma + near) * (1.0f - 1e-5f)) return false;
     }
     return w.b1 - w.b0 > 1e-14 * L;
 }
 
-__device__ void push_win(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, Win w)
+__device__ __noinline__ void push_win(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, Win w)
 {
     const int g = w.he >> 2, j = w.he & 3;
     if (g == src.f0 || !in_domain(M, S, C, src, g)) return;
     w.b0 = fmax(0.0, w.b0);
     w.b1 = fmin(M.geom[9 * g + 3 * j], w.b1);
     if (!trim(M, S, C, w)) return;
-    if (key_of(w) > src.cutoff) return;
+    const double key = key_of(w);
+    if (key > src.cutoff) return;
+    w.key = (float)key;
     int pos = atomicAdd(&ctl->nB, 1);
     if (pos >= C.CW) {
         atomicExch(&ctl->err, CSSG_ST_CAPACITY);
@@ -338,7 +356,15 @@ __device__ __forceinline__ void propose(const Slot& S, const GeoCaps& C, WarpCtl
     }
 }
 
-__device__ bool launchable(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int v)
+// a window's proposal for the vertex at (px, py) of its frame; the start direction is computed only if it wins
+__device__ __forceinline__ void propose_from(const Slot& S, const GeoCaps& C, WarpCtl* ctl, const Win& w, int v,
+                                             double px, double py, VRec& rec)
+{
+    propose(S, C, ctl, v, w.sigma + len2(px - w.sx, py - w.sy), 0.0, 0.0, rec);
+    if (rec.slot >= 0) start_dir(w, px, py, rec.dx, rec.dy);
+}
+
+__device__ __noinline__ bool launchable(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int v)
 {
     if (M.vflag[v] & (VF_BORDER | VF_SADDLE)) return true;
     if (src.full) return false;
@@ -383,9 +409,14 @@ __device__ void process(const DevMesh& M, const Slot& S, const GeoCaps& C, const
         int head = ldv(&S.fhead[fh]);
         if (head >= 0) {
             int pos = atomicAdd(&ctl->nLog, 1);
-            if (pos < C.CLOG) S.wlog[pos] = w;
-            else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+            if (pos < C.CLOG) {
+                S.wlog[pos] = w;
+                S.lognext[pos] = atomicExch(&S.flog[fh], pos);
+            } else {
+                atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+            }
             for (int t = head; t >= 0; t = S.tnext[t]) {
+                if (S.tidx[t] < 0) continue;
                 double b1 = S.tb[3 * t + (j + 1) % 3], b2 = S.tb[3 * t + (j + 2) % 3];
                 double px = b1 * L + b2 * cx, py = b2 * cy;
                 double xp = w.sx + (px - w.sx) * (-w.sy) / (py - w.sy);
@@ -397,30 +428,16 @@ __device__ void process(const DevMesh& M, const Slot& S, const GeoCaps& C, const
         }
     }
     double xC = w.sx + (cx - w.sx) * (-w.sy) / (cy - w.sy);
-    if (xC >= w.b0 - tol && xC <= w.b1 + tol) {
-        double dx, dy;
-        start_dir(w, cx, cy, dx, dy);
-        propose(S, C, ctl, Cv, w.sigma + len2(cx - w.sx, cy - w.sy), dx, dy, rec[0]);
-    }
-    if (w.b0 <= tol) {
-        double dx, dy;
-        start_dir(w, 0, 0, dx, dy);
-        propose(S, C, ctl, A, w.sigma + len2(w.sx, w.sy), dx, dy, rec[1]);
-    }
-    if (w.b1 >= L - tol) {
-        double dx, dy;
-        start_dir(w, L, 0, dx, dy);
-        propose(S, C, ctl, B, w.sigma + len2(L - w.sx, w.sy), dx, dy, rec[2]);
-    }
+    if (xC >= w.b0 - tol && xC <= w.b1 + tol) propose_from(S, C, ctl, w, Cv, cx, cy, rec[0]);
+    if (w.b0 <= tol) propose_from(S, C, ctl, w, A, 0.0, 0.0, rec[1]);
+    if (w.b1 >= L - tol) propose_from(S, C, ctl, w, B, L, 0.0, rec[2]);
     if (w.b0 < xC) {  // exit through edge C->A (local j+2); child frame: origin A, x toward C
         int t = M.twin[3 * g + (j + 2) % 3];
         if (t >= 0) {
-            double n = len2(cx, cy);
-            double ux = cx / n, uy = cy / n;
+            const double ux = M.exitu[12 * g + 4 * j], uy = M.exitu[12 * g + 4 * j + 1];
             double isx = ux * w.sx + uy * w.sy, isy = -uy * w.sx + ux * w.sy;
             Win c;
             c.he = (t / 3) * 4 + t % 3;
-            c.src = w.src;
             c.sigma = w.sigma;
             c.sx = isx;
             c.sy = isy;
@@ -446,14 +463,11 @@ __device__ void process(const DevMesh& M, const Slot& S, const GeoCaps& C, const
     if (w.b1 > xC) {  // exit through edge B->C (local j+1); child frame: origin C, x toward B
         int t = M.twin[3 * g + (j + 1) % 3];
         if (t >= 0) {
-            double bx = L - cx, by = -cy;
-            double n = len2(bx, by);
-            double ux = bx / n, uy = by / n;
+            const double ux = M.exitu[12 * g + 4 * j + 2], uy = M.exitu[12 * g + 4 * j + 3];
             double rx = w.sx - cx, ry = w.sy - cy;
             double isx = ux * rx + uy * ry, isy = -uy * rx + ux * ry;
             Win c;
             c.he = (t / 3) * 4 + t % 3;
-            c.src = w.src;
             c.sigma = w.sigma;
             c.sx = isx;
             c.sy = isy;
@@ -509,7 +523,7 @@ __device__ __forceinline__ void load_pt(const DevMesh& M, int f, const double* b
 }
 
 // final distance of target t: source face, logged windows and face-vertex labels
-__device__ double target_query(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int t, int nLog,
+__device__ __noinline__ double target_query(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int t, int nLog,
                                double* ts, double* te)
 {
     const int f = S.tface[t];
@@ -526,10 +540,11 @@ __device__ double target_query(const DevMesh& M, const Slot& S, const GeoCaps& C
     double best = CUDART_INF, bdx = 0, bdy = 0;
     int bw = -1;
     double bux = 0, buy = 0;
-    for (int e = 0; e < nLog; ++e) {
+    const int fh = ffind(S, C.CF, f);
+    for (int e = fh >= 0 ? __ldcg(&S.flog[fh]) : -1; e >= 0; e = S.lognext[e]) {
+        if (e >= nLog) break;
         const Win w = S.wlog[e];
         const int g = w.he >> 2;
-        if (g != f) continue;
         const int j = w.he & 3;
         const double L = M.geom[9 * g + 3 * j], cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
         double b1 = S.tb[3 * t + (j + 1) % 3], b2 = S.tb[3 * t + (j + 2) % 3];
@@ -584,12 +599,12 @@ __device__ double target_query(const DevMesh& M, const Slot& S, const GeoCaps& C
 }
 
 // candidate-based early exit: no queued window can improve any target any more
-__device__ bool settled(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int nT, double minKey,
+__device__ __noinline__ bool settled(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int nT, double minKey,
                         int lane)
 {
     bool ok = true;
     for (int t = lane; t < nT; t += 32) {
-        if (S.tface[t] == src.f0) continue;
+        if (S.tface[t] == src.f0 || S.tidx[t] < 0) continue;
         double b = bitsd(__ldcg(&S.tbest[t]));
         const double* P = &S.tp[3 * t];
         for (int c = 0; c < 3; ++c) {
@@ -633,18 +648,27 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     __syncwarp();
     // ---- targets ---------------------------------------------------------------------------------------------
     double maxChord2 = 0;
-    if (D.searchMode == 0) {
+    if (D.searchMode == 0 || D.searchMode == 3) {
         int beg = Lp.candOff[si], nT = Lp.candOff[si + 1] - beg;
         if (nT > C.CT) {
             if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
             nT = 0;
         }
         for (int t = lane; t < nT; t += 32) {
-            S.tface[t] = Lp.candFace[beg + t];
-            S.tidx[t] = beg + t;
-            for (int c = 0; c < 3; ++c) S.tb[3 * t + c] = Lp.candBary[3 * (beg + t) + c];
+            if (D.searchMode == 0) {
+                S.tface[t] = Lp.candFace[beg + t];
+                S.tidx[t] = beg + t;
+                for (int c = 0; c < 3; ++c) S.tb[3 * t + c] = Lp.candBary[3 * (beg + t) + c];
+            } else {
+                // screened-out candidates keep their face in the patch but are not queried: index stored as -(j+1)
+                int jj = Lp.candJ[beg + t];
+                S.tface[t] = Lp.partFace[jj];
+                S.tidx[t] = Lp.candSkip[beg + t] ? -(jj + 1) : jj;
+                for (int c = 0; c < 3; ++c) S.tb[3 * t + c] = Lp.partBary[3 * jj + c];
+            }
         }
         if (lane == 0) ctl->nT = nT;
+        if (D.searchMode == 3 && Lp.pairCount && lane == 0) Lp.pairCount[si] = nT;
     } else {
         // candidates j != i with chord^2 < range2 (cell list: 27 cells in (x, y, z) loop order; or all particles)
         const double* Pi = &Lp.srcPos[3 * si];
@@ -722,7 +746,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     // ---- domain: whole mesh or the reference patch ---------------------------------------------------------------
     src.full = !D.submesh;
     double r = D.maxDist;
-    if (D.searchMode == 0) {
+    if (D.searchMode == 0 || D.searchMode == 3) {
         if (Lp.threshold && Lp.threshold[si] < r) r = Lp.threshold[si];
     } else {
         double mc = sqrt(maxChord2);
@@ -841,7 +865,6 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             double sky = b0[(k + 2) % 3] * M.geom[9 * f0 + 3 * k + 2];
             Win w;
             w.he = (t / 3) * 4 + t % 3;
-            w.src = -1;
             w.sigma = 0;
             w.sx = L - skx;
             w.sy = fmin(-sky, -1e-15 * L);
@@ -883,81 +906,113 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             ctl->nLA = 0;
         }
         double mk = CUDART_INF;
-        for (int q = lane; q < nA; q += 32) mk = fmin(mk, key_of(S.wA[q]));
+        for (int q = lane; q < nA; q += 32) mk = fmin(mk, (double)S.wA[q].key);
         for (int q = lane; q < nP; q += 32) mk = fmin(mk, vlabel(S, C.CV, S.lB[q]));
         mk = warp_min(mk);
         __syncwarp();
         if (settled(M, S, C, src, nT, mk, lane)) break;
         const double thr = mk + Lp.delta;
-        // pseudo-source launches within the band (pass 1: windows + edge-path proposals); the rest stay queued
+        // pseudo-source launches within the band; the rest stay queued.  Decide per queued vertex, then spread the
+        // (vertex, incident face) pairs over the lanes.
         for (int q = lane; q < nP; q += 32) {
             int v = S.lB[q];
             int h = vfind(S, C.CV, v);
             S.ld[3 * q] = -1.0;
-            if (h < 0) continue;
-            unsigned long long lb = ldv(&S.vlab[h]);
-            double d = bitsd(lb);
-            if (d > thr) {
-                int pos = atomicAdd(&ctl->nLA, 1);
-                if (pos < C.CL) S.lA[pos] = v;
-                else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
-                continue;
+            int deg = 0;
+            if (h >= 0) {
+                unsigned long long lb = ldv(&S.vlab[h]);
+                double d = bitsd(lb);
+                if (d > thr) {
+                    int pos = atomicAdd(&ctl->nLA, 1);
+                    if (pos < C.CL) S.lA[pos] = v;
+                    else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                } else if (atomicExch(&S.vlaunched[h], lb) != lb) {  // not yet launched with this label
+                    S.ld[3 * q] = d;
+                    S.ld[3 * q + 1] = S.vtx[h];
+                    S.ld[3 * q + 2] = S.vty[h];
+                    deg = M.vfStart[v + 1] - M.vfStart[v];
+                    launches++;
+                }
             }
-            if (atomicExch(&S.vlaunched[h], lb) == lb) continue;  // already launched with this label
-            double tx = S.vtx[h], ty = S.vty[h];
-            S.ld[3 * q] = d;
-            S.ld[3 * q + 1] = tx;
-            S.ld[3 * q + 2] = ty;
-            launches++;
-            for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
-                int f = M.vfList[i];
-                if (!in_domain(M, S, C, src, f)) continue;
-                int k = 0;
-                while (M.F[3 * f + k] != v) ++k;
-                int e = (k + 1) % 3;
-                VRec r1, r2;
-                propose(S, C, ctl, M.F[3 * f + e], d + M.geom[9 * f + 3 * k], tx, ty, r1);
-                propose(S, C, ctl, M.F[3 * f + (k + 2) % 3], d + M.geom[9 * f + 3 * ((k + 2) % 3)], tx, ty, r2);
-                int t = M.twin[3 * f + e];
-                if (t < 0) continue;
-                Win c;
-                c.he = (t / 3) * 4 + t % 3;
-                c.src = v;
-                c.sigma = d;
-                double L = M.geom[9 * f + 3 * e];
-                c.sx = L - M.geom[9 * f + 3 * e + 1];
-                c.sy = -M.geom[9 * f + 3 * e + 2];
-                c.b0 = 0;
-                c.b1 = L;
-                c.c = tx;
-                c.s = ty;
-                push_win(M, S, C, src, ctl, c);
+            S.lpre[q] = deg;
+        }
+        __syncwarp();
+        // exclusive prefix of the face counts (warp scan over chunks of 32 entries)
+        int pairs = 0;
+        for (int base = 0; base < nP; base += 32) {
+            int q = base + lane;
+            int x = q < nP ? S.lpre[q] : 0;
+            int incl = x;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += y;
             }
+            __syncwarp();
+            if (q < nP) S.lpre[q] = pairs + incl - x;
+            pairs += __shfl_sync(FULL, incl, 31);
+        }
+        if (lane == 0) S.lpre[nP] = pairs;
+        __syncwarp();
+        // pass 1: windows on the opposite edges + edge-path proposals, one (vertex, face) pair per lane
+        for (int p = lane; p < pairs; p += 32) {
+            int lo = 0, hi = nP - 1;  // last entry with lpre <= p
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (S.lpre[mid] <= p) lo = mid;
+                else hi = mid - 1;
+            }
+            const int q = lo;
+            const int v = S.lB[q];
+            const double d = S.ld[3 * q], tx = S.ld[3 * q + 1], ty = S.ld[3 * q + 2];
+            const int f = M.vfList[M.vfStart[v] + (p - S.lpre[q])];
+            if (!in_domain(M, S, C, src, f)) continue;
+            int k = 0;
+            while (M.F[3 * f + k] != v) ++k;
+            int e = (k + 1) % 3;
+            VRec r1, r2;
+            propose(S, C, ctl, M.F[3 * f + e], d + M.geom[9 * f + 3 * k], tx, ty, r1);
+            propose(S, C, ctl, M.F[3 * f + (k + 2) % 3], d + M.geom[9 * f + 3 * ((k + 2) % 3)], tx, ty, r2);
+            int t = M.twin[3 * f + e];
+            if (t < 0) continue;
+            Win c;
+            c.he = (t / 3) * 4 + t % 3;
+            c.sigma = d;
+            double L = M.geom[9 * f + 3 * e];
+            c.sx = L - M.geom[9 * f + 3 * e + 1];
+            c.sy = -M.geom[9 * f + 3 * e + 2];
+            c.b0 = 0;
+            c.b1 = L;
+            c.c = tx;
+            c.s = ty;
+            push_win(M, S, C, src, ctl, c);
         }
         __syncwarp();
         // pass 2: surviving edge-path proposals take the start direction their launcher had
-        for (int q = lane; q < nP; q += 32) {
-            double d = S.ld[3 * q];
-            if (d < 0) continue;
-            int v = S.lB[q];
-            double tx = S.ld[3 * q + 1], ty = S.ld[3 * q + 2];
-            for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
-                int f = M.vfList[i];
-                if (!in_domain(M, S, C, src, f)) continue;
-                int k = 0;
-                while (M.F[3 * f + k] != v) ++k;
-                VRec r;
-                r.dx = tx;
-                r.dy = ty;
-                r.v = M.F[3 * f + (k + 1) % 3];
-                r.d = d + M.geom[9 * f + 3 * k];
-                r.slot = vfind(S, C.CV, r.v);
-                resolve(M, S, C, src, ctl, r);
-                r.v = M.F[3 * f + (k + 2) % 3];
-                r.d = d + M.geom[9 * f + 3 * ((k + 2) % 3)];
-                r.slot = vfind(S, C.CV, r.v);
-                resolve(M, S, C, src, ctl, r);
+        for (int p = lane; p < pairs; p += 32) {
+            int lo = 0, hi = nP - 1;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (S.lpre[mid] <= p) lo = mid;
+                else hi = mid - 1;
             }
+            const int q = lo;
+            const int v = S.lB[q];
+            const double d = S.ld[3 * q], tx = S.ld[3 * q + 1], ty = S.ld[3 * q + 2];
+            const int f = M.vfList[M.vfStart[v] + (p - S.lpre[q])];
+            if (!in_domain(M, S, C, src, f)) continue;
+            int k = 0;
+            while (M.F[3 * f + k] != v) ++k;
+            VRec r;
+            r.dx = tx;
+            r.dy = ty;
+            r.v = M.F[3 * f + (k + 1) % 3];
+            r.d = d + M.geom[9 * f + 3 * k];
+            r.slot = vfind(S, C.CV, r.v);
+            resolve(M, S, C, src, ctl, r);
+            r.v = M.F[3 * f + (k + 2) % 3];
+            r.d = d + M.geom[9 * f + 3 * ((k + 2) % 3)];
+            r.slot = vfind(S, C.CV, r.v);
+            resolve(M, S, C, src, ctl, r);
         }
         __syncwarp();
         // windows within the band
@@ -967,7 +1022,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             r[0].slot = r[1].slot = r[2].slot = -1;
             if (q < nA) {
                 Win w = S.wA[q];
-                if (key_of(w) > thr) {
+                if ((double)w.key > thr) {
                     int pos = atomicAdd(&ctl->nB, 1);
                     if (pos < C.CW) S.wB[pos] = w;
                     else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
@@ -996,7 +1051,9 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     int inRange = 0;
     for (int t = lane; t < nT; t += 32) {
         double ts[3], te[3];
-        double d = err ? CUDART_INF : target_query(M, S, C, src, t, nLog, ts, te);
+        const bool screened = S.tidx[t] < 0;
+        double d = (err || screened) ? CUDART_INF : target_query(M, S, C, src, t, nLog, ts, te);
+        if (screened) ts[0] = ts[1] = ts[2] = te[0] = te[1] = te[2] = 0;
         if (d > src.cutoff) {
             d = CUDART_INF;
             ts[0] = ts[1] = ts[2] = te[0] = te[1] = te[2] = 0;
@@ -1017,7 +1074,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             if (Lp.dOut && t < Lp.pairCap) {
                 size_t o = (size_t)si * Lp.pairCap + t;
                 Lp.dOut[o] = d;
-                Lp.pairJ[o] = S.tidx[t];
+                Lp.pairJ[o] = screened ? -S.tidx[t] - 1 : S.tidx[t];
                 for (int c = 0; c < 3; ++c) Lp.tsOut[3 * o + c] = ts[c];
             }
             if (d < CUDART_INF) {
@@ -1079,6 +1136,7 @@ __device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, int la
         int h = S.flist[q];
         S.fkey[h] = -1;
         S.fhead[h] = -1;
+        S.flog[h] = -1;
     }
     if (ctl->nV > C.CV || ctl->nF > C.CF) {
         // a table overflowed its touched list: clear it whole
@@ -1091,6 +1149,7 @@ __device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, int la
         for (int q = lane; q < C.CF; q += 32) {
             S.fkey[q] = -1;
             S.fhead[q] = -1;
+            S.flog[q] = -1;
         }
     }
     __syncwarp();
@@ -1152,6 +1211,7 @@ __global__ void init_scratch_kernel(char* scratch, size_t slotBytes, int nSlots,
     for (int q = threadIdx.x; q < C.CF; q += blockDim.x) {
         S.fkey[q] = -1;
         S.fhead[q] = -1;
+        S.flog[q] = -1;
     }
 }
 
@@ -1179,7 +1239,65 @@ int next_pow2(long long x)
 
 }  // namespace
 
+// warp per source: the same candidate search as the fused kernel's cell-list mode, written out as padded rows
+__global__ void __launch_bounds__(256) candidates_kernel(GeoLaunch L, int n, int cap, int* __restrict__ candJ,
+                                                         int* __restrict__ count, double* __restrict__ maxChord)
+{
+    const int lane = threadIdx.x & 31;
+    for (int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; si < n; si += (gridDim.x * blockDim.x) >> 5) {
+        const SysDesc& D = L.sys[L.sysOf ? L.sysOf[si] : 0];
+        const double* Pi = &L.srcPos[3 * si];
+        int cnt = 0;
+        double mx = 0;
+        auto consider = [&](int jj, bool valid) {
+            bool take = false;
+            double d2 = 0;
+            if (valid && jj != si) {
+                const double* Pj = &L.partPos[3 * jj];
+                double dx = Pi[0] - Pj[0], dy = Pi[1] - Pj[1], dz = Pi[2] - Pj[2];
+                d2 = dx * dx + dy * dy + dz * dz;
+                take = d2 < D.range2;
+            }
+            unsigned m = __ballot_sync(FULL, take);
+            if (take) {
+                int pos = cnt + __popc(m & ((1u << lane) - 1));
+                if (pos < cap) candJ[(size_t)si * cap + pos] = jj;
+                mx = fmax(mx, d2);
+            }
+            cnt += __popc(m);
+        };
+        int ci[3];
+        for (int c = 0; c < 3; ++c) {
+            int q = (int)floor((Pi[c] - D.lo[c]) / D.cs[c]);
+            ci[c] = max(0, min(D.nc[c] - 1, q));
+        }
+        for (int xx = max(0, ci[0] - 1); xx <= min(D.nc[0] - 1, ci[0] + 1); ++xx)
+            for (int yy = max(0, ci[1] - 1); yy <= min(D.nc[1] - 1, ci[1] + 1); ++yy)
+                for (int zz = max(0, ci[2] - 1); zz <= min(D.nc[2] - 1, ci[2] + 1); ++zz) {
+                    int cell = D.cellBase + xx + D.nc[0] * (yy + D.nc[1] * zz);
+                    int a = L.cellStart[cell], b = L.cellStart[cell + 1];
+                    for (int base = a; base < b; base += 32) {
+                        int q = base + lane;
+                        consider(q < b ? L.cellList[q] : 0, q < b);
+                    }
+                }
+        mx = warp_max(mx);
+        if (lane == 0) {
+            count[si] = cnt;
+            maxChord[si] = sqrt(mx);
+        }
+    }
+}
+
 size_t cssg_geo_slot_bytes(const GeoCaps& c) { return align_up(carve(c, nullptr, nullptr)); }
+
+void cssg_launch_candidates(const GeoLaunch& L, int n, int cap, int* candJ, int* count, double* maxChord,
+                            cudaStream_t s)
+{
+    if (n <= 0) return;
+    int blocks = (n + 7) / 8;
+    candidates_kernel<<<blocks, 256, 0, s>>>(L, n, cap, candJ, count, maxChord);
+}
 
 void cssg_geo_init_scratch(void* scratch, size_t slotBytes, int nSlots, const GeoCaps& c, cudaStream_t s)
 {

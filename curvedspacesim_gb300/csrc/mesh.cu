@@ -114,6 +114,18 @@ extern "C" int cssg_mesh_create(const double* V, int nV, const int* F, int nF, i
             edgeSum += L;
         }
     }
+    std::vector<double> exitu(12 * (size_t)nF);
+    for (int f = 0; f < nF; ++f)
+        for (int k = 0; k < 3; ++k) {
+            double L = geom[9 * f + 3 * k], cx = geom[9 * f + 3 * k + 1], cy = geom[9 * f + 3 * k + 2];
+            double n1 = std::sqrt(cx * cx + cy * cy);
+            double bx = L - cx, by = -cy;
+            double n2 = std::sqrt(bx * bx + by * by);
+            exitu[12 * f + 4 * k] = cx / n1;
+            exitu[12 * f + 4 * k + 1] = cy / n1;
+            exitu[12 * f + 4 * k + 2] = bx / n2;
+            exitu[12 * f + 4 * k + 3] = by / n2;
+        }
     std::vector<int> vfStart(nV + 1, 0), vfList(3 * (size_t)nF);
     for (int i = 0; i < 3 * nF; ++i) vfStart[F[i] + 1]++;
     for (int v = 0; v < nV; ++v) vfStart[v + 1] += vfStart[v];
@@ -245,12 +257,13 @@ extern "C" int cssg_mesh_create(const double* V, int nV, const int* F, int nF, i
     int *dF, *dT, *dVS, *dVL, *dRS, *dRV;
     unsigned char* dVF;
     float* dFC;
+    double* dEU;
     if ((rc = upload(hv, &dV, &m->buffers[0])) || (rc = upload(hf, &dF, &m->buffers[1])) ||
         (rc = upload(twin, &dT, &m->buffers[2])) || (rc = upload(N, &dN, &m->buffers[3])) ||
         (rc = upload(geom, &dG, &m->buffers[4])) || (rc = upload(vfStart, &dVS, &m->buffers[5])) ||
         (rc = upload(vfList, &dVL, &m->buffers[6])) || (rc = upload(ringStart, &dRS, &m->buffers[7])) ||
         (rc = upload(ringV, &dRV, &m->buffers[8])) || (rc = upload(vflag, &dVF, &m->buffers[9])) ||
-        (rc = upload(fcurv, &dFC, &m->buffers[11]))) {
+        (rc = upload(fcurv, &dFC, &m->buffers[11])) || (rc = upload(exitu, &dEU, &m->buffers[12]))) {
         cssg_mesh_destroy(m);
         return rc;
     }
@@ -265,6 +278,7 @@ extern "C" int cssg_mesh_create(const double* V, int nV, const int* F, int nF, i
     d.ringV = dRV;
     d.vflag = dVF;
     d.fcurv = dFC;
+    d.exitu = dEU;
     {
         DevMesh* ds = nullptr;
         cudaError_t e = cudaMalloc((void**)&ds, sizeof(DevMesh));

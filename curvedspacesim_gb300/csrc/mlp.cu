@@ -62,11 +62,13 @@ __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__floa
 // In the frame of the source face with u = in-plane chord direction and w = n_i x u:
 //   rho/s, c.n_i/s, n_j.u, n_j.w, n_j.n_i, |c|/s, H_i s, K_i s^2, H_j s, K_j s^2, c.n_j/s, e_i/s, e_j/s, |c|^2/s^2
 __global__ void screen_features(const SysDesc* __restrict__ sys, const int* __restrict__ sysOf, int nPairs,
-                                const int* __restrict__ pi, const int* __restrict__ pj, const int* __restrict__ face,
+                                const int* __restrict__ nPairsDev, const int* __restrict__ pi,
+                                const int* __restrict__ pj, const int* __restrict__ face,
                                 const double* __restrict__ pos, __nv_bfloat16* __restrict__ X,
                                 float* __restrict__ chordOverSigma)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nPairsDev) nPairs = min(nPairs, *nPairsDev);
     if (p >= nPairs) return;
     int i = pi[p], j = pj[p];
     const SysDesc& D = sys[sysOf ? sysOf[i] : 0];
@@ -194,10 +196,11 @@ struct __align__(128) InferSmem {
 
 // one CTA of 128 threads: thread t owns row t of each 128-pair tile (TMEM lane t)
 __global__ void __launch_bounds__(128) mlp_infer_tc(const __nv_bfloat16* __restrict__ X, int n,
-                                                   const float* __restrict__ params, float* __restrict__ yOut,
-                                                   int* __restrict__ errFlag)
+                                                   const int* __restrict__ nDev, const float* __restrict__ params,
+                                                   float* __restrict__ yOut, int* __restrict__ errFlag)
 {
     extern __shared__ __align__(128) unsigned char smraw[];
+    if (nDev) n = min(n, *nDev);
     InferSmem& S = *reinterpret_cast<InferSmem*>(smraw);
     const int t = threadIdx.x, warp = t >> 5;
     // stage weights (BF16, core-matrix layout) and epilogue constants
@@ -435,7 +438,36 @@ __global__ void mlp_adam(float* __restrict__ params, const float* __restrict__ g
 
 size_t train_smem() { return sizeof(float) * (NPARAM + 3 + 4 * TB * NH + TB * NIN); }
 
+__global__ void screen_decide(int n, const int* __restrict__ nDev, const float* __restrict__ chord,
+                              const float* __restrict__ yhat, double margin, unsigned char* __restrict__ skip)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nDev) n = min(n, *nDev);
+    if (p >= n) return;
+    skip[p] = ((double)chord[p] + (double)yhat[p] > 1.0 + margin) ? 1 : 0;
+}
+
+size_t infer_smem() { return sizeof(InferSmem) + 128; }
+
 }  // namespace
+
+void cssg_launch_screen(const SysDesc* sys, const int* sysOf, int maxPairs, const int* nPairsDev, const int* pi,
+                        const int* pj, const int* face, const double* pos, void* X, float* chord, const float* params,
+                        float* yhat, unsigned char* skip, double margin, int* errFlag, int sms, cudaStream_t s)
+{
+    if (maxPairs <= 0) return;
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem());
+        configured = true;
+    }
+    screen_features<<<(maxPairs + 127) / 128, 128, 0, s>>>(sys, sysOf, maxPairs, nPairsDev, pi, pj, face, pos,
+                                                            (__nv_bfloat16*)X, chord);
+    int tiles = (maxPairs + TILE_M - 1) / TILE_M;
+    mlp_infer_tc<<<std::min(tiles, sms * 4), 128, infer_smem(), s>>>((const __nv_bfloat16*)X, maxPairs, nPairsDev,
+                                                                      params, yhat, errFlag);
+    screen_decide<<<(maxPairs + 255) / 256, 256, 0, s>>>(maxPairs, nPairsDev, chord, yhat, margin, skip);
+}
 
 // ======================================================================================================================
 // C ABI
@@ -458,7 +490,7 @@ extern "C" int cssg_screen_features(cssg_ctx* ctx, const cssg_mesh* mesh, double
     SysDesc* dsys = nullptr;
     CSSG_CUDA(cudaMallocAsync((void**)&dsys, sizeof(SysDesc), ctx->stream));
     CSSG_CUDA(cudaMemcpyAsync(dsys, &hd, sizeof(SysDesc), cudaMemcpyHostToDevice, ctx->stream));
-    screen_features<<<(nPairs + 127) / 128, 128, 0, ctx->stream>>>(dsys, nullptr, nPairs, pi, pj, face, pos,
+    screen_features<<<(nPairs + 127) / 128, 128, 0, ctx->stream>>>(dsys, nullptr, nPairs, nullptr, pi, pj, face, pos,
                                                                    (__nv_bfloat16*)X_bf16, chord_over_sigma);
     CSSG_CUDA(cudaGetLastError());
     CSSG_CUDA(cudaFreeAsync(dsys, ctx->stream));
@@ -473,7 +505,7 @@ extern "C" int cssg_mlp_infer(cssg_ctx* ctx, const void* X_bf16, int n, const fl
     }
     if (n == 0) return CSSG_OK;
     static bool configured = false;
-    size_t smem = sizeof(InferSmem) + 128;
+    size_t smem = infer_smem();
     if (!configured) {
         CSSG_CUDA(cudaFuncSetAttribute(mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = true;
@@ -482,7 +514,7 @@ extern "C" int cssg_mlp_infer(cssg_ctx* ctx, const void* X_bf16, int n, const fl
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     int tiles = (n + TILE_M - 1) / TILE_M;
     int blocks = std::min(tiles, sms * 4);
-    mlp_infer_tc<<<blocks, 128, smem, ctx->stream>>>((const __nv_bfloat16*)X_bf16, n, params, y, err_flag);
+    mlp_infer_tc<<<blocks, 128, smem, ctx->stream>>>((const __nv_bfloat16*)X_bf16, n, nullptr, params, y, err_flag);
     CSSG_CUDA(cudaGetLastError());
     return CSSG_OK;
 }

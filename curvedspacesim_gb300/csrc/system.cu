@@ -230,6 +230,46 @@ __global__ void __launch_bounds__(KE_BLOCK) ke_reduce(const double* __restrict__
     if (threadIdx.x == 0) chains[(size_t)k * (4 * (Mc + 1) + 2) + 4 * (Mc + 1)] = sm[0];
 }
 
+// candidate rows -> CSR pairs (pi, pj); rows longer than the row capacity are truncated and reported
+__global__ void compact_pairs(int n, int cap, const int* __restrict__ count, const int* __restrict__ off,
+                              const int* __restrict__ candJ, int* __restrict__ pi, int* __restrict__ pj)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c = count[i], o = off[i];
+    for (int q = 0; q < c; ++q) {
+        pi[o + q] = i;
+        pj[o + q] = candJ[(size_t)i * cap + q];
+    }
+}
+
+// rows longer than the row capacity cannot be screened: clamp them and report a capacity failure
+__global__ void clamp_counts(int n, int cap, int* __restrict__ count, int* __restrict__ statusBits)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && count[i] > cap) {
+        count[i] = cap;
+        atomicOr(statusBits, 1 << CSSG_ST_CAPACITY);
+    }
+}
+
+__global__ void count_screened(int m, const int* __restrict__ total, const unsigned char* __restrict__ skip,
+                               unsigned long long* __restrict__ out)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    int nP = *total;
+    int a = p < nP ? 1 : 0, b = (p < nP && skip[p]) ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0 && a) {
+        atomicAdd(&out[0], (unsigned long long)a);
+        atomicAdd(&out[1], (unsigned long long)b);
+    }
+    (void)m;
+}
+
 __global__ void status_or(int n, const int* __restrict__ st, int* __restrict__ bits)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -257,6 +297,7 @@ struct cssg_system {
     std::vector<int> partBase;  // K + 1
     std::vector<SysDesc> hsys;
     SysDesc* dsys = nullptr;
+    SysDesc* dsysScreen = nullptr;  // the same systems with the screened-CSR search mode
     DevMesh* dmeshes = nullptr;
     int* sysOf = nullptr;       // per particle (null when K == 1)
     int* dPartBase = nullptr;
@@ -296,6 +337,25 @@ struct cssg_system {
     double* pairT = nullptr;
     int* pairJ = nullptr;
     int* pairCount = nullptr;
+    // learned screen (candidate lists -> features -> tensor-core MLP -> screened CSR propagation)
+    bool screen = false;
+    double margin = 0;
+    float* mlpParams = nullptr;
+    int candCap = 0;
+    int* candJPad = nullptr;     // n x candCap
+    int* candCount = nullptr;    // n (+1 for the scan total)
+    double* maxChord = nullptr;  // n
+    int* candOff = nullptr;      // n + 1
+    int* pairI = nullptr;        // n x candCap (compact prefix used)
+    int* pairJc = nullptr;
+    void* X = nullptr;           // n x candCap x 16 BF16
+    float* chordS = nullptr;
+    float* yhat = nullptr;
+    unsigned char* skip = nullptr;
+    int* candScanBlocks = nullptr;
+    int nCandScanBlocks = 0;
+    int* mlpErr = nullptr;
+    unsigned long long* screenCounters = nullptr;  // [0] candidate pairs, [1] screened out
     // NVT
     double* chains = nullptr;
     double* ke = nullptr;
@@ -348,7 +408,7 @@ void launch_forces(cssg_system* s)
     cudaMemsetAsync(s->work, 0, 3 * sizeof(int), st);
     GeoLaunch L;
     memset(&L, 0, sizeof(L));
-    L.sys = s->dsys;
+    L.sys = s->screen ? s->dsysScreen : s->dsys;
     L.sysOf = s->sysOf;
     L.nSrc = n;
     L.srcFace = s->face;
@@ -378,6 +438,27 @@ void launch_forces(cssg_system* s)
     L.workCounter = s->work;
     L.failList = s->failList;
     L.failCount = s->work + 2;
+    if (s->screen) {
+        // learned screen: candidate rows -> CSR pairs -> features -> tensor-core MLP -> skip flags; the propagation
+        // then reads the CSR (screened pairs keep their faces in the patch but are not queried)
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->ctx->device);
+        cssg_launch_candidates(L, n, s->candCap, s->candJPad, s->candCount, s->maxChord, st);
+        clamp_counts<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->candCap, s->candCount, s->statusBits);
+        scan_local<<<s->nCandScanBlocks, SCAN_BLOCK, 0, st>>>(s->candCount, n, s->candOff, s->candScanBlocks);
+        scan_blocks<<<1, 1024, 0, st>>>(s->candScanBlocks, s->nCandScanBlocks, s->candOff + n);
+        scan_add<<<(n + 255) / 256, 256, 0, st>>>(s->candOff, n, s->candScanBlocks);
+        compact_pairs<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->candCap, s->candCount, s->candOff, s->candJPad,
+                                                        s->pairI, s->pairJc);
+        cssg_launch_screen(s->dsysScreen, s->sysOf, n * s->candCap, s->candOff + n, s->pairI, s->pairJc, s->face,
+                           s->pos, s->X, s->chordS, s->mlpParams, s->yhat, s->skip, s->margin, s->mlpErr, sms, st);
+        count_screened<<<(n * s->candCap + 255) / 256, 256, 0, st>>>(n * s->candCap, s->candOff + n, s->skip,
+                                                                    s->screenCounters);
+        L.candOff = s->candOff;
+        L.candJ = s->pairJc;
+        L.candSkip = s->skip;
+        L.threshold = s->maxChord;
+    }
     record(s);
     cssg_launch_geodesic(L, st);
     // retry pass with large tables for the sources whose tables overflowed (usually none: exits at once)
@@ -676,7 +757,9 @@ extern "C" int cssg_system_destroy(cssg_system* s)
     void* ptrs[] = {s->face, s->bary, s->vel, s->force, s->disp, s->pos, s->walkStatus, s->srcStatus,
                     s->statusBits, s->counters, s->cellOf, s->cellCount, s->cellStart, s->cellCursor, s->cellList,
                     s->slotOf, s->scanBlocks, s->scratch, s->bigScratch, s->work, s->failList, s->pairD, s->pairT,
-                    s->pairJ, s->pairCount, s->chains, s->ke, s->dsys, s->dmeshes, s->sysOf, s->dPartBase};
+                    s->pairJ, s->pairCount, s->chains, s->ke, s->dsys, s->dmeshes, s->sysOf, s->dPartBase,
+                    s->mlpParams, s->candJPad, s->candCount, s->maxChord, s->candOff, s->pairI, s->pairJc, s->X,
+                    s->chordS, s->yhat, s->skip, s->candScanBlocks, s->mlpErr, s->screenCounters, s->dsysScreen};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -716,7 +799,7 @@ extern "C" int cssg_system_kernels_per_step(cssg_system* s, int* count)
 {
     if (!s || !count) return CSSG_ERR_ARG;
     // walk + status_or ; [cell list: assign, scan x3, scatter, sort] + geodesic + retry + status_or
-    int walk = 2, forces = (s->useCells ? 6 : 0) + 3;
+    int walk = 2, forces = (s->useCells ? 6 : 0) + 3 + (s->screen ? 10 : 0);
     *count = s->P.integrator == 0 ? (1 + walk + forces + 1) : (2 + walk + forces + 2 + walk + 2);
     return CSSG_OK;
 }
@@ -862,6 +945,77 @@ extern "C" int cssg_system_chain(cssg_system* s, double* chain, int capacity)
     }
     CSSG_CUDA(cudaMemcpyAsync(chain, s->chains, sizeof(double) * len, cudaMemcpyDeviceToHost, s->ctx->stream));
     CSSG_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return CSSG_OK;
+}
+
+// Learned screen on/off.  params_host: cssg_mlp_param_count() FP32 values (nullable when disabling); a pair is
+// skipped when |chord| / sigma + yhat > 1 + margin.  Requires the cell-list neighbour structure.
+extern "C" int cssg_system_set_screen(cssg_system* s, const float* params_host, double margin, int enable)
+{
+    if (!s) return CSSG_ERR_ARG;
+    cudaStream_t st = s->ctx->stream;
+    if (enable) {
+        if (!s->useCells || !params_host) {
+            cssg_set_error("cssg_system_set_screen: needs parameters and the cell-list neighbour structure");
+            return CSSG_ERR_ARG;
+        }
+        const int n = s->n;
+        if (!s->mlpParams) {
+            s->candCap = std::max(32, 2 * s->caps.CT);
+            size_t slots = (size_t)n * s->candCap;
+            int rc;
+            s->nCandScanBlocks = (n + SCAN_BLOCK * SCAN_ITEMS - 1) / (SCAN_BLOCK * SCAN_ITEMS);
+            if ((rc = alloc((void**)&s->mlpParams, sizeof(float) * cssg_mlp_param_count())) ||
+                (rc = alloc((void**)&s->candJPad, sizeof(int) * slots)) ||
+                (rc = alloc((void**)&s->candCount, sizeof(int) * (n + 1))) ||
+                (rc = alloc((void**)&s->maxChord, sizeof(double) * n)) ||
+                (rc = alloc((void**)&s->candOff, sizeof(int) * (n + 1))) ||
+                (rc = alloc((void**)&s->pairI, sizeof(int) * slots)) ||
+                (rc = alloc((void**)&s->pairJc, sizeof(int) * slots)) ||
+                (rc = alloc(&s->X, 32 * slots)) || (rc = alloc((void**)&s->chordS, sizeof(float) * slots)) ||
+                (rc = alloc((void**)&s->yhat, sizeof(float) * slots)) ||
+                (rc = alloc((void**)&s->skip, slots)) ||
+                (rc = alloc((void**)&s->candScanBlocks, sizeof(int) * (s->nCandScanBlocks + 1))) ||
+                (rc = alloc((void**)&s->mlpErr, sizeof(int))) ||
+                (rc = alloc((void**)&s->screenCounters, sizeof(unsigned long long) * 2)) ||
+                (rc = alloc((void**)&s->dsysScreen, sizeof(SysDesc) * s->K)))
+                return rc;
+            std::vector<SysDesc> h = s->hsys;
+            for (auto& d : h) d.searchMode = 3;
+            CSSG_CUDA(cudaMemcpy(s->dsysScreen, h.data(), sizeof(SysDesc) * s->K, cudaMemcpyHostToDevice));
+            CSSG_CUDA(cudaMemset(s->mlpErr, 0, sizeof(int)));
+            CSSG_CUDA(cudaMemset(s->screenCounters, 0, sizeof(unsigned long long) * 2));
+        }
+        CSSG_CUDA(cudaMemcpyAsync(s->mlpParams, params_host, sizeof(float) * cssg_mlp_param_count(),
+                                  cudaMemcpyHostToDevice, st));
+        CSSG_CUDA(cudaStreamSynchronize(st));
+        s->margin = margin;
+    }
+    s->screen = enable != 0;
+    if (s->graphExec) {
+        cudaGraphExecDestroy(s->graphExec);
+        s->graphExec = nullptr;
+    }
+    return CSSG_OK;
+}
+
+// {candidate pairs, screened-out pairs, tensor-core wait failures} since the last call (synchronises, resets)
+extern "C" int cssg_system_screen_counters(cssg_system* s, unsigned long long* out_host)
+{
+    if (!s || !out_host) return CSSG_ERR_ARG;
+    out_host[0] = out_host[1] = out_host[2] = 0;
+    if (!s->screenCounters) return CSSG_OK;
+    cudaStream_t st = s->ctx->stream;
+    unsigned long long h[2];
+    int e = 0;
+    CSSG_CUDA(cudaMemcpyAsync(h, s->screenCounters, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CSSG_CUDA(cudaMemcpyAsync(&e, s->mlpErr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CSSG_CUDA(cudaMemsetAsync(s->screenCounters, 0, sizeof(h), st));
+    CSSG_CUDA(cudaMemsetAsync(s->mlpErr, 0, sizeof(int), st));
+    CSSG_CUDA(cudaStreamSynchronize(st));
+    out_host[0] = h[0];
+    out_host[1] = h[1];
+    out_host[2] = (unsigned long long)e;
     return CSSG_OK;
 }
 

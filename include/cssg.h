@@ -139,6 +139,14 @@ int cssg_system_chain(cssg_system* sys, double* chain_host, int capacity);
  * CUDA events on the system stream (filled when timing is enabled with cssg_system_timing(sys, 1)). */
 int cssg_system_timing(cssg_system* sys, int enable);
 int cssg_system_last_times(cssg_system* sys, double* ms_host, int capacity);
+/* Learned screen for the system's force pass (cell-list systems): enable = 1 uploads params_host
+ * (cssg_mlp_param_count() FP32 values) and skips candidate pairs whose predicted distance |chord| + sigma * yhat
+ * exceeds sigma * (1 + margin); their faces still complete the reference patch, so the patch and every computed
+ * distance stay exact.  enable = 0 returns to the plain exact path. */
+int cssg_system_set_screen(cssg_system* sys, const float* params_host, double margin, int enable);
+/* Screen counters since the last call: out_host[3] = {candidate pairs, screened-out pairs, tensor-core wait
+ * failures}.  Synchronises and resets. */
+int cssg_system_screen_counters(cssg_system* sys, unsigned long long* out_host);
 /* Number of kernels one step() launches (the integrator's fixed sequence). */
 int cssg_system_kernels_per_step(cssg_system* sys, int* count);
 

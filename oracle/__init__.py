@@ -178,7 +178,7 @@ class OracleMesh:
         m = len(idx)
         d = np.full(m, np.inf)
         ts = np.zeros((m, 3))
-        stats = np.zeros(4, dtype=np.int64)
+        stats = np.zeros(5, dtype=np.int64)
         lib().oracle_neighbor_distances(self.h, len(face), _p(face), _p(bary), _p(off), _p(idx), _p(mc),
                                         int(submesh), float(max_dist), float(cutoff), _p(d), _p(ts), _p(stats),
                                         int(threads))

@@ -626,6 +626,8 @@ struct GeoStats {
     long long windowsCreated = 0;
     long long windowsProcessed = 0;
     long long vertexLaunches = 0;
+    long long rounds = 0;
+    long long frontier = 0;
 };
 
 struct GeoWork {
@@ -1056,6 +1058,7 @@ struct Geo {
                 if (done) break;
             }
             double thr = g_bfs ? kInf : mk + g_delta;
+            for (int w : front) frontierSum += key_of(wins[w]) <= thr ? 1 : 0;
             std::vector<int> nf, np;
             for (int v : pend) {
                 double d = W.lab[v];
@@ -1078,6 +1081,7 @@ struct Geo {
     }
 
     long long roundsUsed = 0;
+    long long frontierSum = 0;
 
     double final_candidate(const Target& t) const
     {
@@ -1174,6 +1178,8 @@ void geodesic_one(const Mesh& M, GeoWork& W, int f0, const double* b0, int nT, c
         stats->windowsCreated += G.st.windowsCreated;
         stats->windowsProcessed += G.st.windowsProcessed;
         stats->vertexLaunches += G.st.vertexLaunches;
+        stats->rounds += G.roundsUsed;
+        stats->frontier += G.frontierSum;
     }
     W.reset();
 }
@@ -1703,8 +1709,8 @@ void oracle_neighbor_distances(void* m, int n, const int* face, const double* ba
 #ifdef _OPENMP
     if (nThreads > 0) omp_set_num_threads(nThreads);
 #endif
-    long long w0 = 0, w1 = 0, w2 = 0;
-#pragma omp parallel reduction(+ : w0, w1, w2)
+    long long w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0;
+#pragma omp parallel reduction(+ : w0, w1, w2, w3, w4)
     {
         GeoWork W;
         GeoStats st;
@@ -1735,11 +1741,15 @@ void oracle_neighbor_distances(void* m, int n, const int* face, const double* ba
         w0 += st.windowsCreated;
         w1 += st.windowsProcessed;
         w2 += st.vertexLaunches;
+        w3 += st.rounds;
+        w4 += st.frontier;
     }
     if (statsOut) {
         statsOut[0] = w0;
         statsOut[1] = w1;
         statsOut[2] = w2;
+        statsOut[3] = w3;
+        statsOut[4] = w4;
     }
 }
 

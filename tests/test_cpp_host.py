@@ -46,8 +46,11 @@ def test_host_classes_match_oracle(tmp_path, oracle_mod):
     with open(pp, "w") as fh:
         fh.write(f"{n}\n")
         for i in range(n):
-            fh.write(f"{f[i]} {b[i, 0]!r} {b[i, 1]!r} {b[i, 2]!r} {vel[i, 0]!r} {vel[i, 1]!r} {vel[i, 2]!r}\n")
-    out = subprocess.run([exe, str(mp), str(pp)], check=True, capture_output=True, text=True).stdout
+            vals = " ".join(repr(float(x)) for x in (*b[i], *vel[i]))  # plain decimal text, round-trip exact
+            fh.write(f"{int(f[i])} {vals}\n")
+    run = subprocess.run([exe, str(mp), str(pp)], capture_output=True, text=True)
+    assert run.returncode == 0, run.stderr[-2000:]
+    out = run.stdout
     res = json.loads(out)
     OM = oracle_mod.OracleMesh(V, F)
     assert res["area"] == pytest.approx(OM.area, rel=1e-12)

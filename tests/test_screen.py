@@ -1,0 +1,51 @@
+"""Learned screen on a bumpy sphere: trained on the exact GPU solver's pairs from other seeds, calibrated on held-out
+surfaces; the screened force pass must keep the exact path's in-range pair set and distances."""
+import numpy as np
+import pytest
+
+from curvedspacesim_gb300 import meshes as ms
+
+pytestmark = pytest.mark.gpu
+
+
+def test_screened_path_keeps_pairs_and_distances():
+    from curvedspacesim_gb300 import api, screen
+    ctx = api.Context(0)
+    sub, n, sigma = 5, 3000, 0.06
+
+    def mesh(seed):
+        return ms.bumpy_sphere(sub, amplitude=0.05, seed=seed)
+
+    X, y, c, _ = screen.generate(ctx, mesh, [11, 12, 13], n, sigma)
+    params, _ = screen.train(ctx, X, y, steps=600, batch=4096, lr=3e-3)
+    Xh, yh, ch, _ = screen.generate(ctx, mesh, [21, 22], n, sigma)
+    margin, info = screen.calibrate(ctx, params, Xh, yh, ch)
+    frac, wrong = screen.skipped_fraction(ctx, params, margin, Xh, yh, ch)
+    assert wrong == 0
+    # evaluation surface (seed 0): exact vs screened force pass
+    V, F = mesh(0)
+    rng = np.random.default_rng(5)
+    f, b = ms.area_weighted_positions(V, F, n, rng)
+    M = api.Mesh(V, F)
+    p = api.make_params("nve", "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=sigma, submesh=True,
+                        max_dist=sigma, cutoff=sigma, dt=1e-3)
+    plain = api.System(ctx, M, n, p)
+    plain.set_state(f, b, np.zeros((n, 3)), np.zeros((n, 3)))
+    plain.enable_pairs()
+    plain.compute_forces()
+    assert plain.check()[0] == 0
+    scr = api.System(ctx, M, n, p)
+    scr.set_state(f, b, np.zeros((n, 3)), np.zeros((n, 3)))
+    scr.enable_pairs()
+    scr.set_screen(params, margin)
+    scr.compute_forces()
+    bits, cnt = scr.check()
+    assert bits == 0, cnt
+    sc = scr.screen_counters()
+    assert sc["tc_errors"] == 0 and sc["pairs"] > 0
+    missing, extra, err = screen.audit(plain.pairs(), scr.pairs(), sigma)
+    assert not missing and not extra
+    assert err <= 1e-12
+    fp = plain.get_state()[3]
+    fs = scr.get_state()[3]
+    np.testing.assert_allclose(fs, fp, atol=1e-12)
