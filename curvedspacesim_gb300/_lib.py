@@ -24,7 +24,7 @@ EXPORTS = [
     "cssg_system_pairs", "cssg_system_chain", "cssg_system_timing", "cssg_system_last_times",
     "cssg_system_reset_thermostat", "cssg_system_kernels_per_step", "cssg_diag_fp64_peak",
     "cssg_system_create_batched", "cssg_mlp_param_count", "cssg_screen_features", "cssg_mlp_infer", "cssg_mlp_grad",
-    "cssg_mlp_adam", "cssg_system_set_screen", "cssg_system_screen_counters",
+    "cssg_mlp_adam", "cssg_system_set_screen", "cssg_system_screen_counters", "cssg_distance_batch_noalloc",
 ]
 
 
@@ -80,6 +80,7 @@ def load(build_if_missing: bool = True):
     L.cssg_ctx_stream.restype = P
     L.cssg_transport_batch.argtypes = [P, P, I, P, P, P, P, I, P, P]
     L.cssg_distance_batch.argtypes = [P, P, I, P, P, P, P, P, I, D, P, D, P, P, P, P, P]
+    L.cssg_distance_batch_noalloc.argtypes = [P, P, I, P, P, P, P, P, I, D, P, D, P, P, P, P, P]
     L.cssg_system_create.argtypes = [P, P, I, ctypes.POINTER(cssg_params), PP]
     L.cssg_system_create_batched.argtypes = [P, I, P, P, P, PP]
     L.cssg_system_destroy.argtypes = [P]

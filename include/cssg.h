@@ -86,6 +86,28 @@ int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSrc, const in
                         double max_dist, const double* threshold, double cutoff, double* d_out, double* tstart_out,
                         double* tend_out, int* status, long long* stats);
 
+/* ---- distances without allocation -----------------------------------------------------------------------------
+ * No reference counterpart: the reference allocates freely on the host.  Same arguments, kernels and results as
+ * cssg_distance_batch, but it allocates and frees no device memory: its scratch is a fixed, file-scope device
+ * buffer of CSSG_NOALLOC_SCRATCH_BYTES (64 MiB) in the library, plus a few words for the work counter, the system
+ * descriptor and the largest candidate count.  For host codes that cannot call the allocator during a step.
+ *   - A call whose single propagation slot (set by the largest candidate count and the reach, as in
+ *     cssg_distance_batch) exceeds the scratch returns CSSG_ERR_CAPACITY and launches nothing; a call that fits
+ *     fewer slots than cssg_distance_batch would use runs with fewer slots (same results, less parallelism).
+ *   - Each call resets what must start at zero (the work counter) and empties the slots' tables itself.
+ *   - The scratch is shared by every call on a device: calls that overlap in time on one device (different
+ *     streams or contexts, or several host threads) race on it.  Calls issued on one stream are ordered.
+ *   - The first call on each device looks up the scratch's device address (cudaGetSymbolAddress) and must not be
+ *     made while a stream is being captured.
+ *   - Like cssg_distance_batch it reads the largest candidate count back to the host, so it synchronises the
+ *     context's stream once. */
+#define CSSG_NOALLOC_SCRATCH_BYTES (64u << 20)
+int cssg_distance_batch_noalloc(cssg_ctx* ctx, const cssg_mesh* mesh, int nSrc, const int* src_face,
+                                const double* src_bary, const int* cand_offsets, const int* cand_face,
+                                const double* cand_bary, int submesh, double max_dist, const double* threshold,
+                                double cutoff, double* d_out, double* tstart_out, double* tend_out, int* status,
+                                long long* stats);
+
 /* ---- particle system: simpleModel + force + updater on the device -------------------------------------------- */
 typedef struct cssg_params {
     int integrator;      /* 0 velocityVerletNVE (velocityVerletNVE.cpp:3-29), 1 noseHooverNVT (noseHooverNVT.cpp:3-150) */
