@@ -48,7 +48,7 @@ def workload_config(name):
     if name == "bumpy_screen":
         return dict(workload="bumpy_sphere7_N20000_nve_patch_screen", mesh=("bumpy", 7, 0), n=20000, sigma=0.02,
                     integrator="nve", submesh=True, range_=0.02, dt=0.002, T=0.1, seed=4, screen=True,
-                    train_seeds=list(range(1, 9)), holdout_seeds=[9, 10])
+                    train_seeds=list(range(1, 9)), configs_per_seed=6, holdout_seeds=[9, 10], train_steps=3000)
     if name == "torus_nvt":
         return dict(workload="torus200x100_N2000_nvt_patch", mesh=("torus", 200, 100), n=2000, sigma=0.3,
                     integrator="nvt", submesh=True, range_=0.3, dt=0.002, T=0.05, seed=2)
@@ -390,6 +390,151 @@ def run_ours(args, cfg):
         print(json.dumps(line), flush=True)
 
 
+def _timed_steps(ctx, S, steps, flush, stream, graph=True):
+    """K single steps, each timed with CUDA events on the library's stream after an L2 flush; returns ms per step."""
+    import torch
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for k in range(steps):
+        with ctx.use():
+            flush.zero_()
+        starts[k].record(stream)
+        S.step(1, graph=graph)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(e) for a, e in zip(starts, ends)]
+
+
+def run_screen(args, cfg):
+    """Learned distance screen against the plain exact path on the same surface and particles.
+
+    The screen is trained here on exact pairs that the GPU solver produces on other surfaces (train_seeds), with the
+    library's own forward/backward/Adam kernels; its skip margin is calibrated on held-out surfaces (holdout_seeds) so
+    that no held-out in-range pair is skipped.  Both paths then step the evaluation surface from the same state; the
+    audit recomputes forces on one common state with both and compares in-range pair sets and distances."""
+    import torch
+    from curvedspacesim_gb300 import api, screen
+    world, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    ctx = api.Context(local)
+    sub, sigma, n = cfg["mesh"][1], cfg["sigma"], cfg["n"]
+
+    def mesh_fn(seed):
+        return ms.bumpy_sphere(sub, amplitude=0.05, seed=seed)
+
+    t0 = time.perf_counter()
+    X, y, _, _ = screen.generate(ctx, mesh_fn, cfg["train_seeds"], n, sigma, configs_per_seed=cfg["configs_per_seed"])
+    params, _ = screen.train(ctx, X, y, steps=cfg["train_steps"], batch=8192, lr=3e-3)
+    Xh, yh, ch, _ = screen.generate(ctx, mesh_fn, cfg["holdout_seeds"], n, sigma, configs_per_seed=2)
+    margin, cal = screen.calibrate(ctx, params, Xh, yh, ch)
+    skip_frac, wrong = screen.skipped_fraction(ctx, params, margin, Xh, yh, ch)
+    prep_s = time.perf_counter() - t0
+    n_train = int(X.shape[0])
+    del X, y, Xh, yh, ch
+
+    V, F, f, b, vel = build_inputs(cfg)
+    M = api.Mesh(V, F, device=local)
+    prm = api.make_params(cfg["integrator"], "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=cfg["range_"],
+                          submesh=cfg["submesh"], max_dist=sigma, cutoff=sigma, dt=cfg["dt"], temperature=cfg["T"])
+    plain = api.System(ctx, M, n, prm)
+    scr = api.System(ctx, M, n, prm)
+    scr.set_screen(params, margin)
+    for S in (plain, scr):
+        S.set_state(f, b, vel, np.zeros((n, 3)))
+    stream = ctx.tstream
+    with ctx.use():
+        flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    for S in (plain, scr):
+        S.step(max(args.warmup, 1), graph=True)
+    torch.cuda.synchronize()
+    for name, S in (("plain", plain), ("screened", scr)):
+        bits, cnt = S.check()
+        if bits:
+            raise RuntimeError(f"{name}: per-item errors during warm-up: {bits:#x} {cnt}")
+
+    sampler = ClockSampler(local)
+    barrier(pg)
+    sampler.start()
+    ms_plain = _timed_steps(ctx, plain, args.steps, flush, stream)
+    ms_scr = _timed_steps(ctx, scr, args.steps, flush, stream)
+    clocks = sampler.stop()
+    barrier(pg)
+    t_plain = max_over_ranks(pg, sum(ms_plain))
+    t_scr = max_over_ranks(pg, sum(ms_scr))
+    for name, S in (("plain", plain), ("screened", scr)):
+        bits, cnt = S.check()
+        if bits:
+            raise RuntimeError(f"{name}: per-item errors in the timed region: {bits:#x} {cnt}")
+    value = world * n * args.steps / (t_scr * 1e-3)
+    value_plain = world * n * args.steps / (t_plain * 1e-3)
+    sc = scr.screen_counters()
+
+    # kernel time of the geodesic pass on both paths
+    kt = {}
+    for name, S in (("plain", plain), ("screened", scr)):
+        S.timing(True)
+        S.step(args.steps, graph=False)
+        torch.cuda.synchronize()
+        kt[name] = S.last_times()["geodesic_ms"] / args.steps
+        S.timing(False)
+
+    # audit on one common state: exact vs screened in-range pairs and distances
+    st = plain.get_state()
+    audit_res = {}
+    for S in (plain, scr):
+        S.set_state(*st)
+        S.enable_pairs()
+        S.compute_forces()
+    missing, extra, rel = screen.audit(plain.pairs(), scr.pairs(), sigma)
+    fp = plain.get_state()[3]
+    fs = scr.get_state()[3]
+    audit_res = {"missing_in_range_pairs": len(missing), "extra_in_range_pairs": len(extra),
+                 "max_rel_distance_diff": rel, "max_abs_force_diff": float(np.max(np.abs(fp - fs)))}
+
+    # e2e through the C ABI with host state, screened path
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    hf, hb, hv, hfo = pin((n,), torch.int32), pin((n, 3), torch.float64), pin((n, 3), torch.float64), \
+        pin((n, 3), torch.float64)
+    hf[:], hb[:], hv[:], hfo[:] = scr.get_state()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        scr.set_state(hf, hb, hv, hfo)
+        scr.step(1, graph=True)
+        a, bb, c, d = scr.get_state()
+        hf[:], hb[:], hv[:], hfo[:] = a, bb, c, d
+    e2e = world * n * args.steps / max_over_ranks(pg, time.perf_counter() - t1)
+    io_bytes = n * (4 + 24 + 24 + 24)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(cfg, [dict(V=V, F=F, n=n, sigma=sigma, range_=cfg["range_"], f=f, b=b, vel=vel)])
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_scr / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": cfg["workload"], "n": n, "integrator": cfg["integrator"], "submesh": True,
+                       "graph": True, "l2": "flushed before every timed step (512 MB write)",
+                       "parallelism": f"replicas x{world}"},
+            "plain": {"value": value_plain, "ms_per_step": t_plain / args.steps, "geodesic_ms": kt["plain"]},
+            "screened": {"value": value, "ms_per_step": t_scr / args.steps, "geodesic_ms": kt["screened"],
+                         "speedup_vs_plain": value / value_plain, "counters": sc},
+            "screen": {"training_pairs": n_train, "train_seeds": cfg["train_seeds"],
+                       "holdout_seeds": cfg["holdout_seeds"], "margin": margin, "calibration": cal,
+                       "holdout_skip_fraction": skip_frac, "holdout_wrongly_skipped": wrong,
+                       "prep_seconds": prep_s},
+            "audit": audit_res,
+            "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": io_bytes,
+                    "d2h_bytes_per_step": io_bytes},
+            "gpu_launches": scr.kernels_per_step() * args.steps,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -406,6 +551,8 @@ def main():
     cfg = workload_config(args.workload)
     if args.impl == "reference":
         run_reference(args, cfg)
+    elif cfg.get("screen"):
+        run_screen(args, cfg)
     else:
         run_ours(args, cfg)
 

@@ -64,9 +64,16 @@ __device__ __forceinline__ double bitsd(unsigned long long b)
 
 struct WarpCtl {
     int nA, nB, nLA, nLB, nLog, nV, nF, nT, err, nBA, nBB, nProc;
+    int nPT, nCT;  // task counts of the current batch of windows
 };
 
+// Task lists of one batch of up to 32 windows (per warp, shared memory): vertex proposals (window << 2 | vertex:
+// 0 opposite vertex C, 1 = A, 2 = B) and child windows (window << 1 | exit: 0 through edge C->A, 1 through B->C).
+constexpr int kTaskP = 96, kTaskC = 64;
+
 struct Slot {
+    int* taskP;  // shared memory, kTaskP entries
+    int* taskC;  // shared memory, kTaskC entries
     int* tface;
     int* tidx;
     int* tnext;
@@ -243,6 +250,18 @@ struct VRec {
     double d, dx, dy;
 };
 
+// Does the ray from the window's pseudo-source through (px, py) meet the edge line inside [b0 - tol, b1 + tol]?
+// The crossing is xp = sx + (px - sx) * (-sy) / D with D = py - sy; for D > 0 (the usual case: the point lies above
+// the edge and the pseudo-source below it) the test is done on xp * D, without a division.
+__device__ __forceinline__ bool ray_hits(const Win& w, double px, double py, double tol)
+{
+    const double D = py - w.sy;
+    const double num = w.sx * D + (px - w.sx) * (-w.sy);
+    if (D > 0) return num >= (w.b0 - tol) * D && num <= (w.b1 + tol) * D;
+    const double xp = num / D;
+    return xp >= w.b0 - tol && xp <= w.b1 + tol;
+}
+
 __device__ __forceinline__ double key_of(const Win& w)
 {
     double m;
@@ -315,7 +334,7 @@ __device__ __noinline__ void push_win(const DevMesh& M, const Slot& S, const Geo
     if (!trim(M, S, C, w)) return;
     const double key = key_of(w);
     if (key > src.cutoff) return;
-    w.key = (float)key;
+    w.key = __double2float_rd(key);  // a lower bound: banding and the early exit stay conservative
     int pos = atomicAdd(&ctl->nB, 1);
     if (pos >= C.CW) {
         atomicExch(&ctl->err, CSSG_ST_CAPACITY);
@@ -324,19 +343,23 @@ __device__ __noinline__ void push_win(const DevMesh& M, const Slot& S, const Geo
     S.wB[pos] = w;
 }
 
-__device__ __forceinline__ void start_dir(const Win& w, double px, double py, double& dx, double& dy)
+// unit start direction (source frame) of the path through (px, py); l = |(px, py) - (sx, sy)| when sigma == 0
+__device__ __forceinline__ void start_dir_l(const Win& w, double px, double py, double l, double& dx, double& dy)
 {
     if (w.sigma == 0) {
-        double ux = px - w.sx, uy = py - w.sy;
-        double l = len2(ux, uy);
-        ux /= l;
-        uy /= l;
+        const double inv = 1.0 / l;
+        double ux = (px - w.sx) * inv, uy = (py - w.sy) * inv;
         dx = w.c * ux - w.s * uy;
         dy = w.s * ux + w.c * uy;
     } else {
         dx = w.c;
         dy = w.s;
     }
+}
+
+__device__ __forceinline__ void start_dir(const Win& w, double px, double py, double& dx, double& dy)
+{
+    start_dir_l(w, px, py, w.sigma == 0 ? len2(px - w.sx, py - w.sy) : 1.0, dx, dy);
 }
 
 __device__ __forceinline__ void propose(const Slot& S, const GeoCaps& C, WarpCtl* ctl, int v, double d, double dx,
@@ -360,8 +383,9 @@ __device__ __forceinline__ void propose(const Slot& S, const GeoCaps& C, WarpCtl
 __device__ __forceinline__ void propose_from(const Slot& S, const GeoCaps& C, WarpCtl* ctl, const Win& w, int v,
                                              double px, double py, VRec& rec)
 {
-    propose(S, C, ctl, v, w.sigma + len2(px - w.sx, py - w.sy), 0.0, 0.0, rec);
-    if (rec.slot >= 0) start_dir(w, px, py, rec.dx, rec.dy);
+    const double l = len2(px - w.sx, py - w.sy);
+    propose(S, C, ctl, v, w.sigma + l, 0.0, 0.0, rec);
+    if (rec.slot >= 0) start_dir_l(w, px, py, l, rec.dx, rec.dy);
 }
 
 __device__ __noinline__ bool launchable(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int v)
@@ -391,19 +415,33 @@ __device__ void resolve(const DevMesh& M, const Slot& S, const GeoCaps& C, const
     }
 }
 
-// process one window (lane-local); records up to three vertex proposals
-__device__ void process(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, Win w,
-                        VRec* rec, int& processed)
+// Where b lies relative to xC, the crossing of the edge line by the ray from the pseudo-source through the opposite
+// vertex C = (cx, cy): the sign of (b - xC), scaled by DC = cy - sy when DC > 0 (no division).
+struct CrossC {
+    double DC, nC, xC;
+    bool pos;
+    __device__ __forceinline__ CrossC(const Win& w, double cx, double cy)
+    {
+        DC = cy - w.sy;
+        nC = w.sx * DC + (cx - w.sx) * (-w.sy);  // xC * DC
+        pos = DC > 0;
+        xC = pos ? 0.0 : nC / DC;
+    }
+    __device__ __forceinline__ double rel(double b) const { return pos ? b * DC - nC : b - xC; }
+};
+
+// Phase A of one window (one lane): trim, log it for the target queries and update the targets' running bests,
+// then queue the vertex proposals and the child windows it makes.  The trimmed interval is written back to wA[q],
+// where the tasks read it.
+__device__ void classify(const DevMesh& M, const Slot& S, const GeoCaps& C, WarpCtl* ctl, Win w, int q,
+                         int& processed)
 {
-    rec[0].slot = rec[1].slot = rec[2].slot = -1;
     if (!trim(M, S, C, w)) return;
     processed++;
     atomicAdd(&ctl->nProc, 1);
     const int g = w.he >> 2, j = w.he & 3;
     const double L = M.geom[9 * g + 3 * j], cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
-    const int A = M.F[3 * g + j], B = M.F[3 * g + (j + 1) % 3], Cv = M.F[3 * g + (j + 2) % 3];
     const double tol = 1e-12 * L;
-    // targets in g: log the window for the final query and update the running bests (early exit)
     int fh = ffind(S, C.CF, g);
     if (fh >= 0) {
         int head = ldv(&S.fhead[fh]);
@@ -419,77 +457,103 @@ __device__ void process(const DevMesh& M, const Slot& S, const GeoCaps& C, const
                 if (S.tidx[t] < 0) continue;
                 double b1 = S.tb[3 * t + (j + 1) % 3], b2 = S.tb[3 * t + (j + 2) % 3];
                 double px = b1 * L + b2 * cx, py = b2 * cy;
-                double xp = w.sx + (px - w.sx) * (-w.sy) / (py - w.sy);
-                if (xp >= w.b0 - tol && xp <= w.b1 + tol) {
+                if (ray_hits(w, px, py, tol)) {
                     double d = w.sigma + len2(px - w.sx, py - w.sy);
                     atomicMin(&S.tbest[t], dbits(d));
                 }
             }
         }
     }
-    double xC = w.sx + (cx - w.sx) * (-w.sy) / (cy - w.sy);
-    if (xC >= w.b0 - tol && xC <= w.b1 + tol) propose_from(S, C, ctl, w, Cv, cx, cy, rec[0]);
-    if (w.b0 <= tol) propose_from(S, C, ctl, w, A, 0.0, 0.0, rec[1]);
-    if (w.b1 >= L - tol) propose_from(S, C, ctl, w, B, L, 0.0, rec[2]);
-    if (w.b0 < xC) {  // exit through edge C->A (local j+2); child frame: origin A, x toward C
-        int t = M.twin[3 * g + (j + 2) % 3];
-        if (t >= 0) {
-            const double ux = M.exitu[12 * g + 4 * j], uy = M.exitu[12 * g + 4 * j + 1];
-            double isx = ux * w.sx + uy * w.sy, isy = -uy * w.sx + ux * w.sy;
-            Win c;
-            c.he = (t / 3) * 4 + t % 3;
-            c.sigma = w.sigma;
-            c.sx = isx;
-            c.sy = isy;
-            {
-                double X = ux * w.b0, Y = -uy * w.b0;
-                c.b0 = isx + (X - isx) * (-isy) / (Y - isy);
-            }
-            if (w.b1 >= xC) c.b1 = M.geom[9 * (t / 3) + 3 * (t % 3)];
-            else {
-                double X = ux * w.b1, Y = -uy * w.b1;
-                c.b1 = isx + (X - isx) * (-isy) / (Y - isy);
-            }
-            if (w.sigma == 0) {
-                c.c = w.c * ux - w.s * uy;
-                c.s = w.s * ux + w.c * uy;
-            } else {
-                c.c = w.c;
-                c.s = w.s;
-            }
-            push_win(M, S, C, src, ctl, c);
+    S.wA[q].b0 = w.b0;
+    S.wA[q].b1 = w.b1;
+    const CrossC xc(w, cx, cy);
+    if (xc.rel(w.b0 - tol) <= 0 && xc.rel(w.b1 + tol) >= 0) S.taskP[atomicAdd(&ctl->nPT, 1)] = q << 2;
+    if (w.b0 <= tol) S.taskP[atomicAdd(&ctl->nPT, 1)] = (q << 2) | 1;
+    if (w.b1 >= L - tol) S.taskP[atomicAdd(&ctl->nPT, 1)] = (q << 2) | 2;
+    if (xc.rel(w.b0) < 0 && M.twin[3 * g + (j + 2) % 3] >= 0) S.taskC[atomicAdd(&ctl->nCT, 1)] = q << 1;
+    if (xc.rel(w.b1) > 0 && M.twin[3 * g + (j + 1) % 3] >= 0) S.taskC[atomicAdd(&ctl->nCT, 1)] = (q << 1) | 1;
+}
+
+// a queued vertex proposal: path length through the window to one of its face's vertices
+__device__ void proposal_task(const DevMesh& M, const Slot& S, const GeoCaps& C, WarpCtl* ctl, int task, VRec& rec)
+{
+    const Win w = S.wA[task >> 2];
+    const int k = task & 3;
+    const int g = w.he >> 2, j = w.he & 3;
+    double px = 0, py = 0;
+    int v;
+    if (k == 0) {
+        px = M.geom[9 * g + 3 * j + 1];
+        py = M.geom[9 * g + 3 * j + 2];
+        v = M.F[3 * g + (j + 2) % 3];
+    } else if (k == 1) {
+        v = M.F[3 * g + j];
+    } else {
+        px = M.geom[9 * g + 3 * j];
+        v = M.F[3 * g + (j + 1) % 3];
+    }
+    propose_from(S, C, ctl, w, v, px, py, rec);
+}
+
+// a queued child window: the part of the window's rays that leaves its face through one of the two other edges,
+// expressed in the frame of that edge's twin
+__device__ void child_task(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, int task)
+{
+    const Win w = S.wA[task >> 1];
+    const int g = w.he >> 2, j = w.he & 3;
+    const double cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
+    const CrossC xc(w, cx, cy);
+    const double r0 = xc.rel(w.b0), r1 = xc.rel(w.b1);
+    Win c;
+    c.sigma = w.sigma;
+    double ux, uy;
+    if ((task & 1) == 0) {  // exit through edge C->A (local j+2); child frame: origin A, x toward C
+        const int t = M.twin[3 * g + (j + 2) % 3];
+        ux = M.exitu[12 * g + 4 * j];
+        uy = M.exitu[12 * g + 4 * j + 1];
+        const double isx = ux * w.sx + uy * w.sy, isy = -uy * w.sx + ux * w.sy;
+        c.he = (t / 3) * 4 + t % 3;
+        c.sx = isx;
+        c.sy = isy;
+        // interval ends: rays from the pseudo-source through (b0, 0) and (b1, 0), in the child frame
+        const double X0 = ux * w.b0, D0 = -uy * w.b0 - isy;
+        if (r1 >= 0) {
+            c.b0 = isx + (X0 - isx) * (-isy) / D0;
+            c.b1 = M.geom[9 * (t / 3) + 3 * (t % 3)];
+        } else {
+            const double X1 = ux * w.b1, D1 = -uy * w.b1 - isy;
+            const double R = 1.0 / (D0 * D1);
+            c.b0 = isx + (X0 - isx) * (-isy) * (R * D1);
+            c.b1 = isx + (X1 - isx) * (-isy) * (R * D0);
+        }
+    } else {  // exit through edge B->C (local j+1); child frame: origin C, x toward B
+        const int t = M.twin[3 * g + (j + 1) % 3];
+        ux = M.exitu[12 * g + 4 * j + 2];
+        uy = M.exitu[12 * g + 4 * j + 3];
+        const double rx = w.sx - cx, ry = w.sy - cy;
+        const double isx = ux * rx + uy * ry, isy = -uy * rx + ux * ry;
+        c.he = (t / 3) * 4 + t % 3;
+        c.sx = isx;
+        c.sy = isy;
+        const double X1 = ux * (w.b1 - cx) + uy * (-cy), D1 = -uy * (w.b1 - cx) + ux * (-cy) - isy;
+        if (r0 <= 0) {
+            c.b0 = 0.0;
+            c.b1 = isx + (X1 - isx) * (-isy) / D1;
+        } else {
+            const double X0 = ux * (w.b0 - cx) + uy * (-cy), D0 = -uy * (w.b0 - cx) + ux * (-cy) - isy;
+            const double R = 1.0 / (D0 * D1);
+            c.b0 = isx + (X0 - isx) * (-isy) * (R * D1);
+            c.b1 = isx + (X1 - isx) * (-isy) * (R * D0);
         }
     }
-    if (w.b1 > xC) {  // exit through edge B->C (local j+1); child frame: origin C, x toward B
-        int t = M.twin[3 * g + (j + 1) % 3];
-        if (t >= 0) {
-            const double ux = M.exitu[12 * g + 4 * j + 2], uy = M.exitu[12 * g + 4 * j + 3];
-            double rx = w.sx - cx, ry = w.sy - cy;
-            double isx = ux * rx + uy * ry, isy = -uy * rx + ux * ry;
-            Win c;
-            c.he = (t / 3) * 4 + t % 3;
-            c.sigma = w.sigma;
-            c.sx = isx;
-            c.sy = isy;
-            if (w.b0 <= xC) c.b0 = 0.0;
-            else {
-                double X = ux * (w.b0 - cx) + uy * (-cy), Y = -uy * (w.b0 - cx) + ux * (-cy);
-                c.b0 = isx + (X - isx) * (-isy) / (Y - isy);
-            }
-            {
-                double X = ux * (w.b1 - cx) + uy * (-cy), Y = -uy * (w.b1 - cx) + ux * (-cy);
-                c.b1 = isx + (X - isx) * (-isy) / (Y - isy);
-            }
-            if (w.sigma == 0) {
-                c.c = w.c * ux - w.s * uy;
-                c.s = w.s * ux + w.c * uy;
-            } else {
-                c.c = w.c;
-                c.s = w.s;
-            }
-            push_win(M, S, C, src, ctl, c);
-        }
+    if (w.sigma == 0) {
+        c.c = w.c * ux - w.s * uy;
+        c.s = w.s * ux + w.c * uy;
+    } else {
+        c.c = w.c;
+        c.s = w.s;
     }
+    push_win(M, S, C, src, ctl, c);
 }
 
 __device__ __forceinline__ double warp_min(double x)
@@ -549,9 +613,8 @@ __device__ __noinline__ double target_query(const DevMesh& M, const Slot& S, con
         const double L = M.geom[9 * g + 3 * j], cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
         double b1 = S.tb[3 * t + (j + 1) % 3], b2 = S.tb[3 * t + (j + 2) % 3];
         double px = b1 * L + b2 * cx, py = b2 * cy;
-        double xp = w.sx + (px - w.sx) * (-w.sy) / (py - w.sy);
         const double tol = 1e-12 * L;
-        if (xp >= w.b0 - tol && xp <= w.b1 + tol) {
+        if (ray_hits(w, px, py, tol)) {
             double d = w.sigma + len2(px - w.sx, py - w.sy);
             if (d < best) {
                 best = d;
@@ -1015,11 +1078,15 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             resolve(M, S, C, src, ctl, r);
         }
         __syncwarp();
-        // windows within the band
+        // windows within the band, 32 at a time: each lane classifies one window, then the vertex proposals and the
+        // child windows of the batch are spread over all lanes (FP64 instructions cost the same with 1 or 32 lanes)
         for (int base = 0; base < nA; base += 32) {
-            int q = base + lane;
-            VRec r[3];
-            r[0].slot = r[1].slot = r[2].slot = -1;
+            const int q = base + lane;
+            if (lane == 0) {
+                ctl->nPT = 0;
+                ctl->nCT = 0;
+            }
+            __syncwarp();
             if (q < nA) {
                 Win w = S.wA[q];
                 if ((double)w.key > thr) {
@@ -1027,11 +1094,20 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                     if (pos < C.CW) S.wB[pos] = w;
                     else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
                 } else {
-                    process(M, S, C, src, ctl, w, r, processed);
+                    classify(M, S, C, ctl, w, q, processed);
                 }
             }
             __syncwarp();
-            for (int k = 0; k < 3; ++k) resolve(M, S, C, src, ctl, r[k]);
+            const int nPT = ctl->nPT, nCT = ctl->nCT;
+            for (int p0 = 0; p0 < nPT; p0 += 32) {
+                VRec r;
+                r.slot = -1;
+                if (p0 + lane < nPT) proposal_task(M, S, C, ctl, S.taskP[p0 + lane], r);
+                __syncwarp();
+                resolve(M, S, C, src, ctl, r);
+                __syncwarp();
+            }
+            for (int p = lane; p < nCT; p += 32) child_task(M, S, C, src, ctl, S.taskC[p]);
             __syncwarp();
         }
     }
@@ -1158,6 +1234,7 @@ __device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, int la
 __global__ void __launch_bounds__(256) geodesic_kernel(GeoLaunch L)
 {
     __shared__ WarpCtl ctls[8];
+    __shared__ int tasks[8][kTaskP + kTaskC];
     extern __shared__ __align__(16) char dyn[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -1166,6 +1243,8 @@ __global__ void __launch_bounds__(256) geodesic_kernel(GeoLaunch L)
     WarpCtl* ctl = &ctls[wib];
     Slot S;
     carve(L.caps, (char*)L.scratch + (size_t)warp * L.slotBytes, &S);
+    S.taskP = &tasks[wib][0];
+    S.taskC = &tasks[wib][kTaskP];
     if (L.smemTables) {
         carve_smem(L.caps, dyn + (size_t)wib * smem_per_warp(L.caps), &S);
         for (int q = lane; q < L.caps.CV; q += 32) {
@@ -1322,7 +1401,23 @@ void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
             configured = budget;
         }
     }
-    int blocks = (L.nSlots + wpb - 1) / wpb;
+    // spread the warps evenly over the SMs: sources are FP64-pipe bound per SM, so an SM holding two blocks while
+    // another holds one would take twice as long.  Full occupancy = sms * bps blocks; fewer slots than that get
+    // fewer warps per block, not fewer blocks.
+    int dev = 0, sms = 1, bps = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, geodesic_kernel, 32 * wpb, smem);
+    bps = std::max(bps, 1);
+    const long long full = (long long)sms * bps;
+    int blocks;
+    if ((long long)L.nSlots >= full * wpb) {
+        blocks = (L.nSlots + wpb - 1) / wpb;
+    } else {
+        wpb = (int)((L.nSlots + full - 1) / full);  // warps per block; warps past nSlots return at once
+        if (L.smemTables) smem = per * wpb;
+        blocks = (int)full;
+    }
     geodesic_kernel<<<blocks, 32 * wpb, smem, s>>>(L);
 }
 

@@ -21,13 +21,14 @@ def _torch():
     return torch
 
 
-def pairs_from_exact_solver(ctx, V, F, n, sigma, seed, data_cutoff=1.5):
+def pairs_from_exact_solver(ctx, V, F, n, sigma, seed, data_cutoff=1.5, mesh=None):
     """Exact candidate-pair distances of one random configuration (reference patches, cell list with range sigma,
-    geodesics followed to data_cutoff * sigma).  Returns device tensors X (bf16 features), y, chord/sigma, d/sigma."""
+    geodesics followed to data_cutoff * sigma).  Returns device tensors X (bf16 features), y, chord/sigma, d/sigma.
+    mesh: the api.Mesh of (V, F) when the caller already holds one."""
     torch = _torch()
     rng = np.random.default_rng(seed)
     f, b = ms.area_weighted_positions(V, F, n, rng)
-    M = api.Mesh(V, F, device=ctx.device)
+    M = mesh if mesh is not None else api.Mesh(V, F, device=ctx.device)
     p = api.make_params("nve", "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=sigma, submesh=True,
                         max_dist=sigma, cutoff=data_cutoff * sigma, dt=1e-3)
     S = api.System(ctx, M, n, p)
@@ -56,8 +57,9 @@ def generate(ctx, mesh_fn, seeds, n, sigma, pairs_per_seed=None, configs_per_see
     Xs, ys, cs, ds = [], [], [], []
     for s in seeds:
         V, F = mesh_fn(s)
+        M = api.Mesh(V, F, device=ctx.device)
         for c in range(configs_per_seed):
-            X, y, ch, d = pairs_from_exact_solver(ctx, V, F, n, sigma, 1000 * s + c)
+            X, y, ch, d = pairs_from_exact_solver(ctx, V, F, n, sigma, 1000 * s + c, mesh=M)
             Xs.append(X)
             ys.append(y)
             cs.append(ch)
