@@ -49,6 +49,10 @@ def workload_config(name):
         return dict(workload="bumpy_sphere7_N20000_nve_patch_screen", mesh=("bumpy", 7, 0), n=20000, sigma=0.02,
                     integrator="nve", submesh=True, range_=0.02, dt=0.002, T=0.1, seed=4, screen=True,
                     train_seeds=list(range(1, 9)), configs_per_seed=6, holdout_seeds=[9, 10], train_steps=3000)
+    if name == "noisy_torus_nvt":
+        return dict(workload="noisy_torus1000x500_N100000_nvt_patch", mesh=("noisy_torus", 1000, 500), n=100000,
+                    phi=0.5, sigma=None, integrator="nvt", submesh=True, range_=None, dt=0.001, T=0.05, seed=5,
+                    cpu_subset=1000)
     if name == "torus_nvt":
         return dict(workload="torus200x100_N2000_nvt_patch", mesh=("torus", 200, 100), n=2000, sigma=0.3,
                     integrator="nvt", submesh=True, range_=0.3, dt=0.002, T=0.05, seed=2)
@@ -88,6 +92,8 @@ def build_inputs(cfg):
         V, F = ms.torus(cfg["mesh"][1], cfg["mesh"][2], 3.0, 1.0)
     elif cfg["mesh"][0] == "bumpy":
         V, F = ms.bumpy_sphere(cfg["mesh"][1], amplitude=0.05, seed=cfg["mesh"][2])
+    elif cfg["mesh"][0] == "noisy_torus":
+        V, F = ms.noisy_torus(cfg["mesh"][1], cfg["mesh"][2], 3.0, 1.0, std=0.01, smoothing_rings=3, seed=0)
     else:
         V, F = ms.icosphere(cfg["mesh"][1])
     rng = np.random.default_rng(cfg["seed"])
@@ -184,7 +190,11 @@ def systems_of(cfg):
             sy["range_"] = sy["sigma"]
         return out
     V, F, f, b, vel = build_inputs(cfg)
-    return [dict(V=V, F=F, n=cfg["n"], sigma=cfg["sigma"], range_=cfg["range_"], f=f, b=b, vel=vel)]
+    sigma = cfg["sigma"]
+    if sigma is None:  # from the area fraction: sigma = 2 sqrt(phi A / (N pi))
+        sigma = ms.sigma_for_area_fraction(ms.total_area(V, F), cfg["n"], cfg["phi"])
+    rng_ = cfg["range_"] if cfg["range_"] is not None else sigma
+    return [dict(V=V, F=F, n=cfg["n"], sigma=sigma, range_=rng_, f=f, b=b, vel=vel)]
 
 
 def oracle_step_rate(cfg, systems, threads, budget_s, max_steps=200):
@@ -220,7 +230,7 @@ def run_reference(args, cfg):
     world, rank, _, pg = dist_setup()
     if rank != 0:
         return
-    systems = systems_of(cfg)
+    systems, note = _cpu_subset(cfg, systems_of(cfg))
     threads = os.cpu_count() or 1
     oracle_step_rate(cfg, systems, threads, 0.0, max_steps=args.warmup)  # warm-up
     value, steps = oracle_step_rate(cfg, systems, threads, 1e30, max_steps=args.steps)
@@ -232,20 +242,31 @@ def run_reference(args, cfg):
         "config": {"workload": cfg["workload"], "n": sum(sy["n"] for sy in systems), "systems": len(systems),
                    "integrator": cfg["integrator"], "submesh": cfg["submesh"], "l2": "cpu run"},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{steps} full steps of the workload (oracle restatement; CGAL reference not "
-                                   f"buildable)"},
+                         "sample": f"{steps} full steps of the workload{note} (oracle restatement; CGAL reference "
+                                   f"not buildable)"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
+def _cpu_subset(cfg, systems):
+    """The workload's CPU-baseline sample: the first cfg['cpu_subset'] particles of a single system, if named."""
+    k = cfg.get("cpu_subset")
+    if not k or len(systems) != 1 or systems[0]["n"] <= k:
+        return systems, ""
+    sy = dict(systems[0])
+    sy.update(n=k, f=sy["f"][:k], b=sy["b"][:k], vel=sy["vel"][:k])
+    return [sy], f" ({k}-particle subset of the same mesh and sigma)"
+
+
 def cpu_baseline(cfg, systems, seconds_budget=20.0):
     """Bounded sample of the same workload on the host: the oracle on all threads and on one thread."""
+    systems, note = _cpu_subset(cfg, systems)
     threads = os.cpu_count() or 1
     v_all, s_all = oracle_step_rate(cfg, systems, threads, seconds_budget / 2)
     v_one, s_one = oracle_step_rate(cfg, systems, 1, seconds_budget / 2)
     return {"value": v_all, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{s_all} whole steps of the workload on {threads} threads (oracle restatement; the CGAL "
+            "sample": f"{s_all} whole steps of the workload{note} on {threads} threads (oracle restatement; the CGAL "
                       f"reference is not buildable); single thread: {v_one:.1f} particle-steps/s over {s_one} steps"}
 
 

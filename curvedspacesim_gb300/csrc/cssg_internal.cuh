@@ -91,6 +91,7 @@ struct SysDesc {
     double maxDist;   // patch radius cap
     double cutoff;    // paths longer than this are not followed
     double k, sigma;  // force parameters
+    double delta;     // band width of the propagation rounds for this system's mesh (0: the launch's value)
 };
 
 // Per-launch configuration of the fused neighbour / geodesic / force kernel.
@@ -140,6 +141,7 @@ struct GeoLaunch {
     const int* itemCountDev;     // nullable: number of work items read from the device (retry pass)
     int* failList;               // nullable: sources whose tables overflowed are queued here for a retry pass
     int* failCount;
+    int routeBig;                // 1: sources of systems marked bigBin go straight to failList (first pass only)
     int smemTables;              // set by cssg_launch_geodesic: hash tables in shared memory
 };
 

@@ -691,7 +691,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     const GeoCaps& C = Lp.caps;
     const SysDesc& D = Lp.sys[Lp.sysOf ? Lp.sysOf[si] : 0];
     const DevMesh& M = D.mesh;
-    if (D.bigBin && Lp.failList) {
+    if (D.bigBin && Lp.routeBig && Lp.failList) {
         // binned to the large-table pass
         if (lane == 0) {
             Lp.status[si] = 0;
@@ -974,7 +974,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
         mk = warp_min(mk);
         __syncwarp();
         if (settled(M, S, C, src, nT, mk, lane)) break;
-        const double thr = mk + Lp.delta;
+        const double thr = mk + (D.delta > 0 ? D.delta : Lp.delta);
         // pseudo-source launches within the band; the rest stay queued.  Decide per queued vertex, then spread the
         // (vertex, incident face) pairs over the lanes.
         for (int q = lane; q < nP; q += 32) {

@@ -323,14 +323,19 @@ struct cssg_system {
     int* slotOf = nullptr;
     int* scanBlocks = nullptr;
     int nScanBlocks = 0;
-    // geodesic scratch (regular and retry passes)
-    GeoCaps caps, bigCaps;
+    // geodesic scratch of the three passes: regular (tables in shared memory when they fit), medium (sources of
+    // large-patch systems and regular overflows, many warps) and large (medium overflows, one warp per SM)
+    GeoCaps caps, midCaps, bigCaps;
     void* scratch = nullptr;
+    void* midScratch = nullptr;
     void* bigScratch = nullptr;
-    size_t slotBytes = 0, bigSlotBytes = 0;
-    int nSlots = 0, nBigSlots = 0;
-    int* work = nullptr;  // [0] work counter, [1] retry work counter, [2] failure count
-    int* failList = nullptr;
+    size_t slotBytes = 0, midSlotBytes = 0, bigSlotBytes = 0;
+    int nSlots = 0, nMidSlots = 0, nBigSlots = 0;
+    // [0] regular work counter, [1] medium work counter, [2] medium item count, [3] large work counter,
+    // [4] large item count
+    int* work = nullptr;
+    int* failList = nullptr;   // sources for the medium pass
+    int* failList2 = nullptr;  // sources for the large pass
     // pair output
     int pairCap = 0;
     double* pairD = nullptr;
@@ -362,7 +367,7 @@ struct cssg_system {
     // graph
     cudaGraphExec_t graphExec = nullptr;
     double delta = 1e300;  // bucket width of the propagation order (distance-banded rounds)
-    int maxWindows = 0, bigMaxWindows = 0;  // per-source work caps of the regular and large-table passes
+    int maxWindows = 0, midMaxWindows = 0, bigMaxWindows = 0;  // per-source work caps of the three passes
     // timing
     bool timing = false;
     std::vector<cudaEvent_t> events;
@@ -405,7 +410,7 @@ void launch_forces(cssg_system* s)
                                                        s->slotOf);
         cell_sort<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->cellOf, s->cellStart, s->slotOf, s->cellList);
     }
-    cudaMemsetAsync(s->work, 0, 3 * sizeof(int), st);
+    cudaMemsetAsync(s->work, 0, 5 * sizeof(int), st);
     GeoLaunch L;
     memset(&L, 0, sizeof(L));
     L.sys = s->screen ? s->dsysScreen : s->dsys;
@@ -438,6 +443,7 @@ void launch_forces(cssg_system* s)
     L.workCounter = s->work;
     L.failList = s->failList;
     L.failCount = s->work + 2;
+    L.routeBig = 1;
     if (s->screen) {
         // learned screen: candidate rows -> CSR pairs -> features -> tensor-core MLP -> skip flags; the propagation
         // then reads the CSR (screened pairs keep their faces in the patch but are not queried)
@@ -461,20 +467,34 @@ void launch_forces(cssg_system* s)
     }
     record(s);
     cssg_launch_geodesic(L, st);
-    // retry pass with large tables for the sources whose tables overflowed (usually none: exits at once)
+    // medium pass: sources of large-patch systems and regular-pass overflows (exits at once when there are none)
     GeoLaunch R = L;
-    R.caps = s->bigCaps;
-    R.scratch = s->bigScratch;
-    R.slotBytes = s->bigSlotBytes;
-    R.nSlots = s->nBigSlots;
+    R.caps = s->midCaps;
+    R.scratch = s->midScratch;
+    R.slotBytes = s->midSlotBytes;
+    R.nSlots = s->nMidSlots;
     R.workCounter = s->work + 1;
     R.order = s->failList;
     R.itemCountDev = s->work + 2;
-    R.failList = nullptr;
-    R.failCount = nullptr;
+    R.failList = s->failList2;
+    R.failCount = s->work + 4;
+    R.routeBig = 0;
     R.maxRounds = 1 << 15;
-    R.maxWindows = s->bigMaxWindows;
+    R.maxWindows = s->midMaxWindows;
     cssg_launch_geodesic(R, st);
+    // large pass: medium-pass overflows
+    GeoLaunch B = R;
+    B.caps = s->bigCaps;
+    B.scratch = s->bigScratch;
+    B.slotBytes = s->bigSlotBytes;
+    B.nSlots = s->nBigSlots;
+    B.workCounter = s->work + 3;
+    B.order = s->failList2;
+    B.itemCountDev = s->work + 4;
+    B.failList = nullptr;
+    B.failCount = nullptr;
+    B.maxWindows = s->bigMaxWindows;
+    cssg_launch_geodesic(B, st);
     record(s);
     status_or<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->srcStatus, s->statusBits);
 }
@@ -591,8 +611,9 @@ extern "C" int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh*
     TRY(alloc((void**)&s->srcStatus, sizeof(int) * n));
     TRY(alloc((void**)&s->statusBits, sizeof(int)));
     TRY(alloc((void**)&s->counters, sizeof(unsigned long long) * 8));
-    TRY(alloc((void**)&s->work, sizeof(int) * 4));
+    TRY(alloc((void**)&s->work, sizeof(int) * 5));
     TRY(alloc((void**)&s->failList, sizeof(int) * n));
+    TRY(alloc((void**)&s->failList2, sizeof(int) * n));
     TRY(alloc((void**)&s->ke, sizeof(double) * n));
     TRY(alloc((void**)&s->dPartBase, sizeof(int) * (K + 1)));
     cudaMemset(s->force, 0, sizeof(double) * 3 * n);
@@ -617,6 +638,7 @@ extern "C" int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh*
     long long maxF = 0, maxV = 0, maxT = 0;           // regular tables: systems whose patches fit shared memory
     long long bigF = 0, bigV = 0, bigT = 0;           // large tables: every system (retry and binned sources)
     const long long kRegularTable = 1024;             // entries per table that keep a warp's tables in ~20 KB
+    bool anyBig = false;
     for (int k = 0; k < K; ++k) {
         const cssg_params& P = params[k];
         const cssg_mesh* m = meshes[k];
@@ -634,6 +656,7 @@ extern "C" int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh*
         D.cutoff = P.cutoff;
         D.k = P.k;
         D.sigma = P.sigma;
+        D.delta = m->meanEdge;
         long long cells = 1;
         for (int c = 0; c < 3; ++c) {
             double ext = m->d.bbMax[c] - m->d.bbMin[c];
@@ -670,6 +693,7 @@ extern "C" int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh*
         bigT = std::max(bigT, estT);
         if (next_pow2_ll(3 * (estF + estT) / 2 + 32) > kRegularTable || next_pow2_ll(2 * estV + 32) > kRegularTable) {
             D.bigBin = 1;
+            anyBig = true;
         } else {
             maxF = std::max(maxF, estF);
             maxV = std::max(maxV, estV);
@@ -707,25 +731,44 @@ extern "C" int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh*
     s->caps.CW = (int)(6 * maxF + 256);
     s->caps.CL = (int)(maxV + 64);
     s->caps.CLOG = (int)(4 * s->caps.CT + 2 * maxF + 128);
-    // large tables: 4x the largest estimate of any system (and never smaller than 8x the regular ones)
-    s->bigCaps.CT = (int)std::max<long long>(std::max(s->caps.CT * 8, std::min(n, 4096)), 4 * bigT);
-    s->bigCaps.CF = next_pow2_ll(std::max<long long>(8LL * s->caps.CF, 6 * (bigF + bigT)));
-    s->bigCaps.CV = next_pow2_ll(std::max<long long>(8LL * s->caps.CV, 8 * bigV));
-    s->bigCaps.CW = (int)std::max<long long>(16LL * s->caps.CW, 24 * bigF + 1024);
-    s->bigCaps.CL = (int)std::max<long long>(16LL * s->caps.CL, 4 * bigV + 256);
-    s->bigCaps.CLOG = (int)std::max<long long>(16LL * s->caps.CLOG + 8 * s->bigCaps.CT, 16 * bigT + 8 * bigF);
+    // medium tables: the largest estimate of any system with the regular pass's margins, and never smaller than
+    // 2x the regular tables
+    s->midCaps.CT = (int)std::max<long long>(2LL * s->caps.CT, bigT);
+    s->midCaps.CF = next_pow2_ll(std::max<long long>(2LL * s->caps.CF, 3 * (bigF + s->midCaps.CT) / 2 + 32));
+    s->midCaps.CV = next_pow2_ll(std::max<long long>(2LL * s->caps.CV, 2 * bigV + 32));
+    s->midCaps.CW = (int)std::max<long long>(2LL * s->caps.CW, 6 * bigF + 256);
+    s->midCaps.CL = (int)std::max<long long>(2LL * s->caps.CL, bigV + 64);
+    s->midCaps.CLOG = (int)std::max<long long>(2LL * s->caps.CLOG, 4 * s->midCaps.CT + 2 * bigF + 128);
+    // large tables: 4x the largest estimate of any system (and never smaller than 4x the medium ones)
+    s->bigCaps.CT = (int)std::max<long long>(std::max(s->midCaps.CT * 4, std::min(n, 4096)), 4 * bigT);
+    s->bigCaps.CF = next_pow2_ll(std::max<long long>(4LL * s->midCaps.CF, 6 * (bigF + bigT)));
+    s->bigCaps.CV = next_pow2_ll(std::max<long long>(4LL * s->midCaps.CV, 8 * bigV));
+    s->bigCaps.CW = (int)std::max<long long>(4LL * s->midCaps.CW, 24 * bigF + 1024);
+    s->bigCaps.CL = (int)std::max<long long>(4LL * s->midCaps.CL, 4 * bigV + 256);
+    s->bigCaps.CLOG = (int)std::max<long long>(4LL * s->midCaps.CLOG + 8 * s->bigCaps.CT, 16 * bigT + 8 * bigF);
     s->maxWindows = (int)std::min<long long>(1 << 30, 200 * maxF + 20000);
+    s->midMaxWindows = (int)std::min<long long>(1 << 30, 200 * bigF + 20000);
     s->bigMaxWindows = (int)std::min<long long>(1 << 30, 400 * bigF + 100000);
     s->slotBytes = cssg_geo_slot_bytes(s->caps);
+    s->midSlotBytes = cssg_geo_slot_bytes(s->midCaps);
     s->bigSlotBytes = cssg_geo_slot_bytes(s->bigCaps);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     s->nSlots = std::min(n, sms * 32);
     s->nSlots = ((s->nSlots + 7) / 8) * 8;
     s->nBigSlots = std::min(n, sms);
+    // medium pass: up to 16 warps per SM when some system is routed there, else a token pass for overflows; the
+    // slot count is capped so that the medium scratch stays within 8 GB
+    {
+        long long want = anyBig ? (long long)sms * 16 : (long long)sms;
+        long long fit = std::max<long long>(1, (8LL << 30) / (long long)s->midSlotBytes);
+        s->nMidSlots = (int)std::max<long long>(1, std::min<long long>({(long long)n, want, fit}));
+    }
     TRY(alloc(&s->scratch, s->slotBytes * (size_t)s->nSlots));
+    TRY(alloc(&s->midScratch, s->midSlotBytes * (size_t)s->nMidSlots));
     TRY(alloc(&s->bigScratch, s->bigSlotBytes * (size_t)s->nBigSlots));
     cssg_geo_init_scratch(s->scratch, s->slotBytes, s->nSlots, s->caps, ctx->stream);
+    cssg_geo_init_scratch(s->midScratch, s->midSlotBytes, s->nMidSlots, s->midCaps, ctx->stream);
     cssg_geo_init_scratch(s->bigScratch, s->bigSlotBytes, s->nBigSlots, s->bigCaps, ctx->stream);
     TRY(alloc((void**)&s->chains, sizeof(double) * chain_len(s) * K));
     cudaMemset(s->chains, 0, sizeof(double) * chain_len(s) * K);
@@ -756,7 +799,8 @@ extern "C" int cssg_system_destroy(cssg_system* s)
     for (cudaEvent_t e : s->events) cudaEventDestroy(e);
     void* ptrs[] = {s->face, s->bary, s->vel, s->force, s->disp, s->pos, s->walkStatus, s->srcStatus,
                     s->statusBits, s->counters, s->cellOf, s->cellCount, s->cellStart, s->cellCursor, s->cellList,
-                    s->slotOf, s->scanBlocks, s->scratch, s->bigScratch, s->work, s->failList, s->pairD, s->pairT,
+                    s->slotOf, s->scanBlocks, s->scratch, s->midScratch, s->bigScratch, s->work, s->failList,
+                    s->failList2, s->pairD, s->pairT,
                     s->pairJ, s->pairCount, s->chains, s->ke, s->dsys, s->dmeshes, s->sysOf, s->dPartBase,
                     s->mlpParams, s->candJPad, s->candCount, s->maxChord, s->candOff, s->pairI, s->pairJc, s->X,
                     s->chordS, s->yhat, s->skip, s->candScanBlocks, s->mlpErr, s->screenCounters, s->dsysScreen};
