@@ -262,13 +262,18 @@ __device__ __forceinline__ bool ray_hits(const Win& w, double px, double py, dou
     return xp >= w.b0 - tol && xp <= w.b1 + tol;
 }
 
-__device__ __forceinline__ double key_of(const Win& w)
+// Lower bound (FP32, rounded down) of the window's distances: sigma + the distance from the pseudo-source to the
+// interval.  The float evaluation's error is far below the 1e-6 * scale subtracted, so the bound stays below the
+// exact value: the banding and the early exit only need a lower bound.
+__device__ __forceinline__ float key_lo(const Win& w)
 {
-    double m;
-    if (w.sx < w.b0) m = len2(w.sx - w.b0, w.sy);
-    else if (w.sx > w.b1) m = len2(w.sx - w.b1, w.sy);
-    else m = fabs(w.sy);
-    return w.sigma + m;
+    const float sx = (float)w.sx, sy = (float)w.sy, b0 = (float)w.b0, b1 = (float)w.b1;
+    float m;
+    if (sx < b0) m = sqrtf((sx - b0) * (sx - b0) + sy * sy);
+    else if (sx > b1) m = sqrtf((sx - b1) * (sx - b1) + sy * sy);
+    else m = fabsf(sy);
+    const float scale = fabsf(sx) + fabsf(sy) + fabsf(b0) + fabsf(b1);
+    return __fsub_rd(__fadd_rd(__double2float_rd(w.sigma), m), 1e-6f * scale + 1e-6f * m);
 }
 
 __device__ __forceinline__ bool in_domain(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int g)
@@ -280,61 +285,83 @@ __device__ __forceinline__ bool in_domain(const DevMesh& M, const Slot& S, const
 
 // Remove the parts of the window that a path through an endpoint vertex of its edge beats.  The excess of the
 // window's path over the vertex path is monotone along the edge, so the dominated part is an interval at that end,
-// bounded by the root of a linear equation.  The tests compare squared lengths (no square roots); the opposite
-// vertex can only discard the window as a whole and is tested in FP32 with a 1e-5 relative safety margin (it is a
-// pruning test: a conservative answer keeps the window).
+// bounded by the root of a linear equation.  This is a pruning test, so it runs in FP32 with margins that make it
+// conservative: inputs are rounded from FP64 (relative error 6e-8), and every decision below holds with a margin of
+// 1e-5 * scale^2 (squared lengths) or 1e-6 * scale (lengths), at least 10x the worst float error, where scale bounds
+// the magnitudes involved.  An undecided case keeps the window; a trimmed end is moved back by the root's error
+// bound.  The interval itself (and every distance) stays FP64.
+__device__ __forceinline__ bool trim_end(float a, float sx, float sy2, float b, float bfar, float scale, float& xs)
+{
+    // end at b (distance b from the vertex along the edge), pseudo-source at (sx, sy) in the frame with the vertex at
+    // the origin; a = vertex label - sigma.  Returns false when the whole window is dominated; xs = new end (>= b)
+    // when the end is dominated, else xs = b.
+    xs = b;
+    const float eps = 1e-6f * scale, eps2 = 1e-5f * scale * scale;
+    const float r = a + b, dx = b - sx;
+    const bool dominated = (r < -eps) || (r >= -eps && dx * dx + sy2 > r * r + eps2);
+    if (!dominated) return true;
+    const float den = a + sx;  // > 0: the dominated part ends inside the edge line
+    if (den < -eps) return false;
+    if (den <= eps) return true;  // undecided: keep
+    const float num = (sx - a) * (sx + a) + sy2;
+    float root = num / (2.0f * den);
+    root -= 1e-5f * scale * (scale + fabsf(root)) / den;  // error bound of the float root
+    if (root >= bfar) return false;
+    if (root > b) xs = root;
+    return true;
+}
+
 __device__ __noinline__ bool trim(const DevMesh& M, const Slot& S, const GeoCaps& C, Win& w)
 {
     const int g = w.he >> 2, j = w.he & 3;
     const double L = M.geom[9 * g + 3 * j];
     const int A = M.F[3 * g + j], B = M.F[3 * g + (j + 1) % 3], Cv = M.F[3 * g + (j + 2) % 3];
-    const double sy2 = w.sy * w.sy;
-    double dA = vlabel(S, C.CV, A);
+    const float sx = (float)w.sx, sy = (float)w.sy, Lf = (float)L;
+    const float sy2 = sy * sy;
+    const float b0 = (float)w.b0, b1 = (float)w.b1;
+    const double dA = vlabel(S, C.CV, A);
     if (dA < CUDART_INF) {
-        double a = dA - w.sigma;
-        // dominated at b0 <=> |I - (b0,0)| > a + b0
-        double r = a + w.b0, dx = w.b0 - w.sx;
-        if (r < 0 || dx * dx + sy2 > r * r) {
-            if (a + w.sx <= 0) return false;
-            double xs = (w.sx * w.sx + sy2 - a * a) / (2.0 * (a + w.sx));
-            if (xs >= w.b1) return false;
-            w.b0 = fmax(w.b0, xs);
-        }
+        const float a = (float)(dA - w.sigma);
+        const float scale = fabsf(sx) + fabsf(sy) + Lf + fabsf(a);
+        float xs;
+        if (!trim_end(a, sx, sy2, b0, b1, scale, xs)) return false;
+        if (xs > b0) w.b0 = fmax(w.b0, (double)xs);
     }
-    double dB = vlabel(S, C.CV, B);
+    const double dB = vlabel(S, C.CV, B);
     if (dB < CUDART_INF) {
-        double a = dB - w.sigma;
-        double sxm = L - w.sx, xm = L - w.b1;
-        double r = a + xm, dx = xm - sxm;
-        if (r < 0 || dx * dx + sy2 > r * r) {
-            if (a + sxm <= 0) return false;
-            double xs = (sxm * sxm + sy2 - a * a) / (2.0 * (a + sxm));
-            if (L - xs <= w.b0) return false;
-            w.b1 = fmin(w.b1, L - xs);
-        }
+        // mirrored frame: origin at B, x toward A
+        const float a = (float)(dB - w.sigma);
+        const float scale = fabsf(sx) + fabsf(sy) + Lf + fabsf(a);
+        const float m0 = (float)(L - w.b1), m1 = (float)(L - w.b0);
+        float xs;
+        if (!trim_end(a, Lf - sx, sy2, m0, m1, scale, xs)) return false;
+        if (xs > m0) w.b1 = fmin(w.b1, L - (double)xs);
     }
-    double dC = vlabel(S, C.CV, Cv);
+    if (!(w.b1 - w.b0 > 1e-14 * L)) return false;
+    const double dC = vlabel(S, C.CV, Cv);
     if (dC < CUDART_INF) {
         float cx = (float)M.geom[9 * g + 3 * j + 1], cy = (float)M.geom[9 * g + 3 * j + 2];
-        float b0 = (float)w.b0, b1 = (float)w.b1, sx = (float)w.sx, sy = (float)w.sy;
-        float m = fmaxf(sqrtf((cx - b0) * (cx - b0) + cy * cy), sqrtf((cx - b1) * (cx - b1) + cy * cy));
-        float near = (sx < b0) ? sqrtf((sx - b0) * (sx - b0) + sy * sy)
-                                : (sx > b1 ? sqrtf((sx - b1) * (sx - b1) + sy * sy) : fabsf(sy));
+        float e0 = (float)w.b0, e1 = (float)w.b1;
+        float m = fmaxf(sqrtf((cx - e0) * (cx - e0) + cy * cy), sqrtf((cx - e1) * (cx - e1) + cy * cy));
+        float near = (sx < e0) ? sqrtf((sx - e0) * (sx - e0) + sy2)
+                                : (sx > e1 ? sqrtf((sx - e1) * (sx - e1) + sy2) : fabsf(sy));
         if ((float)dC + m < ((float)w.sigma + near) * (1.0f - 1e-5f)) return false;
     }
-    return w.b1 - w.b0 > 1e-14 * L;
+    return true;
 }
 
 __device__ __noinline__ void push_win(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, Win w)
 {
     const int g = w.he >> 2, j = w.he & 3;
     if (g == src.f0 || !in_domain(M, S, C, src, g)) return;
+    const double L = M.geom[9 * g + 3 * j];
     w.b0 = fmax(0.0, w.b0);
-    w.b1 = fmin(M.geom[9 * g + 3 * j], w.b1);
-    if (!trim(M, S, C, w)) return;
-    const double key = key_of(w);
-    if (key > src.cutoff) return;
-    w.key = __double2float_rd(key);  // a lower bound: banding and the early exit stay conservative
+    w.b1 = fmin(L, w.b1);
+    if (!(w.b1 - w.b0 > 1e-14 * L)) return;
+    // no trim here: the window is trimmed when it is processed, against the labels of that round
+    const float key = key_lo(w);
+    if ((double)key > src.cutoff) return;
+    w.key = key;
     int pos = atomicAdd(&ctl->nB, 1);
     if (pos >= C.CW) {
         atomicExch(&ctl->err, CSSG_ST_CAPACITY);

@@ -49,3 +49,47 @@ def test_screened_path_keeps_pairs_and_distances():
     fp = plain.get_state()[3]
     fs = scr.get_state()[3]
     np.testing.assert_allclose(fs, fp, atol=1e-12)
+
+
+def test_screen_gain_on_thin_torus():
+    """What the trained network gains over the exact path alone: on a thin-tubed torus many candidate pairs
+    (chord < sigma) lie across the tube with geodesics longer than sigma.  The screen skips them (no exact
+    propagation toward them), the early exit comes sooner, and the in-range pair set stays identical."""
+    from curvedspacesim_gb300 import api, screen
+    ctx = api.Context(0)
+    n, sigma = 400, 0.5
+
+    def mesh(seed):
+        return ms.noisy_torus(60, 30, 1.0, 0.3, std=0.01, smoothing_rings=2, seed=seed)
+
+    X, y, c, _ = screen.generate(ctx, mesh, [1, 2, 3], n, sigma, configs_per_seed=2)
+    params, _ = screen.train(ctx, X, y, steps=800, batch=4096, lr=3e-3)
+    Xh, yh, ch, _ = screen.generate(ctx, mesh, [4, 5], n, sigma, configs_per_seed=2)
+    margin, info = screen.calibrate(ctx, params, Xh, yh, ch)
+    frac, wrong = screen.skipped_fraction(ctx, params, margin, Xh, yh, ch)
+    assert wrong == 0
+    V, F = mesh(0)
+    rng = np.random.default_rng(9)
+    f, b = ms.area_weighted_positions(V, F, n, rng)
+    M = api.Mesh(V, F)
+    p = api.make_params("nve", "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=sigma, submesh=True,
+                        max_dist=sigma, cutoff=sigma, dt=1e-3)
+    runs = {}
+    for name in ("plain", "screened"):
+        S = api.System(ctx, M, n, p)
+        S.set_state(f, b, np.zeros((n, 3)), np.zeros((n, 3)))
+        S.enable_pairs()
+        if name == "screened":
+            S.set_screen(params, margin)
+        S.compute_forces()
+        bits, cnt = S.check()
+        assert bits == 0, cnt
+        runs[name] = (S, cnt)
+    sc = runs["screened"][0].screen_counters()
+    missing, extra, err = screen.audit(runs["plain"][0].pairs(), runs["screened"][0].pairs(), sigma)
+    assert not missing and not extra and err <= 1e-12
+    w_plain, w_scr = runs["plain"][1]["windows"], runs["screened"][1]["windows"]
+    print(f"thin torus: holdout skip fraction {frac:.3f}, evaluation skipped {sc['screened']} of {sc['pairs']} "
+          f"candidate pairs, windows {w_plain} -> {w_scr}")
+    assert sc["screened"] > 0
+    assert w_scr < w_plain
