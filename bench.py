@@ -294,12 +294,21 @@ def run_ours(args, cfg):
     with ctx.use():
         flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
-    # warm-up (also captures the graph)
+    # warm-up, then the autotuner (band width, CTA size, medium-pass slots) on the warmed-up state, then one more
+    # step that captures the graph with the chosen configuration
     S.step(max(args.warmup, 1), graph=not args.profile)
     torch.cuda.synchronize()
     bits, cnt = S.check()
     if bits:
         raise RuntimeError(f"per-item errors during warm-up: {bits:#x} {cnt}")
+    tune = None
+    if not args.no_autotune:
+        tune = S.autotune(reps=2)
+        S.step(1, graph=not args.profile)
+        torch.cuda.synchronize()
+        bits, cnt = S.check()
+        if bits:
+            raise RuntimeError(f"per-item errors after autotuning: {bits:#x} {cnt}")
     if args.profile:
         S.step(1, graph=False)
         torch.cuda.synchronize()
@@ -391,7 +400,8 @@ def run_ours(args, cfg):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": cfg["workload"], "n": n, "systems": len(systems), "integrator": cfg["integrator"],
                        "submesh": cfg["submesh"], "graph": True,
-                       "l2": "flushed before every timed step (512 MB write)", "parallelism": f"replicas x{world}"},
+                       "l2": "flushed before every timed step (512 MB write)", "parallelism": f"replicas x{world}",
+                       "autotune": tune},
             "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": io_bytes,
                     "d2h_bytes_per_step": io_bytes},
             "gpu_launches": kps * args.steps,
@@ -466,8 +476,12 @@ def run_screen(args, cfg):
     stream = ctx.tstream
     with ctx.use():
         flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
-    for S in (plain, scr):
+    tunes = {}
+    for name, S in (("plain", plain), ("screened", scr)):
         S.step(max(args.warmup, 1), graph=True)
+        if not args.no_autotune:
+            tunes[name] = S.autotune(reps=2)
+            S.step(1, graph=True)
     torch.cuda.synchronize()
     for name, S in (("plain", plain), ("screened", scr)):
         bits, cnt = S.check()
@@ -538,7 +552,7 @@ def run_screen(args, cfg):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": cfg["workload"], "n": n, "integrator": cfg["integrator"], "submesh": True,
                        "graph": True, "l2": "flushed before every timed step (512 MB write)",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}", "autotune": tunes or None},
             "plain": {"value": value_plain, "ms_per_step": t_plain / args.steps, "geodesic_ms": kt["plain"]},
             "screened": {"value": value, "ms_per_step": t_scr / args.steps, "geodesic_ms": kt["screened"],
                          "speedup_vs_plain": value / value_plain, "counters": sc},
@@ -564,6 +578,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="torus_nvt")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (band width 1, 8 warps)")
     ap.add_argument("--profile", action="store_true",
                     help="minimal run for ncu: warm-up steps, then one step without graph replay, no other legs")
     args = ap.parse_args()

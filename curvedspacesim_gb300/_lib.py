@@ -25,6 +25,7 @@ EXPORTS = [
     "cssg_system_reset_thermostat", "cssg_system_kernels_per_step", "cssg_diag_fp64_peak",
     "cssg_system_create_batched", "cssg_mlp_param_count", "cssg_screen_features", "cssg_mlp_infer", "cssg_mlp_grad",
     "cssg_mlp_adam", "cssg_system_set_screen", "cssg_system_screen_counters", "cssg_distance_batch_noalloc",
+    "cssg_system_set_tuning", "cssg_system_autotune",
 ]
 
 
@@ -89,6 +90,8 @@ def load(build_if_missing: bool = True):
     L.cssg_system_device_state.argtypes = [P, PP, PP, PP, PP]
     L.cssg_system_step.argtypes = [P, I, I]
     L.cssg_system_compute_forces.argtypes = [P]
+    L.cssg_system_set_tuning.argtypes = [P, D, I, I]
+    L.cssg_system_autotune.argtypes = [P, I, P]
     L.cssg_system_check.argtypes = [P, P, P]
     L.cssg_system_pairs.argtypes = [P, I, P, P, P, P, P]
     L.cssg_system_chain.argtypes = [P, P, I]

@@ -142,6 +142,8 @@ struct GeoLaunch {
     int* failList;               // nullable: sources whose tables overflowed are queued here for a retry pass
     int* failCount;
     int routeBig;                // 1: sources of systems marked bigBin go straight to failList (first pass only)
+    double deltaScale;           // band width = deltaScale * the system's delta (<= 0: 1)
+    int wpbMax;                  // largest warps per block (CTA size / 32; <= 0: 8)
     int smemTables;              // set by cssg_launch_geodesic: hash tables in shared memory
 };
 

@@ -1001,7 +1001,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
         mk = warp_min(mk);
         __syncwarp();
         if (settled(M, S, C, src, nT, mk, lane)) break;
-        const double thr = mk + (D.delta > 0 ? D.delta : Lp.delta);
+        const double thr = mk + (Lp.deltaScale > 0 ? Lp.deltaScale : 1.0) * (D.delta > 0 ? D.delta : Lp.delta);
         // pseudo-source launches within the band; the rest stay queued.  Decide per queued vertex, then spread the
         // (vertex, incident face) pairs over the lanes.
         for (int q = lane; q < nP; q += 32) {
@@ -1416,11 +1416,12 @@ void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
 {
     const size_t per = smem_per_warp(L.caps);
     const size_t budget = 200 * 1024;
-    int wpb = 8;
+    const int wmax = (L.wpbMax > 0 && L.wpbMax < 8) ? L.wpbMax : 8;
+    int wpb = wmax;
     size_t smem = 0;
     L.smemTables = per <= budget ? 1 : 0;
     if (L.smemTables) {
-        wpb = (int)std::min<size_t>(8, budget / per);
+        wpb = (int)std::min<size_t>(wmax, budget / per);
         smem = per * wpb;
         static size_t configured = 48 * 1024;
         if (smem > configured) {

@@ -367,6 +367,10 @@ struct cssg_system {
     // graph
     cudaGraphExec_t graphExec = nullptr;
     double delta = 1e300;  // bucket width of the propagation order (distance-banded rounds)
+    // tuning (cssg_system_autotune / cssg_system_set_tuning): band width scale, warps per block, medium-pass slots
+    double tuneDelta = 1.0;
+    int tuneWpb = 8;
+    int midSlotsMax = 0;  // allocated medium slots; the launch uses nMidSlots <= midSlotsMax
     int maxWindows = 0, midMaxWindows = 0, bigMaxWindows = 0;  // per-source work caps of the three passes
     // timing
     bool timing = false;
@@ -444,6 +448,8 @@ void launch_forces(cssg_system* s)
     L.failList = s->failList;
     L.failCount = s->work + 2;
     L.routeBig = 1;
+    L.deltaScale = s->tuneDelta;
+    L.wpbMax = s->tuneWpb;
     if (s->screen) {
         // learned screen: candidate rows -> CSR pairs -> features -> tensor-core MLP -> skip flags; the propagation
         // then reads the CSR (screened pairs keep their faces in the patch but are not queried)
@@ -763,6 +769,7 @@ extern "C" int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh*
         long long want = anyBig ? (long long)sms * 16 : (long long)sms;
         long long fit = std::max<long long>(1, (8LL << 30) / (long long)s->midSlotBytes);
         s->nMidSlots = (int)std::max<long long>(1, std::min<long long>({(long long)n, want, fit}));
+        s->midSlotsMax = s->nMidSlots;
     }
     TRY(alloc(&s->scratch, s->slotBytes * (size_t)s->nSlots));
     TRY(alloc(&s->midScratch, s->midSlotBytes * (size_t)s->nMidSlots));
@@ -912,6 +919,108 @@ extern "C" int cssg_system_compute_forces(cssg_system* s)
     s->eventsUsed = 0;
     launch_forces(s);
     CSSG_CUDA(cudaGetLastError());
+    return CSSG_OK;
+}
+
+namespace {
+void drop_graph(cssg_system* s)
+{
+    if (s->graphExec) {
+        cudaGraphExecDestroy(s->graphExec);
+        s->graphExec = nullptr;
+    }
+}
+}  // namespace
+
+extern "C" int cssg_system_set_tuning(cssg_system* s, double delta_scale, int warps_per_block, int mid_slots)
+{
+    if (!s || !(delta_scale > 0) || warps_per_block < 1 || warps_per_block > 8) {
+        cssg_set_error("cssg_system_set_tuning: bad arguments (delta_scale > 0, 1 <= warps_per_block <= 8)");
+        return CSSG_ERR_ARG;
+    }
+    s->tuneDelta = delta_scale;
+    s->tuneWpb = warps_per_block;
+    if (mid_slots > 0) s->nMidSlots = std::min(mid_slots, s->midSlotsMax);
+    drop_graph(s);
+    return CSSG_OK;
+}
+
+// Times compute_forces (the propagation passes) on the current state for each candidate (band width scale x warps
+// per block x medium slots) and keeps the fastest.  Forces are recomputed on the same state, so the physics does
+// not change; the result differs between candidates only in the work done.
+extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_host)
+{
+    if (!s) return CSSG_ERR_ARG;
+    if (reps < 1) reps = 1;
+    cudaStream_t st = s->ctx->stream;
+    int sms = 0;
+    CSSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->ctx->device));
+    const double deltas[] = {0.5, 1.0, 2.0, 4.0};
+    const int wpbs[] = {4, 8};
+    std::vector<int> mids{s->midSlotsMax};
+    if (s->midSlotsMax > sms * 8) mids.push_back(sms * 8);
+    cudaEvent_t e0, e1;
+    CSSG_CUDA(cudaEventCreate(&e0));
+    CSSG_CUDA(cudaEventCreate(&e1));
+    double best = 1e300, bd = s->tuneDelta;
+    int bw = s->tuneWpb, bm = s->nMidSlots;
+    const bool timing = s->timing;
+    s->timing = false;
+    // status bits raised before the call are kept; a candidate that raises any (a capacity overflow) is rejected
+    int prior = 0;
+    CSSG_CUDA(cudaMemcpyAsync(&prior, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CSSG_CUDA(cudaStreamSynchronize(st));
+    for (double d : deltas)
+        for (int w : wpbs)
+            for (int m : mids) {
+                s->tuneDelta = d;
+                s->tuneWpb = w;
+                s->nMidSlots = m;
+                launch_forces(s);  // warm-up of this configuration
+                cudaEventRecord(e0, st);
+                for (int r = 0; r < reps; ++r) launch_forces(s);
+                cudaEventRecord(e1, st);
+                cudaError_t err = cudaEventSynchronize(e1);
+                if (err != cudaSuccess) {
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    return cssg_cuda_fail(err, "cssg_system_autotune");
+                }
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                int bits = 0;
+                cudaMemcpy(&bits, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost);
+                cudaMemset(s->statusBits, 0, sizeof(int));
+                if (bits == 0 && ms < best) {
+                    best = ms;
+                    bd = d;
+                    bw = w;
+                    bm = m;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    s->timing = timing;
+    s->tuneDelta = bd;
+    s->tuneWpb = bw;
+    s->nMidSlots = bm;
+    drop_graph(s);
+    // leave the forces of the current state computed with the chosen configuration
+    launch_forces(s);
+    CSSG_CUDA(cudaStreamSynchronize(st));
+    if (prior) {
+        int bits = 0;
+        CSSG_CUDA(cudaMemcpy(&bits, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost));
+        bits |= prior;
+        CSSG_CUDA(cudaMemcpy(s->statusBits, &bits, sizeof(int), cudaMemcpyHostToDevice));
+    }
+    CSSG_CUDA(cudaGetLastError());
+    if (result_host) {
+        result_host[0] = bd;
+        result_host[1] = bw;
+        result_host[2] = bm;
+        result_host[3] = best / reps;
+    }
     return CSSG_OK;
 }
 

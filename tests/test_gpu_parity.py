@@ -218,3 +218,22 @@ def test_batched_systems_match_oracle(gpu, oracle_mod):
         pe = np.linalg.norm(OM.r3(fg[a:e], bg[a:e]) - OM.r3(fo, bo), axis=1)
         assert pe.max() < 1e-8, (k, pe.max())
         np.testing.assert_allclose(vg[a:e], vo, atol=1e-8)
+
+
+def test_autotune_keeps_results(gpu, oracle_mod):
+    """The autotuner only changes the work order: forces before and after tuning agree, and a forced extreme
+    tuning (narrow bands, small CTAs) still matches the oracle."""
+    api, ctx = gpu
+    V, F = ms.torus(60, 30, 3.0, 1.0)
+    n, sigma = 300, 0.45
+    S, f, b, _ = _system(api, ctx, V, F, n, 3, "nve", sigma, True, sigma, 1e-3, 0.0)
+    S.compute_forces()
+    f0 = S.get_state()[3]
+    tune = S.autotune(reps=1)
+    assert tune["delta_scale"] in (0.5, 1.0, 2.0, 4.0) and tune["warps_per_block"] in (4, 8)
+    f1 = S.get_state()[3]
+    np.testing.assert_allclose(f1, f0, rtol=0, atol=1e-12)
+    S.set_tuning(0.5, 4)
+    S.compute_forces()
+    assert S.check()[0] == 0
+    np.testing.assert_allclose(S.get_state()[3], f0, rtol=0, atol=1e-12)
