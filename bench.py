@@ -39,6 +39,9 @@ FLOPS_PER_WINDOW = 250          # FP64 flops of one window step (trim, target/ve
 BYTES_PER_SOURCE = 4 + 24 + 24 + 24   # read face, barycentrics, R3 position; write force
 BYTES_PER_CANDIDATE = 4 + 4 + 24 + 24  # read index, face, barycentrics, R3 position
 BYTES_PER_FACE = 12 + 12 + 72         # patch face: vertex ids, neighbours, edge frames
+# DRAM bytes (read + write) of one launch of the regular propagation pass, from a full ncu capture of that workload
+# (profiles/geodesic_kernel_torus200x100_N2000_nvt.txt); workloads without a capture report null
+TRAFFIC_BYTES = {"torus200x100_N2000_nvt_patch": 46_627_840 + 77_552_640}
 
 
 def workload_config(name):
@@ -370,7 +373,7 @@ def run_ours(args, cfg):
     fp64_peak = api.fp64_peak_gflops(ctx)
     achieved_gbs = geo_bytes / (geo_ms * 1e-3) / 1e9
     achieved_fp64 = geo_flops / (geo_ms * 1e-3) / 1e9
-    traffic = os.environ.get("CSSG_GEO_TRAFFIC_BYTES")
+    traffic = TRAFFIC_BYTES.get(cfg["workload"])
 
     # ---- e2e: host state in, step, host state out, every step ----
     pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()

@@ -704,8 +704,11 @@ __device__ __noinline__ bool settled(const DevMesh& M, const Slot& S, const GeoC
             double lab = bitsd(ldv(&S.vlab[h]));
             if (!(lab < CUDART_INF)) continue;
             const double* pv = &M.V[3 * v];
-            double u[3] = {P[0] - pv[0], P[1] - pv[1], P[2] - pv[2]};
-            b = fmin(b, lab + sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
+            // upper bound of the path through v (FP32 length rounded up with a 1e-6 margin): the early exit only
+            // needs upper bounds of the targets' distances
+            const float ux = (float)(P[0] - pv[0]), uy = (float)(P[1] - pv[1]), uz = (float)(P[2] - pv[2]);
+            const float l = sqrtf(ux * ux + uy * uy + uz * uz) * 1.000001f + 1e-30f;
+            b = fmin(b, lab + (double)l);
         }
         if (!(b <= minKey || minKey > src.cutoff)) ok = false;
     }
