@@ -302,18 +302,19 @@ class System:
         check(_lib.load().cssg_system_screen_counters(self.h, _np_ptr(out)), "cssg_system_screen_counters")
         return {"pairs": int(out[0]), "screened": int(out[1]), "tc_errors": int(out[2])}
 
-    def set_tuning(self, delta_scale: float = 1.0, warps_per_block: int = 8, mid_slots: int = 0):
-        """Band width scale, CTA size (warps) and medium-pass slots of the propagation passes."""
-        check(_lib.load().cssg_system_set_tuning(self.h, float(delta_scale), int(warps_per_block), int(mid_slots)),
-              "cssg_system_set_tuning")
+    def set_tuning(self, delta_scale: float = 1.0, warps_per_block: int = 8, mid_slots: int = 0,
+                   warps_per_sm: int = 0, lpt_order: bool = False):
+        """Band width scale, CTA size (warps), medium-pass slots, per-SM warp cap and longest-first source order."""
+        check(_lib.load().cssg_system_set_tuning(self.h, float(delta_scale), int(warps_per_block), int(mid_slots),
+                                                 int(warps_per_sm), int(bool(lpt_order))), "cssg_system_set_tuning")
 
     def autotune(self, reps: int = 3):
         """Pick the fastest tuning on the current state (cssg_system_autotune); returns it with its time."""
-        out = np.zeros(4)
+        out = np.zeros(6)
         with self.ctx.use():
             check(_lib.load().cssg_system_autotune(self.h, int(reps), _np_ptr(out)), "cssg_system_autotune")
         return {"delta_scale": float(out[0]), "warps_per_block": int(out[1]), "mid_slots": int(out[2]),
-                "ms_per_force_pass": float(out[3])}
+                "warps_per_sm": int(out[3]), "lpt_order": bool(out[4]), "ms_per_force_pass": float(out[5])}
 
     def timing(self, enable: bool):
         check(_lib.load().cssg_system_timing(self.h, int(bool(enable))), "cssg_system_timing")

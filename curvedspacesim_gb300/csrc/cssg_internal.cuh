@@ -144,6 +144,8 @@ struct GeoLaunch {
     int routeBig;                // 1: sources of systems marked bigBin go straight to failList (first pass only)
     double deltaScale;           // band width = deltaScale * the system's delta (<= 0: 1)
     int wpbMax;                  // largest warps per block (CTA size / 32; <= 0: 8)
+    int warpsPerSM;              // > 0: at most this many source warps per SM (the rest of the slots stay idle)
+    int* srcCost;                // nullable: work of each source (windows + launches + rounds), for the next order
     int smemTables;              // set by cssg_launch_geodesic: hash tables in shared memory
 };
 

@@ -824,6 +824,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
         return;
     }
     if (nT == 0) {
+        if (Lp.srcCost && lane == 0) Lp.srcCost[si] = 1;
         if (Lp.force && lane == 0) {
             Lp.force[3 * si] = Lp.force[3 * si + 1] = Lp.force[3 * si + 2] = 0;
         }
@@ -1212,6 +1213,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     inRange = warp_sum_i(inRange);
     processed = warp_sum_i(processed);
     launches = warp_sum_i(launches);
+    if (lane == 0 && Lp.srcCost) Lp.srcCost[si] = processed + launches + 8 * round + 1;
     if (lane == 0 && Lp.stats) {
         Lp.stats[4 * si] = processed;
         Lp.stats[4 * si + 1] = launches;
@@ -1438,6 +1440,7 @@ void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
     int dev = 0, sms = 1, bps = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (L.warpsPerSM > 0) L.nSlots = std::min<long long>(L.nSlots, (long long)sms * L.warpsPerSM);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, geodesic_kernel, 32 * wpb, smem);
     bps = std::max(bps, 1);
     const long long full = (long long)sms * bps;

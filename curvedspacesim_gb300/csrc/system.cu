@@ -370,6 +370,11 @@ struct cssg_system {
     // tuning (cssg_system_autotune / cssg_system_set_tuning): band width scale, warps per block, medium-pass slots
     double tuneDelta = 1.0;
     int tuneWpb = 8;
+    int tuneWarpsPerSM = 0;  // 0: every slot
+    bool tuneLpt = false;    // sources in decreasing order of their last cost (longest first) instead of cell order
+    int* srcCost = nullptr;  // n: work of each source in the last force evaluation
+    int* lptOrder = nullptr; // n
+    int* lptBuckets = nullptr;  // 64: bucket counts, then cursors
     int midSlotsMax = 0;  // allocated medium slots; the launch uses nMidSlots <= midSlotsMax
     int maxWindows = 0, midMaxWindows = 0, bigMaxWindows = 0;  // per-source work caps of the three passes
     // timing
@@ -395,6 +400,45 @@ int record(cssg_system* s)
     int k = s->eventsUsed++;
     cudaEventRecord(s->events[k], s->ctx->stream);
     return k;
+}
+
+// ---- longest-processing-time-first order of the sources (by the last evaluation's cost) -----------------------
+__device__ __forceinline__ int cost_bucket(int c)
+{
+    // 32 buckets by log2(cost), largest cost first
+    const int lg = 31 - __clz(max(c, 1));
+    return 31 - min(31, lg);
+}
+
+__global__ void lpt_count(int n, const int* __restrict__ cost, int* __restrict__ buckets)
+{
+    __shared__ int local[32];
+    if (threadIdx.x < 32) local[threadIdx.x] = 0;
+    __syncthreads();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) atomicAdd(&local[cost_bucket(cost[i])], 1);
+    __syncthreads();
+    if (threadIdx.x < 32 && local[threadIdx.x]) atomicAdd(&buckets[threadIdx.x], local[threadIdx.x]);
+}
+
+__global__ void lpt_scan(int* buckets)
+{
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int b = 0; b < 32; ++b) {
+            buckets[32 + b] = acc;
+            acc += buckets[b];
+        }
+    }
+}
+
+__global__ void lpt_scatter(int n, const int* __restrict__ order, const int* __restrict__ cost, int* buckets,
+                            int* __restrict__ out)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int si = order ? order[k] : k;
+    out[atomicAdd(&buckets[32 + cost_bucket(cost[si])], 1)] = si;
 }
 
 // findNeighbors + computeForces into s->force
@@ -450,6 +494,15 @@ void launch_forces(cssg_system* s)
     L.routeBig = 1;
     L.deltaScale = s->tuneDelta;
     L.wpbMax = s->tuneWpb;
+    L.warpsPerSM = s->tuneWarpsPerSM;
+    L.srcCost = s->srcCost;
+    if (s->tuneLpt) {
+        cudaMemsetAsync(s->lptBuckets, 0, 64 * sizeof(int), st);
+        lpt_count<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->srcCost, s->lptBuckets);
+        lpt_scan<<<1, 32, 0, st>>>(s->lptBuckets);
+        lpt_scatter<<<(n + tb - 1) / tb, tb, 0, st>>>(n, L.order, s->srcCost, s->lptBuckets, s->lptOrder);
+        L.order = s->lptOrder;
+    }
     if (s->screen) {
         // learned screen: candidate rows -> CSR pairs -> features -> tensor-core MLP -> skip flags; the propagation
         // then reads the CSR (screened pairs keep their faces in the patch but are not queried)
@@ -485,6 +538,7 @@ void launch_forces(cssg_system* s)
     R.failList = s->failList2;
     R.failCount = s->work + 4;
     R.routeBig = 0;
+    R.warpsPerSM = 0;
     R.maxRounds = 1 << 15;
     R.maxWindows = s->midMaxWindows;
     cssg_launch_geodesic(R, st);
@@ -620,6 +674,10 @@ extern "C" int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh*
     TRY(alloc((void**)&s->work, sizeof(int) * 5));
     TRY(alloc((void**)&s->failList, sizeof(int) * n));
     TRY(alloc((void**)&s->failList2, sizeof(int) * n));
+    TRY(alloc((void**)&s->srcCost, sizeof(int) * n));
+    TRY(alloc((void**)&s->lptOrder, sizeof(int) * n));
+    TRY(alloc((void**)&s->lptBuckets, sizeof(int) * 64));
+    cudaMemset(s->srcCost, 0, sizeof(int) * n);
     TRY(alloc((void**)&s->ke, sizeof(double) * n));
     TRY(alloc((void**)&s->dPartBase, sizeof(int) * (K + 1)));
     cudaMemset(s->force, 0, sizeof(double) * 3 * n);
@@ -807,7 +865,7 @@ extern "C" int cssg_system_destroy(cssg_system* s)
     void* ptrs[] = {s->face, s->bary, s->vel, s->force, s->disp, s->pos, s->walkStatus, s->srcStatus,
                     s->statusBits, s->counters, s->cellOf, s->cellCount, s->cellStart, s->cellCursor, s->cellList,
                     s->slotOf, s->scanBlocks, s->scratch, s->midScratch, s->bigScratch, s->work, s->failList,
-                    s->failList2, s->pairD, s->pairT,
+                    s->failList2, s->srcCost, s->lptOrder, s->lptBuckets, s->pairD, s->pairT,
                     s->pairJ, s->pairCount, s->chains, s->ke, s->dsys, s->dmeshes, s->sysOf, s->dPartBase,
                     s->mlpParams, s->candJPad, s->candCount, s->maxChord, s->candOff, s->pairI, s->pairJc, s->X,
                     s->chordS, s->yhat, s->skip, s->candScanBlocks, s->mlpErr, s->screenCounters, s->dsysScreen};
@@ -932,15 +990,19 @@ void drop_graph(cssg_system* s)
 }
 }  // namespace
 
-extern "C" int cssg_system_set_tuning(cssg_system* s, double delta_scale, int warps_per_block, int mid_slots)
+extern "C" int cssg_system_set_tuning(cssg_system* s, double delta_scale, int warps_per_block, int mid_slots,
+                                      int warps_per_sm, int lpt_order)
 {
-    if (!s || !(delta_scale > 0) || warps_per_block < 1 || warps_per_block > 8) {
-        cssg_set_error("cssg_system_set_tuning: bad arguments (delta_scale > 0, 1 <= warps_per_block <= 8)");
+    if (!s || !(delta_scale > 0) || warps_per_block < 1 || warps_per_block > 8 || warps_per_sm < 0) {
+        cssg_set_error("cssg_system_set_tuning: bad arguments (delta_scale > 0, 1 <= warps_per_block <= 8, "
+                       "warps_per_sm >= 0)");
         return CSSG_ERR_ARG;
     }
     s->tuneDelta = delta_scale;
     s->tuneWpb = warps_per_block;
     if (mid_slots > 0) s->nMidSlots = std::min(mid_slots, s->midSlotsMax);
+    s->tuneWarpsPerSM = warps_per_sm;
+    s->tuneLpt = lpt_order != 0;
     drop_graph(s);
     return CSSG_OK;
 }
@@ -956,14 +1018,16 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     int sms = 0;
     CSSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->ctx->device));
     const double deltas[] = {0.5, 1.0, 2.0, 4.0};
-    const int wpbs[] = {4, 8};
+    // (warps per block, warps per SM cap, longest-first order)
+    const int shapes[][3] = {{8, 0, 0}, {4, 0, 0}, {8, 0, 1}, {8, 8, 1}, {8, 4, 1}};
     std::vector<int> mids{s->midSlotsMax};
     if (s->midSlotsMax > sms * 8) mids.push_back(sms * 8);
     cudaEvent_t e0, e1;
     CSSG_CUDA(cudaEventCreate(&e0));
     CSSG_CUDA(cudaEventCreate(&e1));
     double best = 1e300, bd = s->tuneDelta;
-    int bw = s->tuneWpb, bm = s->nMidSlots;
+    int bw = s->tuneWpb, bm = s->nMidSlots, bc = s->tuneWarpsPerSM;
+    bool bl = s->tuneLpt;
     const bool timing = s->timing;
     s->timing = false;
     // status bits raised before the call are kept; a candidate that raises any (a capacity overflow) is rejected
@@ -971,10 +1035,12 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     CSSG_CUDA(cudaMemcpyAsync(&prior, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost, st));
     CSSG_CUDA(cudaStreamSynchronize(st));
     for (double d : deltas)
-        for (int w : wpbs)
+        for (const auto& sh : shapes)
             for (int m : mids) {
                 s->tuneDelta = d;
-                s->tuneWpb = w;
+                s->tuneWpb = sh[0];
+                s->tuneWarpsPerSM = sh[1];
+                s->tuneLpt = sh[2] != 0;
                 s->nMidSlots = m;
                 launch_forces(s);  // warm-up of this configuration
                 cudaEventRecord(e0, st);
@@ -994,7 +1060,9 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
                 if (bits == 0 && ms < best) {
                     best = ms;
                     bd = d;
-                    bw = w;
+                    bw = sh[0];
+                    bc = sh[1];
+                    bl = sh[2] != 0;
                     bm = m;
                 }
             }
@@ -1003,6 +1071,8 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     s->timing = timing;
     s->tuneDelta = bd;
     s->tuneWpb = bw;
+    s->tuneWarpsPerSM = bc;
+    s->tuneLpt = bl;
     s->nMidSlots = bm;
     drop_graph(s);
     // leave the forces of the current state computed with the chosen configuration
@@ -1019,7 +1089,9 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
         result_host[0] = bd;
         result_host[1] = bw;
         result_host[2] = bm;
-        result_host[3] = best / reps;
+        result_host[3] = bc;
+        result_host[4] = bl ? 1 : 0;
+        result_host[5] = best / reps;
     }
     return CSSG_OK;
 }

@@ -233,7 +233,9 @@ def test_autotune_keeps_results(gpu, oracle_mod):
     assert tune["delta_scale"] in (0.5, 1.0, 2.0, 4.0) and tune["warps_per_block"] in (4, 8)
     f1 = S.get_state()[3]
     np.testing.assert_allclose(f1, f0, rtol=0, atol=1e-12)
-    S.set_tuning(0.5, 4)
-    S.compute_forces()
-    assert S.check()[0] == 0
-    np.testing.assert_allclose(S.get_state()[3], f0, rtol=0, atol=1e-12)
+    for args in ((0.5, 4, 0, 0, False), (2.0, 8, 0, 2, True), (1.0, 8, 0, 4, True)):
+        S.set_tuning(*args)
+        S.compute_forces()
+        S.compute_forces()  # the second evaluation uses the longest-first order built from the first
+        assert S.check()[0] == 0
+        np.testing.assert_allclose(S.get_state()[3], f0, rtol=0, atol=1e-12)
