@@ -25,7 +25,7 @@ EXPORTS = [
     "cssg_system_reset_thermostat", "cssg_system_kernels_per_step", "cssg_diag_fp64_peak",
     "cssg_system_create_batched", "cssg_mlp_param_count", "cssg_screen_features", "cssg_mlp_infer", "cssg_mlp_grad",
     "cssg_mlp_adam", "cssg_system_set_screen", "cssg_system_screen_counters", "cssg_distance_batch_noalloc",
-    "cssg_system_set_tuning", "cssg_system_autotune",
+    "cssg_system_set_tuning", "cssg_system_autotune", "cssg_system_fire", "cssg_system_stress",
 ]
 
 
@@ -43,6 +43,21 @@ class cssg_params(ctypes.Structure):
         ("temperature", ctypes.c_double),
         ("tau", ctypes.c_double),
         ("chain_length", ctypes.c_int),
+    ]
+
+
+class cssg_fire_params(ctypes.Structure):
+    _fields_ = [
+        ("maximum_iterations", ctypes.c_int),
+        ("alpha_start", ctypes.c_double),
+        ("dt_max", ctypes.c_double),
+        ("dt_min", ctypes.c_double),
+        ("dt_inc", ctypes.c_double),
+        ("dt_dec", ctypes.c_double),
+        ("alpha_dec", ctypes.c_double),
+        ("n_min", ctypes.c_int),
+        ("force_cutoff", ctypes.c_double),
+        ("alpha_min", ctypes.c_double),
     ]
 
 
@@ -92,6 +107,8 @@ def load(build_if_missing: bool = True):
     L.cssg_system_compute_forces.argtypes = [P]
     L.cssg_system_set_tuning.argtypes = [P, D, I, I, I, I]
     L.cssg_system_autotune.argtypes = [P, I, P]
+    L.cssg_system_fire.argtypes = [P, ctypes.POINTER(cssg_fire_params), I, P]
+    L.cssg_system_stress.argtypes = [P, P]
     L.cssg_system_check.argtypes = [P, P, P]
     L.cssg_system_pairs.argtypes = [P, I, P, P, P, P, P]
     L.cssg_system_chain.argtypes = [P, P, I]

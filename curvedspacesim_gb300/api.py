@@ -316,6 +316,27 @@ class System:
         return {"delta_scale": float(out[0]), "warps_per_block": int(out[1]), "mid_slots": int(out[2]),
                 "warps_per_sm": int(out[3]), "lpt_order": bool(out[4]), "ms_per_force_pass": float(out[5])}
 
+    def fire(self, maximum_iterations=1000, alpha_start=0.99, dt_max=0.1, dt_min=1e-5, dt_inc=1.1, dt_dec=0.95,
+             alpha_dec=0.9, n_min=4, force_cutoff=1e-12, alpha_min=0.0, reset=False):
+        """FIRE energy minimisation on the device (fireMinimization::minimizeByFire); defaults are the reference's
+        member defaults.  Returns iterations, forceMax and the persistent deltaT / alpha / nSinceNegativePower."""
+        p = _lib.cssg_fire_params(int(maximum_iterations), float(alpha_start), float(dt_max), float(dt_min),
+                                  float(dt_inc), float(dt_dec), float(alpha_dec), int(n_min), float(force_cutoff),
+                                  float(alpha_min))
+        out = np.zeros(5)
+        with self.ctx.use():
+            check(_lib.load().cssg_system_fire(self.h, ctypes.byref(p), int(bool(reset)), _np_ptr(out)),
+                  "cssg_system_fire")
+        return {"iterations": int(out[0]), "force_max": float(out[1]), "dt": float(out[2]), "alpha": float(out[3]),
+                "n_since_negative_power": int(out[4])}
+
+    def stress(self):
+        """simulation::computeMonodisperseStress on the current state: 3x3 array."""
+        out = np.zeros(9)
+        with self.ctx.use():
+            check(_lib.load().cssg_system_stress(self.h, _np_ptr(out)), "cssg_system_stress")
+        return out.reshape(3, 3)
+
     def timing(self, enable: bool):
         check(_lib.load().cssg_system_timing(self.h, int(bool(enable))), "cssg_system_timing")
 

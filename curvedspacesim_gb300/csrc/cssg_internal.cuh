@@ -58,7 +58,7 @@ int cssg_cuda_fail(cudaError_t e, const char* what);
 // meshes: device array of meshes; meshOf (nullable): per-particle index into it (null: all on meshes[0])
 void cssg_launch_transport(const DevMesh* meshes, const int* meshOf, int n, int* face, double* bary, double* disp,
                            double* transport, int nT, int* status, unsigned long long* crossings, double* pos_out,
-                           cudaStream_t s);
+                           cudaStream_t s, const int* skip = nullptr);
 void cssg_launch_positions(const DevMesh* meshes, const int* meshOf, int n, const int* face, const double* bary,
                            double* pos, cudaStream_t s);
 

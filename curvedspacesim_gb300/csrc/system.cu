@@ -16,6 +16,8 @@
 #include <cstring>
 #include <vector>
 
+#include <math_constants.h>
+
 #include "cssg_internal.cuh"
 
 namespace {
@@ -361,6 +363,11 @@ struct cssg_system {
     int nCandScanBlocks = 0;
     int* mlpErr = nullptr;
     unsigned long long* screenCounters = nullptr;  // [0] candidate pairs, [1] screened out
+    // FIRE minimisation (device state, transport buffer, reduction partials) and stress partials
+    void* fireState = nullptr;
+    double* fireTrans = nullptr;  // n x 2 x 3: force and velocity carried by the walk
+    double* firePartials = nullptr;
+    double* stressPartials = nullptr;
     // NVT
     double* chains = nullptr;
     double* ke = nullptr;
@@ -865,7 +872,8 @@ extern "C" int cssg_system_destroy(cssg_system* s)
     void* ptrs[] = {s->face, s->bary, s->vel, s->force, s->disp, s->pos, s->walkStatus, s->srcStatus,
                     s->statusBits, s->counters, s->cellOf, s->cellCount, s->cellStart, s->cellCursor, s->cellList,
                     s->slotOf, s->scanBlocks, s->scratch, s->midScratch, s->bigScratch, s->work, s->failList,
-                    s->failList2, s->srcCost, s->lptOrder, s->lptBuckets, s->pairD, s->pairT,
+                    s->failList2, s->srcCost, s->lptOrder, s->lptBuckets, s->fireState, s->fireTrans,
+                    s->firePartials, s->stressPartials, s->pairD, s->pairT,
                     s->pairJ, s->pairCount, s->chains, s->ke, s->dsys, s->dmeshes, s->sysOf, s->dPartBase,
                     s->mlpParams, s->candJPad, s->candCount, s->maxChord, s->candOff, s->pairI, s->pairJc, s->X,
                     s->chordS, s->yhat, s->skip, s->candScanBlocks, s->mlpErr, s->screenCounters, s->dsysScreen};
@@ -1277,5 +1285,358 @@ extern "C" int cssg_system_last_times(cssg_system* s, double* ms, int capacity)
     }
     ms[0] = geo;
     ms[1] = walk;
+    return CSSG_OK;
+}
+
+
+// ---------------------------------------------------------------------------------------------------------------------
+// FIRE minimisation: fireMinimization::minimizeByFire (src/updaters/fireMinimization.cpp:3-21) on the device.  One
+// iteration = velocity-Verlet half step, walk with force and velocity transported (simpleModel::moveParticles with both
+// transport flags, force first), forces, second half step, fireStep (:38-77), getMaxForce (baseUpdater.cpp:39-54).
+// The scalar state (deltaT, alpha, nSinceNegativePower, iteration count, stop flag) lives on the device, so a chunk of
+// iterations is one graph replay; every kernel that changes state returns at once when the stop flag is set, and the
+// host reads the flag once per chunk.
+// ---------------------------------------------------------------------------------------------------------------------
+namespace {
+
+struct FireState {
+    double dt, alpha, mixAlpha, mixScale, forceMax;
+    double alphaStart, dtMax, dtMin, dtInc, dtDec, alphaDec, forceCutoff, alphaMin;
+    int nMin, maxIterations, nSince, iterations, done, resetV;
+};
+
+constexpr int kFireBlock = 256;
+constexpr int kFireChunk = 16;
+
+__global__ void fire_first_half(int n, double* __restrict__ v, const double* __restrict__ f, double* __restrict__ disp,
+                                double* __restrict__ trans, const FireState* __restrict__ st)
+{
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double dt = st->dt;
+    for (int c = 0; c < 3; ++c) {
+        const int k = 3 * i + c;
+        disp[k] = dt * v[k] + 0.5 * dt * dt * f[k];
+        v[k] += 0.5 * dt * f[k];
+        trans[6 * i + c] = f[k];
+        trans[6 * i + 3 + c] = v[k];
+    }
+}
+
+__global__ void fire_unpack(int n, const double* __restrict__ trans, double* __restrict__ v, const FireState* st)
+{
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int c = 0; c < 3; ++c) v[3 * i + c] = trans[6 * i + 3 + c];
+}
+
+// v += dt/2 f, then per-block partial sums of F.F, v.v, F.v (fixed order within a block)
+__global__ void __launch_bounds__(kFireBlock) fire_second_half(int n, double* __restrict__ v,
+                                                               const double* __restrict__ f, const FireState* st,
+                                                               double* __restrict__ partials)
+{
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double ff = 0, vv = 0, fv = 0;
+    if (i < n) {
+        const double dt = st->dt;
+        double a[3], b[3];
+        for (int c = 0; c < 3; ++c) {
+            v[3 * i + c] += 0.5 * dt * f[3 * i + c];
+            a[c] = f[3 * i + c];
+            b[c] = v[3 * i + c];
+        }
+        ff = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+        vv = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+        fv = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+    }
+    __shared__ double sh[3][kFireBlock];
+    sh[0][threadIdx.x] = ff;
+    sh[1][threadIdx.x] = vv;
+    sh[2][threadIdx.x] = fv;
+    __syncthreads();
+    for (int w = kFireBlock / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int k = 0; k < 3; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 3; ++k) partials[3 * blockIdx.x + k] = sh[k][0];
+}
+
+// fireStep's scalar part: scaling from the norms, then the deltaT / alpha update on the sign of the power
+__global__ void fire_scalar(int nBlocks, const double* __restrict__ partials, FireState* st)
+{
+    if (st->done || threadIdx.x != 0) return;
+    double forceNorm = 0, velocityNorm = 0, power = 0;
+    for (int b = 0; b < nBlocks; ++b) {
+        forceNorm += partials[3 * b];
+        velocityNorm += partials[3 * b + 1];
+        power += partials[3 * b + 2];
+    }
+    double scaling = 0.0;
+    if (forceNorm > 0) scaling = sqrt(velocityNorm / forceNorm);
+    st->mixAlpha = st->alpha;
+    st->mixScale = scaling;
+    if (power > 0) {
+        if (st->nSince > st->nMin) {
+            st->dt = fmin(st->dt * st->dtInc, st->dtMax);
+            st->alpha = fmax(st->alpha * st->alphaDec, st->alphaMin);
+        }
+        st->nSince += 1;
+        st->resetV = 0;
+    } else {
+        st->nSince = 0;
+        st->dt = fmax(st->dt * st->dtDec, st->dtMin);
+        st->alpha = st->alphaStart;
+        st->resetV = 1;
+    }
+}
+
+// v = (1 - alpha) v + alpha * scaling * F (zero after a non-positive power), then per-block max |F|^2
+__global__ void __launch_bounds__(kFireBlock) fire_mix(int n, double* __restrict__ v, const double* __restrict__ f,
+                                                       const FireState* st, double* __restrict__ partialMax)
+{
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double q = 0;
+    if (i < n) {
+        const double a = st->mixAlpha, as = st->mixAlpha * st->mixScale;
+        const bool reset = st->resetV != 0;
+        for (int c = 0; c < 3; ++c) {
+            const int k = 3 * i + c;
+            v[k] = reset ? 0.0 : (1 - a) * v[k] + as * f[k];
+        }
+        q = f[3 * i] * f[3 * i] + f[3 * i + 1] * f[3 * i + 1] + f[3 * i + 2] * f[3 * i + 2];
+    }
+    for (int o = 16; o > 0; o >>= 1) q = fmax(q, __shfl_xor_sync(0xffffffffu, q, o));
+    __shared__ double sh[kFireBlock / 32];
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = q;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0;
+        for (int w = 0; w < kFireBlock / 32; ++w) m = fmax(m, sh[w]);
+        partialMax[blockIdx.x] = m;
+    }
+}
+
+__global__ void __launch_bounds__(kFireBlock) fire_force_max(int n, const double* __restrict__ f,
+                                                             double* __restrict__ partialMax)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double q = 0;
+    if (i < n) q = f[3 * i] * f[3 * i] + f[3 * i + 1] * f[3 * i + 1] + f[3 * i + 2] * f[3 * i + 2];
+    for (int o = 16; o > 0; o >>= 1) q = fmax(q, __shfl_xor_sync(0xffffffffu, q, o));
+    __shared__ double sh[kFireBlock / 32];
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = q;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0;
+        for (int w = 0; w < kFireBlock / 32; ++w) m = fmax(m, sh[w]);
+        partialMax[blockIdx.x] = m;
+    }
+}
+
+// forceMax from the block maxima; `count` = 1 after an iteration (iterations += 1), 0 for the initial check
+__global__ void fire_check(int nBlocks, const double* __restrict__ partialMax, FireState* st, int count)
+{
+    if (threadIdx.x != 0) return;
+    if (count && st->done) return;
+    double m = 0;
+    for (int b = 0; b < nBlocks; ++b) m = fmax(m, partialMax[b]);
+    st->forceMax = sqrt(m);
+    if (count) st->iterations += 1;
+    if (!(st->iterations < st->maxIterations && st->forceMax > st->forceCutoff)) st->done = 1;
+}
+
+void fire_iteration(cssg_system* s, FireState* dst, int nBlocks)
+{
+    cudaStream_t st = s->ctx->stream;
+    const int n = s->n;
+    double* partials = s->firePartials;
+    double* partialMax = s->firePartials + 3 * nBlocks;
+    fire_first_half<<<nBlocks, kFireBlock, 0, st>>>(n, s->vel, s->force, s->disp, s->fireTrans, dst);
+    cssg_launch_transport(s->dmeshes, s->sysOf, n, s->face, s->bary, s->disp, s->fireTrans, 2, s->walkStatus,
+                          s->counters, s->pos, st, &dst->done);
+    status_or<<<(n + 255) / 256, 256, 0, st>>>(n, s->walkStatus, s->statusBits);
+    fire_unpack<<<nBlocks, kFireBlock, 0, st>>>(n, s->fireTrans, s->vel, dst);
+    launch_forces(s);
+    fire_second_half<<<nBlocks, kFireBlock, 0, st>>>(n, s->vel, s->force, dst, partials);
+    fire_scalar<<<1, 32, 0, st>>>(nBlocks, partials, dst);
+    fire_mix<<<nBlocks, kFireBlock, 0, st>>>(n, s->vel, s->force, dst, partialMax);
+    fire_check<<<1, 32, 0, st>>>(nBlocks, partialMax, dst, 1);
+}
+
+// stress partials per block: f(t, d) (x) t over every stored pair and, once per pair, v_i (x) v_i
+__global__ void __launch_bounds__(256) stress_partials(int n, int pairCap, const int* __restrict__ pairCount,
+                                                       const double* __restrict__ pairD,
+                                                       const double* __restrict__ pairT,
+                                                       const double* __restrict__ vel, const SysDesc* __restrict__ sys,
+                                                       double* __restrict__ partials, int* __restrict__ overflow)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc[18];
+    for (int k = 0; k < 18; ++k) acc[k] = 0;
+    if (i < n) {
+        const SysDesc& D = sys[0];
+        int cnt = pairCount[i];
+        if (cnt > pairCap) {
+            atomicExch(overflow, 1);
+            cnt = pairCap;
+        }
+        const double v[3] = {vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]};
+        for (int t = 0; t < cnt; ++t) {
+            const size_t o = (size_t)i * pairCap + t;
+            const double d = pairD[o];
+            const double ts[3] = {pairT[3 * o], pairT[3 * o + 1], pairT[3 * o + 2]};
+            double f3[3] = {0, 0, 0};
+            if (d < CUDART_INF) {
+                double fm = 0;
+                bool use = true;
+                if (D.forceKind == 0) {
+                    use = d <= D.sigma;
+                    if (use) fm = -D.k * (D.sigma - d);
+                } else {
+                    const double sqrtTwoPi = 2.50662827463100050241576528481104525300698674061;
+                    fm = -(d * D.k * exp(-d * d / (2.0 * D.sigma * D.sigma)) / ((sqrtTwoPi * D.sigma) * sqrt(D.sigma)));
+                }
+                if (use)
+                    for (int c = 0; c < 3; ++c) f3[c] = fm * ts[c];
+            }
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    acc[3 * a + b] += f3[a] * ts[b];
+                    acc[9 + 3 * a + b] += v[a] * v[b];
+                }
+        }
+    }
+    __shared__ double sh[18][256];
+    for (int k = 0; k < 18; ++k) sh[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int k = 0; k < 18; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 18) partials[18 * blockIdx.x + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+}  // namespace
+
+extern "C" int cssg_system_fire(cssg_system* s, const cssg_fire_params* fp, int reset, double* result_host)
+{
+    if (!s || !fp || s->K != 1 || fp->maximum_iterations < 0) {
+        cssg_set_error("cssg_system_fire: bad arguments (one system per call object; maximum_iterations >= 0)");
+        return CSSG_ERR_ARG;
+    }
+    cudaStream_t st = s->ctx->stream;
+    const int n = s->n;
+    const int nBlocks = (n + kFireBlock - 1) / kFireBlock;
+    if (!s->fireState) {
+        if (int rc = alloc(&s->fireState, sizeof(FireState))) return rc;
+        if (int rc = alloc((void**)&s->fireTrans, sizeof(double) * 6 * (size_t)n)) return rc;
+        if (int rc = alloc((void**)&s->firePartials, sizeof(double) * 4 * (size_t)nBlocks)) return rc;
+        reset = 1;
+    }
+    FireState h;
+    FireState* dst = (FireState*)s->fireState;
+    if (reset) {
+        memset(&h, 0, sizeof(h));
+        h.dt = s->P.dt;
+        h.alpha = fp->alpha_start;
+    } else {
+        CSSG_CUDA(cudaMemcpyAsync(&h, dst, sizeof(h), cudaMemcpyDeviceToHost, st));
+        CSSG_CUDA(cudaStreamSynchronize(st));
+    }
+    h.alphaStart = fp->alpha_start;
+    h.dtMax = fp->dt_max;
+    h.dtMin = fp->dt_min;
+    h.dtInc = fp->dt_inc;
+    h.dtDec = fp->dt_dec;
+    h.alphaDec = fp->alpha_dec;
+    h.forceCutoff = fp->force_cutoff;
+    h.alphaMin = fp->alpha_min;
+    h.nMin = fp->n_min;
+    h.maxIterations = fp->maximum_iterations;
+    h.iterations = 0;
+    h.done = 0;
+    CSSG_CUDA(cudaMemcpyAsync(dst, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+    // minimizeByFire: forces and forceMax before the loop
+    launch_forces(s);
+    fire_force_max<<<nBlocks, kFireBlock, 0, st>>>(n, s->force, s->firePartials + 3 * nBlocks);
+    fire_check<<<1, 32, 0, st>>>(nBlocks, s->firePartials + 3 * nBlocks, dst, 0);
+    // chunks of iterations as one graph; the stop flag is read after each chunk
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    CSSG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < kFireChunk; ++k) fire_iteration(s, dst, nBlocks);
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cssg_cuda_fail(e, "cssg_system_fire: graph capture");
+    const int maxChunks = fp->maximum_iterations / kFireChunk + 2;
+    int done = 0;
+    for (int c = 0; c < maxChunks; ++c) {
+        CSSG_CUDA(cudaMemcpyAsync(&done, &dst->done, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CSSG_CUDA(cudaStreamSynchronize(st));
+        if (done) break;
+        e = cudaGraphLaunch(ge, st);
+        if (e != cudaSuccess) {
+            cudaGraphExecDestroy(ge);
+            return cssg_cuda_fail(e, "cssg_system_fire: graph launch");
+        }
+    }
+    cudaGraphExecDestroy(ge);
+    CSSG_CUDA(cudaMemcpyAsync(&h, dst, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CSSG_CUDA(cudaStreamSynchronize(st));
+    CSSG_CUDA(cudaGetLastError());
+    if (result_host) {
+        result_host[0] = h.iterations;
+        result_host[1] = h.forceMax;
+        result_host[2] = h.dt;
+        result_host[3] = h.alpha;
+        result_host[4] = h.nSince;
+    }
+    return CSSG_OK;
+}
+
+extern "C" int cssg_system_stress(cssg_system* s, double* stress_host)
+{
+    if (!s || !stress_host || s->K != 1) {
+        cssg_set_error("cssg_system_stress: bad arguments (one system per call object)");
+        return CSSG_ERR_ARG;
+    }
+    cudaStream_t st = s->ctx->stream;
+    const int n = s->n;
+    const int nBlocks = (n + 255) / 256;
+    if (!s->pairD) {
+        int cnt = 0;
+        if (int rc = cssg_system_pairs(s, 0, nullptr, nullptr, nullptr, nullptr, &cnt)) return rc;
+    }
+    if (!s->stressPartials)
+        if (int rc = alloc((void**)&s->stressPartials, sizeof(double) * 18 * (size_t)nBlocks + 16)) return rc;
+    // simulation::computeMonodisperseStress calls findNeighbors on the current positions first
+    launch_forces(s);
+    int* overflow = (int*)(s->stressPartials + 18 * (size_t)nBlocks);
+    CSSG_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), st));
+    stress_partials<<<nBlocks, 256, 0, st>>>(n, s->pairCap, s->pairCount, s->pairD, s->pairT, s->vel, s->dsys,
+                                             s->stressPartials, overflow);
+    std::vector<double> part(18 * (size_t)nBlocks);
+    int ovf = 0;
+    CSSG_CUDA(cudaMemcpyAsync(part.data(), s->stressPartials, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, st));
+    CSSG_CUDA(cudaMemcpyAsync(&ovf, overflow, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CSSG_CUDA(cudaStreamSynchronize(st));
+    if (ovf) {
+        cssg_set_error("cssg_system_stress: a source has more candidate pairs than the pair buffer holds");
+        return CSSG_ERR_CAPACITY;
+    }
+    double acc[18] = {0};
+    for (int b = 0; b < nBlocks; ++b)
+        for (int k = 0; k < 18; ++k) acc[k] += part[18 * b + k];
+    const double area = s->meshes[0]->area;
+    const double density = n / area;
+    for (int k = 0; k < 9; ++k) stress_host[k] = density * 1.0 * acc[9 + k] / (2 * n) + acc[k] / (2 * 2 * area * n);
     return CSSG_OK;
 }

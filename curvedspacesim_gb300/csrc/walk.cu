@@ -371,8 +371,10 @@ __global__ void __launch_bounds__(128) transport_kernel(const DevMesh* __restric
                                                         int n, int* __restrict__ face,
                                                         double* __restrict__ bary, double* __restrict__ disp,
                                                         double* __restrict__ transport, int ntv, int* __restrict__ status,
-                                                        unsigned long long* crossings, double* __restrict__ posOut)
+                                                        unsigned long long* crossings, double* __restrict__ posOut,
+                                                        const int* __restrict__ skip)
 {
+    if (skip && *skip) return;  // a device-side stop flag (FIRE after convergence): nothing moves
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int cr = 0;
     if (i < n) {
@@ -422,12 +424,12 @@ __global__ void positions_kernel(const DevMesh* __restrict__ meshes, const int* 
 
 void cssg_launch_transport(const DevMesh* meshes, const int* meshOf, int n, int* face, double* bary, double* disp,
                            double* transport, int nT, int* status, unsigned long long* crossings, double* pos_out,
-                           cudaStream_t s)
+                           cudaStream_t s, const int* skip)
 {
     if (n <= 0) return;
     int threads = 128;
     transport_kernel<<<(n + threads - 1) / threads, threads, 0, s>>>(meshes, meshOf, n, face, bary, disp, transport, nT,
-                                                                     status, crossings, pos_out);
+                                                                     status, crossings, pos_out, skip);
 }
 
 void cssg_launch_positions(const DevMesh* meshes, const int* meshOf, int n, const int* face, const double* bary,

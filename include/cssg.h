@@ -149,6 +149,28 @@ int cssg_system_step(cssg_system* sys, int steps, int use_graph);
 /* simulation::computeForces (simulation.cpp:61-70 -> baseForce.cpp:12-28): neighbours, geodesics, forces. */
 int cssg_system_compute_forces(cssg_system* sys);
 
+/* ---- FIRE minimisation: fireMinimization::minimizeByFire (src/updaters/fireMinimization.cpp:3-21) ------------------
+ * Replaces the reference's performUpdate of a fireMinimization updater: forces, then until forceMax <= force_cutoff
+ * or maximum_iterations: velocity-Verlet half steps (velocityVerletNVE.cpp:14-29) with force and velocity carried by
+ * the walk (simpleModel.cpp:44-66), fireStep (fireMinimization.cpp:38-77), getMaxForce (baseUpdater.cpp:39-54).
+ * Fields as setFIREParameters (:79-96).  The initial deltaT is the system's dt (the reference's setFIREParameters
+ * does not apply its _deltaT argument either).  deltaT, alpha and nSinceNegativePower persist between calls like the
+ * reference's members; reset = 1 (or the first call) restarts them at (dt, alpha_start, 0).  One system per object.
+ * result_host (nullable, 5 doubles) = {iterations, forceMax, deltaT, alpha, nSinceNegativePower}.  Synchronises. */
+typedef struct cssg_fire_params {
+    int maximum_iterations;
+    double alpha_start, dt_max, dt_min, dt_inc, dt_dec, alpha_dec;
+    int n_min;
+    double force_cutoff, alpha_min;
+} cssg_fire_params;
+int cssg_system_fire(cssg_system* sys, const cssg_fire_params* params, int reset, double* result_host);
+
+/* simulation::computeMonodisperseStress (src/simulation/simulation.cpp:104-173): recomputes the neighbour pairs on the
+ * current positions and returns stress_host[9] (row-major 3x3) = rho <v (x) v> / (2N) + <f_ij (x) t_ij> / (4 A N),
+ * rho = N / A, kB = 1; like the reference, v_i (x) v_i is summed once per neighbour pair of i.  Enables pair output.
+ * One system per object; CSSG_ERR_CAPACITY if a source has more candidates than the pair buffer.  Synchronises. */
+int cssg_system_stress(cssg_system* sys, double* stress_host);
+
 /* Tuning of the propagation passes (no reference counterpart).  delta_scale: band width of the distance-banded
  * rounds in units of each mesh's mean edge length (default 1); warps_per_block: CTA size / 32 of the persistent
  * launches (1..8, default 8; the grid always covers every SM equally); mid_slots: warps of the medium-tier pass

@@ -57,6 +57,9 @@ def lib():
         L.oracle_simulate.argtypes = [P, I, I, I, P, P, P, P, P, P, I, P]
         L.oracle_nvt_init.argtypes = [I, D, D, I, P]
         L.oracle_set_order.argtypes = [I, D, I]
+        L.oracle_fire.restype = I
+        L.oracle_fire.argtypes = [P, I, P, P, P, P, P, P, P, I, P]
+        L.oracle_stress.argtypes = [P, I, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -215,6 +218,31 @@ class OracleMesh:
         err = lib().oracle_simulate(self.h, int(kind), int(steps), len(face), _p(face), _p(bary), _p(vel), _p(force),
                                     _p(params), _p(chain), int(threads), _p(stats))
         return face, bary, vel, force, chain, err, stats
+
+    def fire(self, face, bary, vel, force, params, maximum_iterations=1000, alpha_start=0.99, dt_max=0.1, dt_min=1e-5,
+             dt_inc=1.1, dt_dec=0.95, alpha_dec=0.9, n_min=4, force_cutoff=1e-12, alpha_min=0.0, state=None,
+             threads=0):
+        """fireMinimization::minimizeByFire; state = [deltaT, alpha, nSinceNegativePower] (default: params' dt,
+        alpha_start, 0).  Returns (face, bary, vel, force, state, iterations, forceMax, err)."""
+        face = np.array(face, dtype=np.int32, copy=True)
+        bary = np.array(bary, dtype=np.float64, copy=True)
+        vel = np.array(vel, dtype=np.float64, copy=True)
+        force = np.array(force, dtype=np.float64, copy=True)
+        fire = np.array([maximum_iterations, alpha_start, dt_max, dt_min, dt_inc, dt_dec, alpha_dec, n_min,
+                         force_cutoff, alpha_min], dtype=np.float64)
+        st = np.array(state if state is not None else [params[7], alpha_start, 0], dtype=np.float64)
+        out = np.zeros(2)
+        err = lib().oracle_fire(self.h, len(face), _p(face), _p(bary), _p(vel), _p(force), _p(params), _p(fire),
+                                _p(st), int(threads), _p(out))
+        return face, bary, vel, force, st, int(out[0]), float(out[1]), err
+
+    def stress(self, face, bary, vel, params):
+        face = np.ascontiguousarray(face, dtype=np.int32)
+        bary = np.ascontiguousarray(bary, dtype=np.float64)
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        out = np.zeros(9)
+        lib().oracle_stress(self.h, len(face), _p(face), _p(bary), _p(vel), _p(params), _p(out))
+        return out.reshape(3, 3)
 
     @staticmethod
     def nvt_chain(n, params):

@@ -1863,6 +1863,162 @@ int oracle_simulate(void* m, int kind, int steps, int n, int* face, double* bary
     return err;
 }
 
+// fireMinimization::minimizeByFire (src/updaters/fireMinimization.cpp:3-21): forces, then velocity-Verlet half
+// steps (velocityVerletNVE.cpp:14-29) with the force and the velocity transported by the walk (simpleModel.cpp:44-66:
+// force first, then velocity, because fireMinimization::setModel sets both transport flags), fireStep (:38-77) and
+// getMaxForce (src/updaters/baseUpdater.cpp:39-54) until forceMax <= forceCutoff or maximumIterations.
+//   fire : maximumIterations, alphaStart, deltaTMax, deltaTMin, deltaTInc, deltaTDec, alphaDec, nMin, forceCutoff,
+//          alphaMin
+//   state: deltaT, alpha, nSinceNegativePower (in/out: the reference keeps them as members between calls)
+//   out  : iterations, forceMax
+int oracle_fire(void* m, int n, int* face, double* bary, double* vel, double* force, const double* params,
+                const double* fire, double* state, int nThreads, double* out)
+{
+    Mesh* M = (Mesh*)m;
+    SysParams P{(int)params[0], params[1], params[2], params[3], (int)params[4], params[5], params[6]};
+    const int maxIt = (int)fire[0];
+    const double alphaStart = fire[1], dtMax = fire[2], dtMin = fire[3], dtInc = fire[4], dtDec = fire[5];
+    const double alphaDec = fire[6], cutoff = fire[8], alphaMin = fire[9];
+    const int nMin = (int)fire[7];
+    double dt = state[0], alpha = state[1];
+    int nSince = (int)state[2];
+    std::vector<double> disp(3 * n), tv(6 * (size_t)n);
+    long long inr = 0;
+    GeoStats st;
+    int err = 0;
+    auto maxForce = [&]() {
+        double mx = 0;
+        for (int i = 0; i < n; ++i) {
+            double q = force[3 * i] * force[3 * i] + force[3 * i + 1] * force[3 * i + 1] + force[3 * i + 2] * force[3 * i + 2];
+            if (q > mx) mx = q;
+        }
+        return std::sqrt(mx);
+    };
+    auto dot = [&](const double* a, const double* b) {
+        double acc = 0;
+        for (int i = 0; i < n; ++i) acc += a[3 * i] * b[3 * i] + a[3 * i + 1] * b[3 * i + 1] + a[3 * i + 2] * b[3 * i + 2];
+        return acc;
+    };
+    compute_forces(*M, P, n, face, bary, force, nullptr, nThreads, &inr, &st);
+    double fmax = maxForce();
+    int it = 0;
+    while (it < maxIt && fmax > cutoff) {
+        it += 1;
+        for (int i = 0; i < 3 * n; ++i) {
+            disp[i] = dt * vel[i] + 0.5 * dt * dt * force[i];
+            vel[i] += 0.5 * dt * force[i];
+        }
+        for (int i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c) {
+                tv[6 * i + c] = force[3 * i + c];
+                tv[6 * i + 3 + c] = vel[3 * i + c];
+            }
+#pragma omp parallel for schedule(static) reduction(| : err)
+        for (int i = 0; i < n; ++i) {
+            int s2 = transport_one(*M, face[i], &bary[3 * i], &disp[3 * i], &tv[6 * i], 2, 100000, nullptr);
+            if (s2) err |= (1 << s2);
+        }
+        for (int i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c) {
+                force[3 * i + c] = tv[6 * i + c];
+                vel[3 * i + c] = tv[6 * i + 3 + c];
+            }
+        compute_forces(*M, P, n, face, bary, force, nullptr, nThreads, &inr, &st);
+        for (int i = 0; i < 3 * n; ++i) vel[i] += 0.5 * dt * force[i];
+        // fireStep
+        const double forceNorm = dot(force, force), velocityNorm = dot(vel, vel), power = dot(force, vel);
+        double scaling = 0.0;
+        if (forceNorm > 0) scaling = std::sqrt(velocityNorm / forceNorm);
+        for (int i = 0; i < 3 * n; ++i) vel[i] = (1 - alpha) * vel[i] + alpha * scaling * force[i];
+        if (power > 0) {
+            if (nSince > nMin) {
+                dt = std::min(dt * dtInc, dtMax);
+                alpha = alpha * alphaDec;
+                alpha = std::max(alpha, alphaMin);
+            }
+            nSince += 1;
+        } else {
+            nSince = 0;
+            dt = dt * dtDec;
+            dt = std::max(dt, dtMin);
+            alpha = alphaStart;
+            for (int i = 0; i < 3 * n; ++i) vel[i] = 0.0;
+        }
+        fmax = maxForce();
+    }
+    state[0] = dt;
+    state[1] = alpha;
+    state[2] = nSince;
+    out[0] = it;
+    out[1] = fmax;
+    return err;
+}
+
+// simulation::computeMonodisperseStress (src/simulation/simulation.cpp:104-173) for one force computer: sums
+// f(t_ij, d_ij) (x) t_ij over every neighbour pair and, as the reference does inside the same pair loop, v_i (x) v_i
+// once per neighbour pair; stress = rho v(x)v / (2N) + f(x)t / (2 * 2 * area * N) with rho = N / area, kB = 1.
+void oracle_stress(void* m, int n, const int* face, const double* bary, const double* vel, const double* params,
+                   double* stress)
+{
+    Mesh* M = (Mesh*)m;
+    SysParams P{(int)params[0], params[1], params[2], params[3], (int)params[4], params[5], params[6]};
+    std::vector<int> off(n + 1);
+    long long cap = (long long)n * 64 + 1024;
+    std::vector<int> idx;
+    std::vector<double> mc(n);
+    long long tot;
+    while (true) {
+        idx.resize(cap);
+        tot = oracle_candidates((void*)M, n, face, bary, P.range, off.data(), idx.data(), cap, mc.data());
+        if (tot >= 0) break;
+        cap = -tot;
+    }
+    double fdr[9] = {0}, vv[9] = {0};
+    GeoWork W;
+    GeoStats st;
+    std::vector<int> tf, faces;
+    std::vector<double> tb, d, ts;
+    for (int i = 0; i < n; ++i) {
+        int a = off[i], b = off[i + 1], nt = b - a;
+        if (nt == 0) continue;
+        tf.resize(nt);
+        tb.resize(3 * nt);
+        d.resize(nt);
+        ts.resize(3 * nt);
+        for (int q = 0; q < nt; ++q) {
+            int jj = idx[a + q];
+            tf[q] = face[jj];
+            for (int c = 0; c < 3; ++c) tb[3 * q + c] = bary[3 * jj + c];
+        }
+        const int* fs = nullptr;
+        int nfs = 0;
+        if (P.submesh) {
+            double r = P.maxDist;
+            if (mc[i] < P.maxDist) r = mc[i];
+            build_patch(*M, face[i], &bary[3 * i], tf.data(), nt, r, faces);
+            fs = faces.data();
+            nfs = (int)faces.size();
+        }
+        geodesic_one(*M, W, face[i], &bary[3 * i], nt, tf.data(), tb.data(), fs, nfs, P.cutoff, true, d.data(),
+                     ts.data(), nullptr, &st);
+        for (int q = 0; q < nt; ++q) {
+            double f3[3] = {0, 0, 0};
+            if (d[q] < kInf && (P.forceKind != 0 || d[q] <= P.sigma)) {
+                double fm = pair_force_mag(P, d[q]);
+                for (int c = 0; c < 3; ++c) f3[c] = fm * ts[3 * q + c];
+            }
+            for (int al = 0; al < 3; ++al)
+                for (int be = 0; be < 3; ++be) {
+                    fdr[3 * al + be] += f3[al] * ts[3 * q + be];
+                    vv[3 * al + be] += vel[3 * i + al] * vel[3 * i + be];
+                }
+        }
+    }
+    const double area = M->area;
+    const double density = n / area;
+    for (int k = 0; k < 9; ++k) stress[k] = density * 1.0 * vv[k] / (2 * n) + fdr[k] / (2 * 2 * area * n);
+}
+
 // noseHooverNVT::setBathVariables (noseHooverNVT.cpp:28-36): fills chain as used by oracle_simulate
 void oracle_nvt_init(int n, double T, double tau, int Mc, double* chain)
 {

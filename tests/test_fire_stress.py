@@ -1,0 +1,86 @@
+"""FIRE minimisation (fireMinimization::minimizeByFire) and the monodisperse stress (simulation::
+computeMonodisperseStress): the oracle's restatement on the CPU, the device path against it on the GPU."""
+import numpy as np
+import pytest
+
+from curvedspacesim_gb300 import meshes as ms
+
+
+def _setup(n=60, sigma=0.4, seed=4, T=0.0):
+    V, F = ms.icosphere(3)
+    rng = np.random.default_rng(seed)
+    f, b = ms.area_weighted_positions(V, F, n, rng)
+    vel = ms.tangent_velocities(V, F, f, T, rng) if T > 0 else np.zeros((n, 3))
+    return V, F, f, b, vel
+
+
+def test_oracle_fire_converges_and_stress_is_symmetric(oracle_mod):
+    V, F, f, b, vel = _setup()
+    OM = oracle_mod.OracleMesh(V, F)
+    prm = OM.params(0, k=1 / 0.16, sigma=0.4, rng=0.4, submesh=1, max_dist=0.4, cutoff=0.4, dt=0.01)
+    f0 = OM.forces(f, b, prm)[0]
+    fa, ba, va, fo, st, it, fmax, err = OM.fire(f, b, vel, np.zeros_like(vel), prm, maximum_iterations=400,
+                                               force_cutoff=1e-10)
+    assert err == 0
+    assert fmax <= 1e-10 and it < 400
+    assert np.max(np.linalg.norm(fo, axis=1)) == pytest.approx(fmax, rel=1e-12)
+    assert fmax < 1e-6 * np.max(np.linalg.norm(f0, axis=1))
+    # stress of an overlapping, moving configuration: symmetric (f_ij is parallel to t_ij), negative virial trace
+    V2, F2, f2, b2, v2 = _setup(n=80, seed=7, T=0.1)
+    OM2 = oracle_mod.OracleMesh(V2, F2)
+    s = OM2.stress(f2, b2, v2, prm)
+    np.testing.assert_allclose(s, s.T, atol=1e-15)
+    s0 = OM2.stress(f2, b2, np.zeros_like(v2), prm)
+    assert np.trace(s0) < 0
+
+
+@pytest.mark.gpu
+def test_fire_matches_oracle(gpu, oracle_mod):
+    """20 iterations step for step (sums differ only in order: tolerance 1e-9), then a full minimisation converges."""
+    api, ctx = gpu
+    V, F, f, b, vel = _setup()
+    n, sigma = len(f), 0.4
+    OM = oracle_mod.OracleMesh(V, F)
+    prm = OM.params(0, k=1 / sigma ** 2, sigma=sigma, rng=sigma, submesh=1, max_dist=sigma, cutoff=sigma, dt=0.01)
+    M = api.Mesh(V, F)
+    p = api.make_params("nve", "harmonic", k=1 / sigma ** 2, sigma=sigma, range_=sigma, submesh=True, max_dist=sigma,
+                        cutoff=sigma, dt=0.01)
+    S = api.System(ctx, M, n, p)
+    S.set_state(f, b, vel, np.zeros((n, 3)))
+    res = S.fire(maximum_iterations=20, force_cutoff=1e-300, reset=True)
+    fo, bo, vo, fco, st, it, fmax, err = OM.fire(f, b, vel, np.zeros((n, 3)), prm, maximum_iterations=20,
+                                                 force_cutoff=1e-300)
+    assert err == 0 and it == 20 and res["iterations"] == 20
+    bits, _ = S.check()
+    assert bits == 0
+    fg, bg, vg, fcg = S.get_state()
+    assert np.array_equal(fg, fo)
+    np.testing.assert_allclose(OM.r3(fg, bg), OM.r3(fo, bo), atol=1e-9)
+    np.testing.assert_allclose(vg, vo, atol=1e-9)
+    np.testing.assert_allclose(fcg, fco, atol=1e-9)
+    assert res["dt"] == pytest.approx(st[0], rel=1e-12) and res["alpha"] == pytest.approx(st[1], rel=1e-12)
+    assert res["n_since_negative_power"] == int(st[2])
+    assert res["force_max"] == pytest.approx(fmax, rel=1e-9)
+    # continue (state persists) until converged
+    res2 = S.fire(maximum_iterations=1000, force_cutoff=1e-10)
+    assert res2["force_max"] <= 1e-10 and res2["iterations"] < 1000
+    fcg2 = S.get_state()[3]
+    assert np.max(np.linalg.norm(fcg2, axis=1)) <= 1e-10
+
+
+@pytest.mark.gpu
+def test_stress_matches_oracle(gpu, oracle_mod):
+    api, ctx = gpu
+    V, F, f, b, vel = _setup(n=80, seed=7, T=0.1)
+    n, sigma = len(f), 0.4
+    OM = oracle_mod.OracleMesh(V, F)
+    for kind, k in ((0, 1 / sigma ** 2), (1, 0.5)):
+        prm = OM.params(kind, k=k, sigma=sigma, rng=sigma, submesh=1, max_dist=sigma, cutoff=sigma, dt=0.01)
+        M = api.Mesh(V, F)
+        p = api.make_params("nve", "harmonic" if kind == 0 else "gaussian", k=k, sigma=sigma, range_=sigma,
+                            submesh=True, max_dist=sigma, cutoff=sigma, dt=0.01)
+        S = api.System(ctx, M, n, p)
+        S.set_state(f, b, vel, np.zeros((n, 3)))
+        sg = S.stress()
+        so = OM.stress(f, b, vel, prm)
+        np.testing.assert_allclose(sg, so, rtol=1e-9, atol=1e-14)
