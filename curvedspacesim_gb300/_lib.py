@@ -26,6 +26,7 @@ EXPORTS = [
     "cssg_system_create_batched", "cssg_mlp_param_count", "cssg_screen_features", "cssg_mlp_infer", "cssg_mlp_grad",
     "cssg_mlp_adam", "cssg_system_set_screen", "cssg_system_screen_counters", "cssg_distance_batch_noalloc",
     "cssg_system_set_tuning", "cssg_system_autotune", "cssg_system_fire", "cssg_system_stress",
+    "cssg_mesh_set_boundary",
 ]
 
 
@@ -89,6 +90,7 @@ def load(build_if_missing: bool = True):
     L.cssg_mesh_create.argtypes = [P, I, P, I, I, PP]
     L.cssg_mesh_destroy.argtypes = [P]
     L.cssg_mesh_info.argtypes = [P, P, P, P, P]
+    L.cssg_mesh_set_boundary.argtypes = [P, I]
     L.cssg_ctx_create.argtypes = [I, P, PP]
     L.cssg_ctx_destroy.argtypes = [P]
     L.cssg_ctx_synchronize.argtypes = [P]

@@ -70,7 +70,11 @@ class Context:
 class Mesh:
     """cssg_mesh: the triangulated surface on the device (triangulatedMeshSpace::loadMeshFromFile)."""
 
-    def __init__(self, V, F, device: int = 0):
+    BOUNDARY = {"closed": 0, "tangential": 1, "absorbing": 2}
+
+    def __init__(self, V, F, device: int = 0, boundary="closed"):
+        """boundary: walk condition at border edges/vertices - "closed" (an error, triangulatedMeshSpace),
+        "tangential" (tangentialOpenMeshSpace) or "absorbing" (absorbingOpenMeshSpace)."""
         L = _lib.load()
         self.V = np.ascontiguousarray(V, dtype=np.float64)
         self.F = np.ascontiguousarray(F, dtype=np.int32)
@@ -85,6 +89,14 @@ class Mesh:
               "cssg_mesh_info")
         self.nV, self.nF, self.area = nv.value, nf.value, area.value
         self.bbox = (bbox[:3].copy(), bbox[3:].copy())
+        self.boundary = "closed"
+        if boundary != "closed":
+            self.set_boundary(boundary)
+
+    def set_boundary(self, boundary):
+        bc = self.BOUNDARY[boundary] if isinstance(boundary, str) else int(boundary)
+        check(_lib.load().cssg_mesh_set_boundary(self.h, bc), "cssg_mesh_set_boundary")
+        self.boundary = boundary
 
     def __del__(self):
         if getattr(self, "h", None) is not None and _lib._lib is not None:

@@ -23,9 +23,11 @@ struct DevMesh {
     const unsigned char* vflag; // bit0 closed ring available, bit1 border vertex, bit2 saddle (angle sum > 2 pi)
     const float* fcurv;         // 3 nF: per face mean curvature, Gaussian curvature, mean edge length (screen features)
     double bbMin[3], bbMax[3];
+    int bc;                     // walk boundary condition: 0 closed, 1 tangential, 2 absorbing (open meshes)
 };
 
 enum { VF_RING = 1, VF_BORDER = 2, VF_SADDLE = 4 };
+enum { BC_CLOSED = 0, BC_TANGENTIAL = 1, BC_ABSORBING = 2 };
 
 struct cssg_mesh {
     DevMesh d;

@@ -279,6 +279,7 @@ extern "C" int cssg_mesh_create(const double* V, int nV, const int* F, int nF, i
     d.vflag = dVF;
     d.fcurv = dFC;
     d.exitu = dEU;
+    d.bc = BC_CLOSED;
     {
         DevMesh* ds = nullptr;
         cudaError_t e = cudaMalloc((void**)&ds, sizeof(DevMesh));
@@ -301,6 +302,18 @@ extern "C" int cssg_mesh_destroy(cssg_mesh* m)
     for (void* b : m->buffers)
         if (b) cudaFree(b);
     delete m;
+    return CSSG_OK;
+}
+
+extern "C" int cssg_mesh_set_boundary(cssg_mesh* m, int bc)
+{
+    if (!m || bc < BC_CLOSED || bc > BC_ABSORBING) {
+        cssg_set_error("cssg_mesh_set_boundary: bad arguments (0 closed, 1 tangential, 2 absorbing)");
+        return CSSG_ERR_ARG;
+    }
+    m->d.bc = bc;
+    CSSG_CUDA(cudaSetDevice(m->device));
+    CSSG_CUDA(cudaMemcpy(&m->dself->bc, &bc, sizeof(int), cudaMemcpyHostToDevice));
     return CSSG_OK;
 }
 

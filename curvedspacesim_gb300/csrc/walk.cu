@@ -232,6 +232,80 @@ __device__ int face_across(const DevMesh& M, int f, int va, int vb)
     return -1;
 }
 
+__device__ __forceinline__ void normalize3(double* v)
+{
+    const double l = sqrt(dot3(v, v));
+    for (int c = 0; c < 3; ++c) v[c] = v[c] / l;
+}
+
+// triangulatedMeshSpace::projectVectorsIfOverBoundary (triangulatedMeshSpace.cpp:411-426) with
+// projectVectorOrthogonalToDirection (meshUtilities.cpp:125-129)
+__device__ void project_if_over_boundary(double (*tv)[3], int ntv, const double* orthogonal, const double* inward)
+{
+    const bool pointsOut = dot3(orthogonal, inward) < 0;
+    double dh[3] = {orthogonal[0], orthogonal[1], orthogonal[2]};
+    normalize3(dh);
+    for (int i = 0; i < ntv; ++i) {
+        const bool alongPerp = dot3(tv[i], orthogonal) > 0;
+        if ((pointsOut && alongPerp) || (!pointsOut && !alongPerp)) {
+            const double d = dot3(tv[i], dh);
+            for (int c = 0; c < 3; ++c) tv[i][c] = tv[i][c] - d * dh[c];
+        }
+    }
+}
+
+// openMeshSpace::getBoundaryVertexHeading (openMeshSpace.cpp:3-75) by its stated rule: the next heading runs along
+// the edge from v that overlaps most with the displacement, among the edges of v's faces other than the current one
+// (every (neighbour, face) pair, faces in increasing index order, first maximum kept; the reference's circulator
+// loop sees a subset that depends on CGAL's per-vertex halfedge).  Returns the new face or -1.
+__device__ int boundary_vertex_heading(const DevMesh& M, int v, int f, const double* disp, double* heading,
+                                       int* neighbour)
+{
+    double dn[3] = {disp[0], disp[1], disp[2]};
+    normalize3(dn);
+    double best = -1;
+    int bestFace = -1;
+    for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
+        const int g = M.vfList[i];
+        if (g == f) continue;
+        for (int k = 0; k < 3; ++k) {
+            const int w = M.F[3 * g + k];
+            if (w == v) continue;
+            double out[3] = {M.V[3 * w] - M.V[3 * v], M.V[3 * w + 1] - M.V[3 * v + 1], M.V[3 * w + 2] - M.V[3 * v + 2]};
+            normalize3(out);
+            const double ov = dot3(out, dn);
+            if (ov > best) {
+                best = ov;
+                bestFace = g;
+                *neighbour = w;
+                for (int c = 0; c < 3; ++c) heading[c] = out[c];
+            }
+        }
+    }
+    return bestFace;
+}
+
+// openMeshSpace::projectVectorsForBoundaryVertex (openMeshSpace.cpp:77-99)
+__device__ void project_for_boundary_vertex(const DevMesh& M, const double* heading, int v, int w,
+                                            const double* fNormal, int g, double (*tv)[3], int ntv)
+{
+    double orth[3];
+    cross3(fNormal, heading, orth);
+    normalize3(orth);
+    int inside = -1;
+    for (int k = 0; k < 3; ++k) {
+        const int u = M.F[3 * g + k];
+        if (u == v || u == w) continue;
+        inside = u;
+    }
+    double inward[3];
+    for (int c = 0; c < 3; ++c) inward[c] = (inside >= 0 ? M.V[3 * inside + c] : 0.0) - M.V[3 * v + c];
+    project_if_over_boundary(tv, ntv, orth, inward);
+}
+
+// With M.bc != BC_CLOSED, the loop of openMeshSpace::transportParticleAndVectors (openMeshSpace.cpp:101-238), which
+// differs only at border edges (updateAtBoundaryEdge) and border vertices (updateAtBoundaryVertex) of the
+// tangential (tangentialOpenMeshSpace.cpp) and absorbing (absorbingOpenMeshSpace.cpp) conditions.
 __device__ int transport_one(const DevMesh& M, int& face, double* bary, double* disp, double (*tv)[3], int ntv,
                              int maxIter, int* crossings, double* finalPos)
 {
@@ -292,7 +366,34 @@ __device__ int transport_one(const DevMesh& M, int& face, double* bary, double* 
         cross++;
         if (nhit == 2) {
             int v = inv0;  // the reference passes involvedVertex[0], the first vertex of the first edge hit
-            if (M.vflag[v] & VF_BORDER) return CSSG_ST_BORDER;
+            if (M.vflag[v] & VF_BORDER) {
+                if (M.bc == BC_CLOSED) return CSSG_ST_BORDER;
+                double heading[3];
+                int w = -1;
+                const int g = boundary_vertex_heading(M, v, f, disp, heading, &w);
+                if (g < 0) return CSSG_ST_VERTEX;
+                f = g;
+                load_face(M, f, P);
+                bary_of(P, &M.V[3 * v], sb);
+                if (ntv > 0) project_for_boundary_vertex(M, heading, v, w, ns, f, tv, ntv);
+                // the reference hands vertexPositions and sourceNormal to getBoundaryVertexHeading by value, so its
+                // caller keeps the previous face's; here they follow the new face
+                ld3(&M.N[3 * f], ns);
+                lastA = lastB = -1;
+                if (M.bc == BC_ABSORBING) {
+                    for (int c = 0; c < 3; ++c) tb[c] = sb[c];
+                    break;
+                }
+                double hh[3] = {heading[0], heading[1], heading[2]};  // projectVectorOntoDirection
+                normalize3(hh);
+                const double d2 = dot3(disp, hh);
+                construct_pt(P, sb, sp);
+                for (int c = 0; c < 3; ++c) {
+                    disp[c] = d2 * hh[c];
+                    target[c] = sp[c] + disp[c];
+                }
+                continue;
+            }
             int g = -1;
             double heading[3];
             int st = through_vertex(M, v, toI, f, &g, heading);
@@ -328,7 +429,41 @@ __device__ int transport_one(const DevMesh& M, int& face, double* bary, double* 
         }
         if (nhit != 1) return CSSG_ST_NO_INTERSECTION;
         int g = face_across(M, f, inv0, inv1);
-        if (g < 0) return CSSG_ST_BORDER;
+        if (g < 0) {
+            if (M.bc == BC_CLOSED) return CSSG_ST_BORDER;
+            // updateAtBoundaryEdge (tangentialOpenMeshSpace.cpp:3-39, absorbingOpenMeshSpace.cpp:2-26)
+            int inner = -1;
+            for (int k = 0; k < 3; ++k)
+                if (M.F[3 * f + k] != inv0 && M.F[3 * f + k] != inv1) inner = M.F[3 * f + k];
+            double edge[3], orth[3], inward[3], here[3];
+            for (int c = 0; c < 3; ++c) edge[c] = M.V[3 * inv1 + c] - M.V[3 * inv0 + c];
+            cross3(ns, edge, orth);
+            normalize3(orth);
+            construct_pt(P, sb, here);
+            for (int c = 0; c < 3; ++c) inward[c] = M.V[3 * inner + c] - here[c];
+            if (M.bc == BC_ABSORBING) {
+                if (ntv > 0) project_if_over_boundary(tv, ntv, orth, inward);
+                for (int c = 0; c < 3; ++c) tb[c] = sb[c];
+                break;
+            }
+            double fwd[3] = {edge[0], edge[1], edge[2]}, bwd[3];
+            for (int c = 0; c < 3; ++c) bwd[c] = M.V[3 * inv0 + c] - M.V[3 * inv1 + c];
+            normalize3(fwd);
+            normalize3(bwd);
+            double dn[3] = {disp[0], disp[1], disp[2]};
+            normalize3(dn);
+            const double fd = dot3(dn, fwd), bd = dot3(dn, bwd);
+            const double len = sqrt(dot3(disp, disp));  // the whole remaining displacement, measured before the edge
+            project_if_over_boundary(tv, ntv, orth, inward);
+            const bool stop = fd <= 0 && bd <= 0;
+            for (int c = 0; c < 3; ++c) {
+                disp[c] = fd > bd ? fd * len * fwd[c] : bd * len * bwd[c];
+                target[c] = here[c] + disp[c];
+            }
+            lastA = lastB = -1;
+            if (stop) break;  // the reference then writes the target weights found at the top of this pass
+            continue;
+        }
         construct_pt(P, ip, sp);
         double nt[3];
         ld3(&M.N[3 * g], nt);

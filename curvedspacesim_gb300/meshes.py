@@ -146,6 +146,42 @@ def prism(nsides: int, nz: int, radius: float = 1.0, height: float = 2.0):
     return np.array(V, dtype=np.float64), np.array(F, dtype=np.int32)
 
 
+def silo(nsides: int = 48, ncap: int = 12, nz: int = 24, radius: float = 2.0, height: float = 4.0):
+    """Open "silo": a hemispherical bowl of the given radius (pole at the bottom) continued by a cylinder of the
+    same radius up to z = height, open at the top rim (a border loop of nsides vertices)."""
+    V = [[0.0, 0.0, -radius]]
+    rings = []
+    for i in range(1, ncap + 1):  # hemisphere latitudes from the pole to the equator (z = 0)
+        th = 0.5 * np.pi * i / ncap
+        r, z = radius * math.sin(th), -radius * math.cos(th)
+        rings.append(len(V))
+        for s in range(nsides):
+            a = 2.0 * np.pi * (s + 0.5 * (i % 2)) / nsides
+            V.append([r * math.cos(a), r * math.sin(a), z])
+    for k in range(1, nz + 1):
+        z = height * k / nz
+        rings.append(len(V))
+        for s in range(nsides):
+            a = 2.0 * np.pi * (s + 0.5 * ((ncap + k) % 2)) / nsides
+            V.append([radius * math.cos(a), radius * math.sin(a), z])
+    F = []
+    r0 = rings[0]
+    for s in range(nsides):
+        F.append([0, r0 + (s + 1) % nsides, r0 + s])
+    for i in range(len(rings) - 1):
+        lo, hi = rings[i], rings[i + 1]
+        odd = (i + 1) % 2  # the upper ring is rotated by half a step when the lower one is not
+        for s in range(nsides):
+            a, b = lo + s, lo + (s + 1) % nsides
+            if odd:
+                c, d = hi + s, hi + (s + 1) % nsides
+                F += [[a, b, c], [b, d, c]]
+            else:
+                c, d = hi + (s - 1) % nsides, hi + s
+                F += [[a, d, c], [a, b, d]]
+    return np.array(V, dtype=np.float64), np.array(F, dtype=np.int32)
+
+
 def pyramid_cone(nsides: int, nrings: int, radius: float = 1.0, height: float = 1.0):
     """Open polygonal cone (apex + rings, no base): developable except at the apex (angle < 2*pi)."""
     V = [[0.0, 0.0, height]]

@@ -52,6 +52,14 @@ int cssg_mesh_destroy(cssg_mesh* mesh);
 /* area (triangulatedMeshSpace::getArea, :153), bbox_host[6] = min xyz, max xyz with the origin included (:6-30). */
 int cssg_mesh_info(const cssg_mesh* mesh, int* nV, int* nF, double* area, double* bbox_host);
 
+/* Boundary condition of walks on this mesh (the reference picks it by the space class): 0 closed
+ * (triangulatedMeshSpace: a border edge or vertex is the per-item error CSSG_ST_BORDER), 1 tangential
+ * (tangentialOpenMeshSpace.cpp: slide along the border, transported vectors that point out are projected), 2 absorbing
+ * (absorbingOpenMeshSpace.cpp: stop at the border).  Systems copy it when they are created.  At a border vertex the
+ * next border heading is the edge of the vertex's other faces that overlaps most with the displacement (the rule
+ * stated in openMeshSpace.cpp:35-37); the reference's candidate loop depends on CGAL internals and is not followed. */
+int cssg_mesh_set_boundary(cssg_mesh* mesh, int bc);
+
 /* ---- context ----------------------------------------------------------------------------------------------- */
 /* stream: a cudaStream_t, or NULL to create a private non-blocking stream. */
 int cssg_ctx_create(int device, void* stream, cssg_ctx** out);

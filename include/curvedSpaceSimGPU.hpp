@@ -93,7 +93,7 @@ struct devbuf {
 class closedMeshSpace {
 public:
     explicit closedMeshSpace(int device = 0) : device_(device) { throwIf(cssg_ctx_create(device, nullptr, &ctx_), "cssg_ctx_create"); }
-    ~closedMeshSpace()
+    virtual ~closedMeshSpace()
     {
         if (mesh_) cssg_mesh_destroy(mesh_);
         cssg_ctx_destroy(ctx_);
@@ -102,7 +102,7 @@ public:
     closedMeshSpace& operator=(const closedMeshSpace&) = delete;
 
     //! vertices (x,y,z per vertex) and counter-clockwise triangles
-    void loadMesh(const std::vector<double>& V, const std::vector<int>& F)
+    virtual void loadMesh(const std::vector<double>& V, const std::vector<int>& F)
     {
         if (mesh_) cssg_mesh_destroy(mesh_);
         mesh_ = nullptr;
@@ -281,6 +281,29 @@ private:
     double maximumDistance_ = 0;
 };
 
+//! openMeshSpace with tangential walls (tangentialOpenMeshSpace.cpp): walks slide along the border and transported
+//! vectors that point out of the surface are projected onto the wall.
+class tangentialOpenMeshSpace : public closedMeshSpace {
+public:
+    explicit tangentialOpenMeshSpace(int device = 0) : closedMeshSpace(device) {}
+    void loadMesh(const std::vector<double>& V, const std::vector<int>& F) override
+    {
+        closedMeshSpace::loadMesh(V, F);
+        throwIf(cssg_mesh_set_boundary(mesh(), 1), "cssg_mesh_set_boundary");
+    }
+};
+
+//! openMeshSpace with absorbing walls (absorbingOpenMeshSpace.cpp): a walk that reaches the border stops there.
+class absorbingOpenMeshSpace : public closedMeshSpace {
+public:
+    explicit absorbingOpenMeshSpace(int device = 0) : closedMeshSpace(device) {}
+    void loadMesh(const std::vector<double>& V, const std::vector<int>& F) override
+    {
+        closedMeshSpace::loadMesh(V, F);
+        throwIf(cssg_mesh_set_boundary(mesh(), 2), "cssg_mesh_set_boundary");
+    }
+};
+
 //! harmonicRepulsion: E = k/2 (sigma - d)^2 for d < sigma, F = -k (sigma - d) t for d <= sigma
 class harmonicRepulsion {
 public:
@@ -382,6 +405,31 @@ public:
     }
     cssg_system* handle() const { return sys_; }
 
+    //! fireMinimization::minimizeByFire on the device (fireMinimization.cpp:3-21); parameters as setFIREParameters
+    //! (:79-96), the initial deltaT is the simulation's dt.  Returns the iterations used; pulls the state.
+    int minimizeByFire(int maximumIterations = 1000, double alphaStart = 0.99, double deltaTMax = 0.1,
+                       double deltaTMin = 1e-5, double deltaTInc = 1.1, double deltaTDec = 0.95, double alphaDec = 0.9,
+                       int nMin = 4, double forceCutoff = 1e-12, double alphaMin = 0.0, bool reset = false)
+    {
+        cssg_fire_params fp{maximumIterations, alphaStart, deltaTMax, deltaTMin, deltaTInc, deltaTDec, alphaDec,
+                            nMin, forceCutoff, alphaMin};
+        double out[5];
+        throwIf(cssg_system_fire(sys_, &fp, reset ? 1 : 0, out), "cssg_system_fire");
+        checkItems();
+        pull();
+        forceMax = out[1];
+        return (int)out[0];
+    }
+    //! simulation::computeMonodisperseStress (simulation.cpp:104-173): stress[9], row-major
+    void computeMonodisperseStress(std::vector<double>& stress)
+    {
+        stress.resize(9);
+        throwIf(cssg_system_stress(sys_, stress.data()), "cssg_system_stress");
+    }
+    //! the library's autotuner (band width, CTA size, medium-pass slots, warp cap, source order) on this state
+    void autotune(int reps = 2) { throwIf(cssg_system_autotune(sys_, reps, nullptr), "cssg_system_autotune"); }
+
+    double forceMax = 0;
     closedMeshSpace& space_;
     int N;
     std::vector<meshPosition> positions;

@@ -60,6 +60,7 @@ def lib():
         L.oracle_fire.restype = I
         L.oracle_fire.argtypes = [P, I, P, P, P, P, P, P, P, I, P]
         L.oracle_stress.argtypes = [P, I, P, P, P, P, P]
+        L.oracle_set_boundary.argtypes = [I]
         _lib = L
     return _lib
 
@@ -72,6 +73,11 @@ def set_order(order: int = 0, delta: float = 0.0, bfs: bool = False):
     """Processing order of the oracle's propagation: 0 priority queue (default), 1 distance-banded rounds of width
     delta (the CUDA kernel's order; bfs=True drops the banding).  Results are identical; only the work differs."""
     lib().oracle_set_order(int(order), float(delta), int(bool(bfs)))
+
+
+def set_boundary(bc: int = 0):
+    """Boundary condition of the oracle's walks: 0 closed mesh, 1 tangential, 2 absorbing (open meshes)."""
+    lib().oracle_set_boundary(int(bc))
 
 
 class OracleMesh:

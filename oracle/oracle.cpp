@@ -409,8 +409,92 @@ int through_vertex(const Mesh& M, int v, const double* toInter, int srcFace, int
     return ST_OK;
 }
 
-// triangulatedMeshSpace::transportParticleAndVectors (triangulatedMeshSpace.cpp:448-564)
-int transport_one(const Mesh& M, int& face, double* bary, double* disp, double* tv, int ntv, int maxIter, int* crossings)
+// Open-mesh boundary conditions (src/models/openMeshSpace.cpp, tangentialOpenMeshSpace.cpp,
+// absorbingOpenMeshSpace.cpp).  0: closed mesh (a border is an error), 1: tangential, 2: absorbing.
+enum { BC_CLOSED = 0, BC_TANGENTIAL = 1, BC_ABSORBING = 2 };
+
+inline void normalize3(double* v)
+{
+    const double l = norm3(v);
+    for (int c = 0; c < 3; ++c) v[c] = v[c] / l;
+}
+
+// triangulatedMeshSpace::projectVectorsIfOverBoundary (triangulatedMeshSpace.cpp:411-426) with
+// projectVectorOrthogonalToDirection (meshUtilities.cpp:125-129)
+void project_if_over_boundary(double* tv, int ntv, const double* orthogonal, const double* inward)
+{
+    const bool pointsOut = dot3(orthogonal, inward) < 0;
+    double dh[3] = {orthogonal[0], orthogonal[1], orthogonal[2]};
+    normalize3(dh);
+    for (int i = 0; i < ntv; ++i) {
+        double* v = &tv[3 * i];
+        const bool alongPerp = dot3(v, orthogonal) > 0;
+        if ((pointsOut && alongPerp) || (!pointsOut && !alongPerp)) {
+            const double d = dot3(v, dh);
+            for (int c = 0; c < 3; ++c) v[c] = v[c] - d * dh[c];
+        }
+    }
+}
+
+// openMeshSpace::getBoundaryVertexHeading (openMeshSpace.cpp:3-75), by its stated rule: the next heading runs along
+// the edge from v that overlaps most with the displacement, among the edges of v's faces other than the current one.
+// The reference collects its (neighbour, face) candidates with a vertex circulator that advances once per face
+// compared, so which pairs it sees depends on CGAL's per-vertex halfedge choice; here every (neighbour, face) pair
+// around v is a candidate, faces in increasing index order, the first maximum kept.  Returns the new face and the
+// neighbour, or -1 (the reference's "New face not found").
+int boundary_vertex_heading(const Mesh& M, int v, int f, const double* disp, double* heading, int* neighbour)
+{
+    double dn[3] = {disp[0], disp[1], disp[2]};
+    normalize3(dn);
+    double best = -1;
+    int bestFace = -1;
+    for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
+        const int g = M.vfList[i];
+        if (g == f) continue;
+        for (int k = 0; k < 3; ++k) {
+            const int w = M.F[3 * g + k];
+            if (w == v) continue;
+            double out[3];
+            sub3(vp(M, w), vp(M, v), out);
+            normalize3(out);
+            const double ov = dot3(out, dn);
+            if (ov > best) {
+                best = ov;
+                bestFace = g;
+                *neighbour = w;
+                for (int c = 0; c < 3; ++c) heading[c] = out[c];
+            }
+        }
+    }
+    return bestFace;
+}
+
+// openMeshSpace::projectVectorsForBoundaryVertex (openMeshSpace.cpp:77-99)
+void project_for_boundary_vertex(const Mesh& M, const double* heading, int v, int w, const double* fNormal, int g,
+                                 double* tv, int ntv)
+{
+    double orth[3];
+    cross3(fNormal, heading, orth);
+    normalize3(orth);
+    int inside = -1;
+    for (int k = 0; k < 3; ++k) {
+        const int u = M.F[3 * g + k];
+        if (u == v || u == w) continue;
+        inside = u;
+    }
+    double inward[3] = {0, 0, 0};
+    if (inside >= 0) sub3(vp(M, inside), vp(M, v), inward);
+    else for (int c = 0; c < 3; ++c) inward[c] = -vp(M, v)[c];  // the reference's insideVertex stays (0,0,0)
+    project_if_over_boundary(tv, ntv, orth, inward);
+}
+
+int g_bc = BC_CLOSED;  // boundary condition used by the oracle's API entry points (oracle_set_boundary)
+
+// triangulatedMeshSpace::transportParticleAndVectors (triangulatedMeshSpace.cpp:448-564); with bc != 0 the loop of
+// openMeshSpace::transportParticleAndVectors (openMeshSpace.cpp:101-238), which differs only at border edges and
+// vertices
+int transport_one(const Mesh& M, int& face, double* bary, double* disp, double* tv, int ntv, int maxIter, int* crossings,
+                  int bc = BC_CLOSED)
 {
     int f = face;
     const double* p[3];
@@ -466,11 +550,40 @@ int transport_one(const Mesh& M, int& face, double* bary, double* disp, double* 
         for (int c = 0; c < 3; ++c) { sb[c] = ip[c]; sp[c] = ep[c]; }
         cross++;
         if (nhit == 2) {
-            cross += (1 << 16) - 1;  // vertex crossings are counted in the high half
             // vertex crossing (triangulatedMeshSpace.cpp:520-532, 566-611); like the reference, the vertex passed on
             // is the first vertex of the first edge that reported a hit
             int v = inv0;
-            if (M.borderV[v]) return ST_BORDER;
+            if (!M.borderV[v]) cross += (1 << 16) - 1;  // crossings of interior vertices are counted in the high half
+            if (M.borderV[v]) {
+                if (bc == BC_CLOSED) return ST_BORDER;
+                // updateAtBoundaryVertex (tangentialOpenMeshSpace.cpp:41-64, absorbingOpenMeshSpace.cpp:28-50)
+                double heading[3];
+                int w = -1;
+                const int g = boundary_vertex_heading(M, v, f, disp, heading, &w);
+                if (g < 0) return ST_VERTEX;
+                f = g;
+                face_pts(M, f, p);
+                bary_of(p[0], p[1], p[2], vp(M, v), sb);
+                if (ntv > 0) project_for_boundary_vertex(M, heading, v, w, ns, f, tv, ntv);
+                // the reference hands vertexPositions and sourceNormal to getBoundaryVertexHeading by value, so its
+                // caller keeps the previous face's; here they follow the new face
+                for (int c = 0; c < 3; ++c) ns[c] = M.N[3 * f + c];
+                lastA = lastB = -1;
+                if (bc == BC_ABSORBING) {
+                    for (int c = 0; c < 3; ++c) tb[c] = sb[c];
+                    break;
+                }
+                // projectVectorOntoDirection (meshUtilities.cpp:119-123)
+                double hh[3] = {heading[0], heading[1], heading[2]};
+                normalize3(hh);
+                const double d2 = dot3(disp, hh);
+                construct_pt(p[0], p[1], p[2], sb, sp);
+                for (int c = 0; c < 3; ++c) {
+                    disp[c] = d2 * hh[c];
+                    target[c] = sp[c] + disp[c];
+                }
+                continue;
+            }
             int g;
             double heading[3];
             int st = through_vertex(M, v, toI, f, &g, heading);
@@ -506,7 +619,41 @@ int transport_one(const Mesh& M, int& face, double* bary, double* disp, double* 
         if (nhit != 1) return ST_NO_INTERSECTION;
         // edge crossing (triangulatedMeshSpace.cpp:543-557, 614-658)
         int g = face_across(M, f, inv0, inv1);
-        if (g < 0) return ST_BORDER;
+        if (g < 0) {
+            if (bc == BC_CLOSED) return ST_BORDER;
+            // updateAtBoundaryEdge (tangentialOpenMeshSpace.cpp:3-39, absorbingOpenMeshSpace.cpp:2-26)
+            int inner = -1;
+            for (int k = 0; k < 3; ++k)
+                if (M.F[3 * f + k] != inv0 && M.F[3 * f + k] != inv1) inner = M.F[3 * f + k];
+            double edge[3], orth[3], inward[3], here[3];
+            sub3(vp(M, inv1), vp(M, inv0), edge);
+            cross3(ns, edge, orth);
+            normalize3(orth);
+            construct_pt(p[0], p[1], p[2], sb, here);
+            sub3(vp(M, inner), here, inward);
+            if (bc == BC_ABSORBING) {
+                if (ntv > 0) project_if_over_boundary(tv, ntv, orth, inward);
+                for (int c = 0; c < 3; ++c) tb[c] = sb[c];
+                break;
+            }
+            double fwd[3] = {edge[0], edge[1], edge[2]}, bwd[3];
+            sub3(vp(M, inv0), vp(M, inv1), bwd);
+            normalize3(fwd);
+            normalize3(bwd);
+            double dn[3] = {disp[0], disp[1], disp[2]};
+            normalize3(dn);
+            const double fd = dot3(dn, fwd), bd = dot3(dn, bwd);
+            const double len = norm3(disp);  // the whole remaining displacement, measured before the edge was reached
+            project_if_over_boundary(tv, ntv, orth, inward);
+            const bool stop = fd <= 0 && bd <= 0;
+            for (int c = 0; c < 3; ++c) {
+                disp[c] = fd > bd ? fd * len * fwd[c] : bd * len * bwd[c];
+                target[c] = here[c] + disp[c];
+            }
+            lastA = lastB = -1;
+            if (stop) break;  // the reference then writes the target weights found at the top of this pass
+            continue;
+        }
         construct_pt(p[0], p[1], p[2], ip, sp);
         double nt[3] = {M.N[3 * g], M.N[3 * g + 1], M.N[3 * g + 2]};
         double ndt = dot3(ns, nt);
@@ -1395,7 +1542,7 @@ void oracle_transport(void* m, int n, int* face, double* bary, double* disp, dou
     for (int i = 0; i < n; ++i) {
         int cr = 0;
         int st = transport_one(*M, face[i], &bary[3 * i], &disp[3 * i], transport ? &transport[3 * ntv * i] : nullptr,
-                               ntv, maxIter, &cr);
+                               ntv, maxIter, &cr, g_bc);
         if (status) status[i] = st;
         if (crossings) crossings[i] = cr;
     }
@@ -1688,7 +1835,7 @@ int move_all(const Mesh& M, int n, int* face, double* bary, double* disp, double
 #pragma omp parallel for schedule(static) reduction(| : err)
     for (int i = 0; i < n; ++i) {
         int st = transport_one(M, face[i], &bary[3 * i], &disp[3 * i], vel ? &vel[3 * i] : nullptr, vel ? 1 : 0,
-                               100000, nullptr);
+                               100000, nullptr, g_bc);
         if (st) err |= (1 << st);
     }
     (void)nThreads;
@@ -1915,7 +2062,7 @@ int oracle_fire(void* m, int n, int* face, double* bary, double* vel, double* fo
             }
 #pragma omp parallel for schedule(static) reduction(| : err)
         for (int i = 0; i < n; ++i) {
-            int s2 = transport_one(*M, face[i], &bary[3 * i], &disp[3 * i], &tv[6 * i], 2, 100000, nullptr);
+            int s2 = transport_one(*M, face[i], &bary[3 * i], &disp[3 * i], &tv[6 * i], 2, 100000, nullptr, g_bc);
             if (s2) err |= (1 << s2);
         }
         for (int i = 0; i < n; ++i)
@@ -2018,6 +2165,10 @@ void oracle_stress(void* m, int n, const int* face, const double* bary, const do
     const double density = n / area;
     for (int k = 0; k < 9; ++k) stress[k] = density * 1.0 * vv[k] / (2 * n) + fdr[k] / (2 * 2 * area * n);
 }
+
+// Boundary condition of every later walk: 0 closed (triangulatedMeshSpace), 1 tangentialOpenMeshSpace,
+// 2 absorbingOpenMeshSpace.
+void oracle_set_boundary(int bc) { g_bc = bc; }
 
 // noseHooverNVT::setBathVariables (noseHooverNVT.cpp:28-36): fills chain as used by oracle_simulate
 void oracle_nvt_init(int n, double T, double tau, int Mc, double* chain)

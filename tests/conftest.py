@@ -17,3 +17,11 @@ def oracle_mod():
     import oracle
     oracle.build()
     return oracle
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    """The library's Python front end and a context on cuda:0 (GPU tests only)."""
+    from curvedspacesim_gb300 import api
+    ctx = api.Context(0)
+    return api, ctx

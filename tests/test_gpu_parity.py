@@ -9,13 +9,6 @@ from curvedspacesim_gb300 import meshes as ms
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def gpu():
-    from curvedspacesim_gb300 import api
-    ctx = api.Context(0)
-    return api, ctx
-
-
 def _tangent(V, F, f, rng, scale):
     N = ms.face_normals(V, F)[f]
     raw = rng.standard_normal((len(f), 3))
