@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "cssg.h"
+#include "curvedSpaceSimDatabase.hpp"
 
 namespace cssg {
 
@@ -262,6 +263,19 @@ public:
         }
     }
 
+    //! triangulatedMeshSpace::meshPositionToEuclideanLocation: R3 points of mesh positions (PMP::construct_point)
+    void meshPositionToEuclideanLocation(const std::vector<meshPosition>& p, std::vector<double>& out) const
+    {
+        out.resize(3 * p.size());
+        for (size_t i = 0; i < p.size(); ++i) {
+            const int* f = &F_[3 * (size_t)p[i].faceIndex];
+            const double s = p[i].x[0] + p[i].x[1] + p[i].x[2];
+            for (int c = 0; c < 3; ++c)
+                out[3 * i + c] = (p[i].x[0] * V_[3 * (size_t)f[0] + c] + p[i].x[1] * V_[3 * (size_t)f[1] + c] +
+                                  p[i].x[2] * V_[3 * (size_t)f[2] + c]) / s;
+        }
+    }
+
     cssg_ctx* context() const { return ctx_; }
     cssg_mesh* mesh() const { return mesh_; }
     bool submeshing() const { return submeshingActivated_; }
@@ -439,6 +453,41 @@ public:
 private:
     cssg_system* sys_ = nullptr;
 };
+
+//! simpleModelDatabase::writeState for a device-resident simulation: pulls the state and appends a record
+inline void writeState(simpleModelDatabase& db, gpuSimulation& sim, double time)
+{
+    sim.pull();
+    const int n = sim.N;
+    std::vector<double> r3, bary(3 * (size_t)n), vel(3 * (size_t)n), frc(3 * (size_t)n);
+    std::vector<int> face(n), types(n, 0);
+    sim.space_.meshPositionToEuclideanLocation(sim.positions, r3);
+    for (int i = 0; i < n; ++i) {
+        face[i] = sim.positions[i].faceIndex;
+        for (int c = 0; c < 3; ++c) {
+            bary[3 * i + c] = sim.positions[i].x[c];
+            vel[3 * i + c] = sim.velocities[i][c];
+            frc[3 * i + c] = sim.forces[i][c];
+        }
+    }
+    db.writeState(r3, bary, face, vel, frc, types, time);
+}
+
+//! simpleModelDatabase::readState into a device-resident simulation (fields the database lacks are left unchanged)
+inline double readState(const simpleModelDatabase& db, gpuSimulation& sim, int rec)
+{
+    sim.pull();
+    std::vector<double> bary, vel, frc;
+    std::vector<int> face, types;
+    const double t = db.readState(rec, bary, face, vel, frc, types);
+    for (int i = 0; i < sim.N; ++i) {
+        sim.positions[i] = meshPosition(point3(bary[3 * i], bary[3 * i + 1], bary[3 * i + 2]), face[i]);
+        if (!vel.empty()) sim.velocities[i] = vector3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+        if (!frc.empty()) sim.forces[i] = vector3(frc[3 * i], frc[3 * i + 1], frc[3 * i + 2]);
+    }
+    sim.push();
+    return t;
+}
 
 }  // namespace cssg
 
