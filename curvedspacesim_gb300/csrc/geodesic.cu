@@ -64,7 +64,9 @@ __device__ __forceinline__ double bitsd(unsigned long long b)
 
 struct WarpCtl {
     int nA, nB, nLA, nLB, nLog, nV, nF, nT, err, nBA, nBB, nProc;
-    int nPT, nCT;  // task counts of the current batch of windows
+    int nPT, nCT;       // task counts of the current batch of windows
+    int qHead, qTail;   // band queue: a ring over S.wA (absolute counts; slot = count % CW)
+    double thr;         // upper edge of the current distance band (-inf outside the rounds)
 };
 
 // Task lists of one batch of up to 32 windows (per warp, shared memory): vertex proposals (window << 2 | vertex:
@@ -362,6 +364,16 @@ __device__ __noinline__ void push_win(const DevMesh& M, const Slot& S, const Geo
     const float key = key_lo(w);
     if ((double)key > src.cutoff) return;
     w.key = key;
+    if ((double)key <= ctl->thr) {
+        // inside the current band: queue it for this round
+        const int pos = atomicAdd(&ctl->qTail, 1);
+        if (pos - ctl->qHead >= C.CW) {
+            atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+            return;
+        }
+        S.wA[pos % C.CW] = w;
+        return;
+    }
     int pos = atomicAdd(&ctl->nB, 1);
     if (pos >= C.CW) {
         atomicExch(&ctl->err, CSSG_ST_CAPACITY);
@@ -737,6 +749,8 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     if (lane == 0) {
         ctl->nA = ctl->nB = ctl->nLA = ctl->nLB = ctl->nLog = ctl->nV = ctl->nF = ctl->nT = ctl->err = 0;
         ctl->nBA = ctl->nBB = ctl->nProc = 0;
+        ctl->qHead = ctl->qTail = 0;
+        ctl->thr = -CUDART_INF;
     }
     __syncwarp();
     // ---- targets ---------------------------------------------------------------------------------------------
@@ -1006,6 +1020,13 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
         __syncwarp();
         if (settled(M, S, C, src, nT, mk, lane)) break;
         const double thr = mk + (Lp.deltaScale > 0 ? Lp.deltaScale : 1.0) * (D.delta > 0 ? D.delta : Lp.delta);
+        // the band queue starts with this round's frontier; windows created inside the band join it
+        if (lane == 0) {
+            ctl->qHead = 0;
+            ctl->qTail = nA;
+            ctl->thr = thr;
+        }
+        __syncwarp();
         // pseudo-source launches within the band; the rest stay queued.  Decide per queued vertex, then spread the
         // (vertex, incident face) pairs over the lanes.
         for (int q = lane; q < nP; q += 32) {
@@ -1109,16 +1130,27 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             resolve(M, S, C, src, ctl, r);
         }
         __syncwarp();
-        // windows within the band, 32 at a time: each lane classifies one window, then the vertex proposals and the
-        // child windows of the batch are spread over all lanes (FP64 instructions cost the same with 1 or 32 lanes)
-        for (int base = 0; base < nA; base += 32) {
-            const int q = base + lane;
+        // the band queue, 32 windows at a time: each lane classifies one window, then the vertex proposals and the
+        // child windows of the batch are spread over all lanes (FP64 instructions cost the same with 1 or 32 lanes);
+        // children inside the band join the queue, so a round runs until its band is empty
+        while (true) {
+            __syncwarp();
+            const int head = ctl->qHead;
+            const int tail = min(ctl->qTail, head + C.CW);
+            if (head >= tail || ctl->err) break;
+            if (ctl->nProc > Lp.maxWindows) {
+                if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
+                break;
+            }
+            const int cnt = min(32, tail - head);
+            const int q = (head + lane) % C.CW;
+            __syncwarp();
             if (lane == 0) {
                 ctl->nPT = 0;
                 ctl->nCT = 0;
             }
             __syncwarp();
-            if (q < nA) {
+            if (lane < cnt) {
                 Win w = S.wA[q];
                 if ((double)w.key > thr) {
                     int pos = atomicAdd(&ctl->nB, 1);
@@ -1140,7 +1172,9 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             }
             for (int p = lane; p < nCT; p += 32) child_task(M, S, C, src, ctl, S.taskC[p]);
             __syncwarp();
+            if (lane == 0) ctl->qHead = head + cnt;
         }
+        if (lane == 0) ctl->thr = -CUDART_INF;
     }
     __syncwarp();
     // ---- results -------------------------------------------------------------------------------------------------
