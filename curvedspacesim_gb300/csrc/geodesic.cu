@@ -352,19 +352,29 @@ __device__ __noinline__ bool trim(const DevMesh& M, const Slot& S, const GeoCaps
     return true;
 }
 
-__device__ __noinline__ void push_win(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, Win w)
+// Where a new window goes: 0 nowhere (outside the domain, empty, beyond the cutoff), 1 the current band queue,
+// 2 the next frontier.  Clamps its interval to the edge and sets its key.  No trim here: windows are trimmed when
+// they are processed, against the labels of that round.
+__device__ __forceinline__ int window_dest(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src,
+                                           const WarpCtl* ctl, Win& w)
 {
     const int g = w.he >> 2, j = w.he & 3;
-    if (g == src.f0 || !in_domain(M, S, C, src, g)) return;
+    if (g == src.f0 || !in_domain(M, S, C, src, g)) return 0;
     const double L = M.geom[9 * g + 3 * j];
     w.b0 = fmax(0.0, w.b0);
     w.b1 = fmin(L, w.b1);
-    if (!(w.b1 - w.b0 > 1e-14 * L)) return;
-    // no trim here: the window is trimmed when it is processed, against the labels of that round
+    if (!(w.b1 - w.b0 > 1e-14 * L)) return 0;
     const float key = key_lo(w);
-    if ((double)key > src.cutoff) return;
+    if ((double)key > src.cutoff) return 0;
     w.key = key;
-    if ((double)key <= ctl->thr) {
+    return (double)key <= ctl->thr ? 1 : 2;
+}
+
+__device__ __noinline__ void push_win(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, Win w)
+{
+    const int dest = window_dest(M, S, C, src, ctl, w);
+    if (dest == 0) return;
+    if (dest == 1) {
         // inside the current band: queue it for this round
         const int pos = atomicAdd(&ctl->qTail, 1);
         if (pos - ctl->qHead >= C.CW) {
@@ -472,12 +482,12 @@ struct CrossC {
 // Phase A of one window (one lane): trim, log it for the target queries and update the targets' running bests,
 // then queue the vertex proposals and the child windows it makes.  The trimmed interval is written back to wA[q],
 // where the tasks read it.
-__device__ void classify(const DevMesh& M, const Slot& S, const GeoCaps& C, WarpCtl* ctl, Win w, int q,
-                         int& processed)
+// Returns the tasks the window makes as a mask: bits 0-2 vertex proposals (opposite vertex, A, B), bits 3-4 child
+// windows (through C->A, through B->C); bit 5 = processed (it survived the trim).  The caller appends them with
+// warp-aggregated offsets.
+__device__ int classify(const DevMesh& M, const Slot& S, const GeoCaps& C, WarpCtl* ctl, Win w, int q)
 {
-    if (!trim(M, S, C, w)) return;
-    processed++;
-    atomicAdd(&ctl->nProc, 1);
+    if (!trim(M, S, C, w)) return 0;
     const int g = w.he >> 2, j = w.he & 3;
     const double L = M.geom[9 * g + 3 * j], cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
     const double tol = 1e-12 * L;
@@ -506,11 +516,24 @@ __device__ void classify(const DevMesh& M, const Slot& S, const GeoCaps& C, Warp
     S.wA[q].b0 = w.b0;
     S.wA[q].b1 = w.b1;
     const CrossC xc(w, cx, cy);
-    if (xc.rel(w.b0 - tol) <= 0 && xc.rel(w.b1 + tol) >= 0) S.taskP[atomicAdd(&ctl->nPT, 1)] = q << 2;
-    if (w.b0 <= tol) S.taskP[atomicAdd(&ctl->nPT, 1)] = (q << 2) | 1;
-    if (w.b1 >= L - tol) S.taskP[atomicAdd(&ctl->nPT, 1)] = (q << 2) | 2;
-    if (xc.rel(w.b0) < 0 && M.twin[3 * g + (j + 2) % 3] >= 0) S.taskC[atomicAdd(&ctl->nCT, 1)] = q << 1;
-    if (xc.rel(w.b1) > 0 && M.twin[3 * g + (j + 1) % 3] >= 0) S.taskC[atomicAdd(&ctl->nCT, 1)] = (q << 1) | 1;
+    int mask = 32;
+    if (xc.rel(w.b0 - tol) <= 0 && xc.rel(w.b1 + tol) >= 0) mask |= 1;
+    if (w.b0 <= tol) mask |= 2;
+    if (w.b1 >= L - tol) mask |= 4;
+    if (xc.rel(w.b0) < 0 && M.twin[3 * g + (j + 2) % 3] >= 0) mask |= 8;
+    if (xc.rel(w.b1) > 0 && M.twin[3 * g + (j + 1) % 3] >= 0) mask |= 16;
+    return mask;
+}
+
+// warp-aggregated append: lanes with `take` get consecutive slots starting at *counter (shared); returns the lane's
+// slot (or -1).  Every lane of the warp must call it.
+__device__ __forceinline__ int warp_append(int* counter, bool take, int lane)
+{
+    const unsigned m = __ballot_sync(FULL, take);
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(FULL, base, 0);
+    return take ? base + __popc(m & ((1u << lane) - 1)) : -1;
 }
 
 // a queued vertex proposal: path length through the window to one of its face's vertices
@@ -536,14 +559,13 @@ __device__ void proposal_task(const DevMesh& M, const Slot& S, const GeoCaps& C,
 
 // a queued child window: the part of the window's rays that leaves its face through one of the two other edges,
 // expressed in the frame of that edge's twin
-__device__ void child_task(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, int task)
+__device__ void child_task(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int task, Win& c)
 {
     const Win w = S.wA[task >> 1];
     const int g = w.he >> 2, j = w.he & 3;
     const double cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
     const CrossC xc(w, cx, cy);
     const double r0 = xc.rel(w.b0), r1 = xc.rel(w.b1);
-    Win c;
     c.sigma = w.sigma;
     double ux, uy;
     if ((task & 1) == 0) {  // exit through edge C->A (local j+2); child frame: origin A, x toward C
@@ -592,7 +614,6 @@ __device__ void child_task(const DevMesh& M, const Slot& S, const GeoCaps& C, co
         c.c = w.c;
         c.s = w.s;
     }
-    push_win(M, S, C, src, ctl, c);
 }
 
 __device__ __forceinline__ double warp_min(double x)
@@ -1150,15 +1171,33 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                 ctl->nCT = 0;
             }
             __syncwarp();
+            int tmask = 0;
+            bool defer = false;
+            Win w;
             if (lane < cnt) {
-                Win w = S.wA[q];
-                if ((double)w.key > thr) {
-                    int pos = atomicAdd(&ctl->nB, 1);
+                w = S.wA[q];
+                defer = (double)w.key > thr;
+                if (!defer) tmask = classify(M, S, C, ctl, w, q);
+            }
+            {
+                const int pos = warp_append(&ctl->nB, defer, lane);  // beyond the band: next frontier
+                if (defer) {
                     if (pos < C.CW) S.wB[pos] = w;
                     else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
-                } else {
-                    classify(M, S, C, ctl, w, q, processed);
                 }
+            }
+            {
+                const unsigned pm = __ballot_sync(FULL, tmask & 32);
+                processed += (tmask & 32) ? 1 : 0;
+                if (lane == 0) ctl->nProc += __popc(pm);
+            }
+            for (int k = 0; k < 3; ++k) {
+                const int pos = warp_append(&ctl->nPT, (tmask >> k) & 1, lane);
+                if (pos >= 0) S.taskP[pos] = (q << 2) | k;
+            }
+            for (int k = 0; k < 2; ++k) {
+                const int pos = warp_append(&ctl->nCT, (tmask >> (3 + k)) & 1, lane);
+                if (pos >= 0) S.taskC[pos] = (q << 1) | k;
             }
             __syncwarp();
             const int nPT = ctl->nPT, nCT = ctl->nCT;
@@ -1170,7 +1209,23 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                 resolve(M, S, C, src, ctl, r);
                 __syncwarp();
             }
-            for (int p = lane; p < nCT; p += 32) child_task(M, S, C, src, ctl, S.taskC[p]);
+            for (int p0 = 0; p0 < nCT; p0 += 32) {
+                Win c;
+                int dest = 0;
+                if (p0 + lane < nCT) {
+                    child_task(M, S, C, src, S.taskC[p0 + lane], c);
+                    dest = window_dest(M, S, C, src, ctl, c);
+                }
+                const int pr = warp_append(&ctl->qTail, dest == 1, lane);
+                const int pb = warp_append(&ctl->nB, dest == 2, lane);
+                if (dest == 1) {
+                    if (pr - head >= C.CW) atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                    else S.wA[pr % C.CW] = c;
+                } else if (dest == 2) {
+                    if (pb < C.CW) S.wB[pb] = c;
+                    else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                }
+            }
             __syncwarp();
             if (lane == 0) ctl->qHead = head + cnt;
         }
