@@ -26,7 +26,7 @@ EXPORTS = [
     "cssg_system_create_batched", "cssg_mlp_param_count", "cssg_screen_features", "cssg_mlp_infer", "cssg_mlp_grad",
     "cssg_mlp_adam", "cssg_system_set_screen", "cssg_system_screen_counters", "cssg_distance_batch_noalloc",
     "cssg_system_set_tuning", "cssg_system_autotune", "cssg_system_fire", "cssg_system_stress",
-    "cssg_mesh_set_boundary",
+    "cssg_mesh_set_boundary", "cssg_diag_reciprocal",
 ]
 
 
@@ -119,6 +119,7 @@ def load(build_if_missing: bool = True):
     L.cssg_system_reset_thermostat.argtypes = [P]
     L.cssg_system_kernels_per_step.argtypes = [P, P]
     L.cssg_diag_fp64_peak.argtypes = [P, P]
+    L.cssg_diag_reciprocal.argtypes = [P, I, P, P]
     L.cssg_mlp_param_count.argtypes = []
     L.cssg_system_set_screen.argtypes = [P, P, D, I]
     L.cssg_system_screen_counters.argtypes = [P, P]

@@ -45,6 +45,21 @@ struct cssg_ctx {
     bool ownStream;
 };
 
+// Reciprocal by Newton-Raphson iteration r <- r (2 - d r) (two fused multiply-adds per step) seeded with the
+// single-precision reciprocal: the relative error squares each step (2^-23 -> 2^-46 -> below double rounding), so
+// two steps give 1/d within a few ulps (not correctly rounded).  Cheaper on the FP64 pipe than an IEEE double
+// division; used for geometric denominators.  Outside the float range it falls back to the division.
+__device__ __forceinline__ double rcp_nr(double d)
+{
+    const double a = fabs(d);
+    if (!(a > 1e-30 && a < 1e30)) return 1.0 / d;
+    double r = (double)__frcp_rn((float)d);
+    double e = fma(-d, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-d, r, 1.0);
+    return fma(r, e, r);
+}
+
 // error plumbing
 void cssg_set_error(const std::string& msg);
 int cssg_cuda_fail(cudaError_t e, const char* what);

@@ -50,3 +50,23 @@ extern "C" int cssg_diag_fp64_peak(cssg_ctx* ctx, double* gflops)
     *gflops = flops / (ms * 1e-3) / 1e9;
     return CSSG_OK;
 }
+
+namespace {
+__global__ void reciprocal_kernel(int n, const double* __restrict__ x, double* __restrict__ out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = rcp_nr(x[i]);
+}
+}  // namespace
+
+// The propagation's reciprocal (rcp_nr) on n device values, for accuracy tests.
+extern "C" int cssg_diag_reciprocal(cssg_ctx* ctx, int n, const double* x, double* out)
+{
+    if (!ctx || n < 0 || (n > 0 && (!x || !out))) {
+        cssg_set_error("cssg_diag_reciprocal: bad arguments");
+        return CSSG_ERR_ARG;
+    }
+    if (n) reciprocal_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, x, out);
+    CSSG_CUDA(cudaGetLastError());
+    return CSSG_OK;
+}

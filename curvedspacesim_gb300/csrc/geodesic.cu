@@ -396,7 +396,7 @@ __device__ __noinline__ void push_win(const DevMesh& M, const Slot& S, const Geo
 __device__ __forceinline__ void start_dir_l(const Win& w, double px, double py, double l, double& dx, double& dy)
 {
     if (w.sigma == 0) {
-        const double inv = 1.0 / l;
+        const double inv = rcp_nr(l);
         double ux = (px - w.sx) * inv, uy = (py - w.sy) * inv;
         dx = w.c * ux - w.s * uy;
         dy = w.s * ux + w.c * uy;
@@ -579,11 +579,11 @@ __device__ void child_task(const DevMesh& M, const Slot& S, const GeoCaps& C, co
         // interval ends: rays from the pseudo-source through (b0, 0) and (b1, 0), in the child frame
         const double X0 = ux * w.b0, D0 = -uy * w.b0 - isy;
         if (r1 >= 0) {
-            c.b0 = isx + (X0 - isx) * (-isy) / D0;
+            c.b0 = isx + (X0 - isx) * (-isy) * rcp_nr(D0);
             c.b1 = M.geom[9 * (t / 3) + 3 * (t % 3)];
         } else {
             const double X1 = ux * w.b1, D1 = -uy * w.b1 - isy;
-            const double R = 1.0 / (D0 * D1);
+            const double R = rcp_nr(D0 * D1);
             c.b0 = isx + (X0 - isx) * (-isy) * (R * D1);
             c.b1 = isx + (X1 - isx) * (-isy) * (R * D0);
         }
@@ -599,10 +599,10 @@ __device__ void child_task(const DevMesh& M, const Slot& S, const GeoCaps& C, co
         const double X1 = ux * (w.b1 - cx) + uy * (-cy), D1 = -uy * (w.b1 - cx) + ux * (-cy) - isy;
         if (r0 <= 0) {
             c.b0 = 0.0;
-            c.b1 = isx + (X1 - isx) * (-isy) / D1;
+            c.b1 = isx + (X1 - isx) * (-isy) * rcp_nr(D1);
         } else {
             const double X0 = ux * (w.b0 - cx) + uy * (-cy), D0 = -uy * (w.b0 - cx) + ux * (-cy) - isy;
-            const double R = 1.0 / (D0 * D1);
+            const double R = rcp_nr(D0 * D1);
             c.b0 = isx + (X0 - isx) * (-isy) * (R * D1);
             c.b1 = isx + (X1 - isx) * (-isy) * (R * D0);
         }

@@ -223,6 +223,9 @@ int cssg_system_kernels_per_step(cssg_system* sys, int* count);
  * dependent-chain kernel timed with CUDA events on the context stream; the denominator of the FP64 roofline of the
  * geodesic kernel.  Synchronises. */
 int cssg_diag_fp64_peak(cssg_ctx* ctx, double* gflops_host);
+/* The reciprocal the propagation uses for geometric denominators (Newton-Raphson from a float seed), on n device
+ * doubles: out[i] = 1/x[i] within a few ulps.  For accuracy tests. */
+int cssg_diag_reciprocal(cssg_ctx* ctx, int n, const double* x, double* out);
 
 /* ---- learned distance screen -------------------------------------------------------------------------------
  * No counterpart in the reference: a 14 -> 64 -> 64 -> 64 -> 1 GELU MLP that predicts the normalised geodesic

@@ -232,3 +232,24 @@ def test_autotune_keeps_results(gpu, oracle_mod):
         S.compute_forces()  # the second evaluation uses the longest-first order built from the first
         assert S.check()[0] == 0
         np.testing.assert_allclose(S.get_state()[3], f0, rtol=0, atol=1e-12)
+
+
+def test_device_reciprocal_accuracy(gpu):
+    """The Newton-Raphson reciprocal used for window geometry stays within a few ulps of 1/x (and falls back to the
+    division outside the float range)."""
+    import ctypes
+    import torch
+    from curvedspacesim_gb300 import _lib
+    api, ctx = gpu
+    rng = np.random.default_rng(0)
+    x = np.concatenate([10.0 ** rng.uniform(-12, 12, 200000) * rng.choice([-1.0, 1.0], 200000),
+                        [1.0, -1.0, 3.0, 1e-40, 1e40, 2.0 ** -1022]])
+    xd = torch.tensor(x, device="cuda:0")
+    od = torch.empty_like(xd)
+    with ctx.use():
+        assert _lib.load().cssg_diag_reciprocal(ctx.h, len(x), ctypes.c_void_p(xd.data_ptr()),
+                                                ctypes.c_void_p(od.data_ptr())) == 0
+    ctx.synchronize()
+    out = od.cpu().numpy()
+    rel = np.abs(out * x - 1.0)
+    assert rel.max() < 2.0 ** -50, rel.max()
