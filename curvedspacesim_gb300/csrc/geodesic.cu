@@ -520,8 +520,11 @@ __device__ int classify(const DevMesh& M, const Slot& S, const GeoCaps& C, WarpC
     if (xc.rel(w.b0 - tol) <= 0 && xc.rel(w.b1 + tol) >= 0) mask |= 1;
     if (w.b0 <= tol) mask |= 2;
     if (w.b1 >= L - tol) mask |= 4;
-    if (xc.rel(w.b0) < 0 && M.twin[3 * g + (j + 2) % 3] >= 0) mask |= 8;
-    if (xc.rel(w.b1) > 0 && M.twin[3 * g + (j + 1) % 3] >= 0) mask |= 16;
+    const double r0 = xc.rel(w.b0), r1 = xc.rel(w.b1);
+    if (r0 < 0 && M.twin[3 * g + (j + 2) % 3] >= 0) mask |= 8;
+    if (r1 > 0 && M.twin[3 * g + (j + 1) % 3] >= 0) mask |= 16;
+    if (r1 >= 0) mask |= 64;   // the C->A child reaches C
+    if (r0 <= 0) mask |= 128;  // the B->C child starts at C
     return mask;
 }
 
@@ -561,14 +564,15 @@ __device__ void proposal_task(const DevMesh& M, const Slot& S, const GeoCaps& C,
 // expressed in the frame of that edge's twin
 __device__ void child_task(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int task, Win& c)
 {
-    const Win w = S.wA[task >> 1];
+    // task = window << 2 | exit << 1 | flag: exit 0 (C->A) with flag "the interval reaches past C", exit 1 (B->C)
+    // with flag "the interval starts before C" (both decided by classify)
+    const Win w = S.wA[task >> 2];
     const int g = w.he >> 2, j = w.he & 3;
     const double cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
-    const CrossC xc(w, cx, cy);
-    const double r0 = xc.rel(w.b0), r1 = xc.rel(w.b1);
+    const bool flag = task & 1;
     c.sigma = w.sigma;
     double ux, uy;
-    if ((task & 1) == 0) {  // exit through edge C->A (local j+2); child frame: origin A, x toward C
+    if ((task & 2) == 0) {  // exit through edge C->A (local j+2); child frame: origin A, x toward C
         const int t = M.twin[3 * g + (j + 2) % 3];
         ux = M.exitu[12 * g + 4 * j];
         uy = M.exitu[12 * g + 4 * j + 1];
@@ -578,7 +582,7 @@ __device__ void child_task(const DevMesh& M, const Slot& S, const GeoCaps& C, co
         c.sy = isy;
         // interval ends: rays from the pseudo-source through (b0, 0) and (b1, 0), in the child frame
         const double X0 = ux * w.b0, D0 = -uy * w.b0 - isy;
-        if (r1 >= 0) {
+        if (flag) {
             c.b0 = isx + (X0 - isx) * (-isy) * rcp_nr(D0);
             c.b1 = M.geom[9 * (t / 3) + 3 * (t % 3)];
         } else {
@@ -597,7 +601,7 @@ __device__ void child_task(const DevMesh& M, const Slot& S, const GeoCaps& C, co
         c.sx = isx;
         c.sy = isy;
         const double X1 = ux * (w.b1 - cx) + uy * (-cy), D1 = -uy * (w.b1 - cx) + ux * (-cy) - isy;
-        if (r0 <= 0) {
+        if (flag) {
             c.b0 = 0.0;
             c.b1 = isx + (X1 - isx) * (-isy) * rcp_nr(D1);
         } else {
@@ -1197,7 +1201,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             }
             for (int k = 0; k < 2; ++k) {
                 const int pos = warp_append(&ctl->nCT, (tmask >> (3 + k)) & 1, lane);
-                if (pos >= 0) S.taskC[pos] = (q << 1) | k;
+                if (pos >= 0) S.taskC[pos] = (q << 2) | (k << 1) | ((tmask >> (6 + k)) & 1);
             }
             __syncwarp();
             const int nPT = ctl->nPT, nCT = ctl->nCT;
