@@ -1052,186 +1052,205 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             ctl->thr = thr;
         }
         __syncwarp();
-        // pseudo-source launches within the band; the rest stay queued.  Decide per queued vertex, then spread the
-        // (vertex, incident face) pairs over the lanes.
-        for (int q = lane; q < nP; q += 32) {
-            int v = S.lB[q];
-            int h = vfind(S, C.CV, v);
-            S.ld[3 * q] = -1.0;
-            int deg = 0;
-            if (h >= 0) {
-                unsigned long long lb = ldv(&S.vlab[h]);
-                double d = bitsd(lb);
-                if (d > thr) {
-                    int pos = atomicAdd(&ctl->nLA, 1);
-                    if (pos < C.CL) S.lA[pos] = v;
-                    else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
-                } else if (atomicExch(&S.vlaunched[h], lb) != lb) {  // not yet launched with this label
-                    S.ld[3 * q] = d;
-                    S.ld[3 * q + 1] = S.vtx[h];
-                    S.ld[3 * q + 2] = S.vty[h];
-                    deg = M.vfStart[v + 1] - M.vfStart[v];
-                    launches++;
-                }
-            }
-            S.lpre[q] = deg;
-        }
-        __syncwarp();
-        // exclusive prefix of the face counts (warp scan over chunks of 32 entries)
-        int pairs = 0;
-        for (int base = 0; base < nP; base += 32) {
-            int q = base + lane;
-            int x = q < nP ? S.lpre[q] : 0;
-            int incl = x;
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(FULL, incl, o);
-                if (lane >= o) incl += y;
-            }
-            __syncwarp();
-            if (q < nP) S.lpre[q] = pairs + incl - x;
-            pairs += __shfl_sync(FULL, incl, 31);
-        }
-        if (lane == 0) S.lpre[nP] = pairs;
-        __syncwarp();
-        // pass 1: windows on the opposite edges + edge-path proposals, one (vertex, face) pair per lane
-        for (int p = lane; p < pairs; p += 32) {
-            int lo = 0, hi = nP - 1;  // last entry with lpre <= p
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (S.lpre[mid] <= p) lo = mid;
-                else hi = mid - 1;
-            }
-            const int q = lo;
-            const int v = S.lB[q];
-            const double d = S.ld[3 * q], tx = S.ld[3 * q + 1], ty = S.ld[3 * q + 2];
-            const int f = M.vfList[M.vfStart[v] + (p - S.lpre[q])];
-            if (!in_domain(M, S, C, src, f)) continue;
-            int k = 0;
-            while (M.F[3 * f + k] != v) ++k;
-            int e = (k + 1) % 3;
-            VRec r1, r2;
-            propose(S, C, ctl, M.F[3 * f + e], d + M.geom[9 * f + 3 * k], tx, ty, r1);
-            propose(S, C, ctl, M.F[3 * f + (k + 2) % 3], d + M.geom[9 * f + 3 * ((k + 2) % 3)], tx, ty, r2);
-            int t = M.twin[3 * f + e];
-            if (t < 0) continue;
-            Win c;
-            c.he = (t / 3) * 4 + t % 3;
-            c.sigma = d;
-            double L = M.geom[9 * f + 3 * e];
-            c.sx = L - M.geom[9 * f + 3 * e + 1];
-            c.sy = -M.geom[9 * f + 3 * e + 2];
-            c.b0 = 0;
-            c.b1 = L;
-            c.c = tx;
-            c.s = ty;
-            push_win(M, S, C, src, ctl, c);
-        }
-        __syncwarp();
-        // pass 2: surviving edge-path proposals take the start direction their launcher had
-        for (int p = lane; p < pairs; p += 32) {
-            int lo = 0, hi = nP - 1;
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (S.lpre[mid] <= p) lo = mid;
-                else hi = mid - 1;
-            }
-            const int q = lo;
-            const int v = S.lB[q];
-            const double d = S.ld[3 * q], tx = S.ld[3 * q + 1], ty = S.ld[3 * q + 2];
-            const int f = M.vfList[M.vfStart[v] + (p - S.lpre[q])];
-            if (!in_domain(M, S, C, src, f)) continue;
-            int k = 0;
-            while (M.F[3 * f + k] != v) ++k;
-            VRec r;
-            r.dx = tx;
-            r.dy = ty;
-            r.v = M.F[3 * f + (k + 1) % 3];
-            r.d = d + M.geom[9 * f + 3 * k];
-            r.slot = vfind(S, C.CV, r.v);
-            resolve(M, S, C, src, ctl, r);
-            r.v = M.F[3 * f + (k + 2) % 3];
-            r.d = d + M.geom[9 * f + 3 * ((k + 2) % 3)];
-            r.slot = vfind(S, C.CV, r.v);
-            resolve(M, S, C, src, ctl, r);
-        }
-        __syncwarp();
-        // the band queue, 32 windows at a time: each lane classifies one window, then the vertex proposals and the
-        // child windows of the batch are spread over all lanes (FP64 instructions cost the same with 1 or 32 lanes);
-        // children inside the band join the queue, so a round runs until its band is empty
+        // The band: pseudo-source launches within it, then its window queue until empty; launches queued meanwhile
+        // whose labels fall inside the band are launched in the same round, then the queue runs again.
+        int nPc = nP;
         while (true) {
-            __syncwarp();
-            const int head = ctl->qHead;
-            const int tail = min(ctl->qTail, head + C.CW);
-            if (head >= tail || ctl->err) break;
-            if (ctl->nProc > Lp.maxWindows) {
-                if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
-                break;
-            }
-            const int cnt = min(32, tail - head);
-            const int q = (head + lane) % C.CW;
-            __syncwarp();
-            if (lane == 0) {
-                ctl->nPT = 0;
-                ctl->nCT = 0;
-            }
-            __syncwarp();
-            int tmask = 0;
-            bool defer = false;
-            Win w;
-            if (lane < cnt) {
-                w = S.wA[q];
-                defer = (double)w.key > thr;
-                if (!defer) tmask = classify(M, S, C, ctl, w, q);
-            }
-            {
-                const int pos = warp_append(&ctl->nB, defer, lane);  // beyond the band: next frontier
-                if (defer) {
-                    if (pos < C.CW) S.wB[pos] = w;
-                    else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+            if (nPc > 0) {
+                const int nP = nPc;
+                // pseudo-source launches within the band; the rest stay queued.  Decide per queued vertex, then
+                // spread the (vertex, incident face) pairs over the lanes.
+                for (int q = lane; q < nP; q += 32) {
+                    int v = S.lB[q];
+                    int h = vfind(S, C.CV, v);
+                    S.ld[3 * q] = -1.0;
+                    int deg = 0;
+                    if (h >= 0) {
+                        unsigned long long lb = ldv(&S.vlab[h]);
+                        double d = bitsd(lb);
+                        if (d > thr) {
+                            int pos = atomicAdd(&ctl->nLA, 1);
+                            if (pos < C.CL) S.lA[pos] = v;
+                            else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                        } else if (atomicExch(&S.vlaunched[h], lb) != lb) {  // not yet launched with this label
+                            S.ld[3 * q] = d;
+                            S.ld[3 * q + 1] = S.vtx[h];
+                            S.ld[3 * q + 2] = S.vty[h];
+                            deg = M.vfStart[v + 1] - M.vfStart[v];
+                            launches++;
+                        }
+                    }
+                    S.lpre[q] = deg;
                 }
-            }
-            {
-                const unsigned pm = __ballot_sync(FULL, tmask & 32);
-                processed += (tmask & 32) ? 1 : 0;
-                if (lane == 0) ctl->nProc += __popc(pm);
-            }
-            for (int k = 0; k < 3; ++k) {
-                const int pos = warp_append(&ctl->nPT, (tmask >> k) & 1, lane);
-                if (pos >= 0) S.taskP[pos] = (q << 2) | k;
-            }
-            for (int k = 0; k < 2; ++k) {
-                const int pos = warp_append(&ctl->nCT, (tmask >> (3 + k)) & 1, lane);
-                if (pos >= 0) S.taskC[pos] = (q << 2) | (k << 1) | ((tmask >> (6 + k)) & 1);
-            }
-            __syncwarp();
-            const int nPT = ctl->nPT, nCT = ctl->nCT;
-            for (int p0 = 0; p0 < nPT; p0 += 32) {
-                VRec r;
-                r.slot = -1;
-                if (p0 + lane < nPT) proposal_task(M, S, C, ctl, S.taskP[p0 + lane], r);
                 __syncwarp();
-                resolve(M, S, C, src, ctl, r);
+                // exclusive prefix of the face counts (warp scan over chunks of 32 entries)
+                int pairs = 0;
+                for (int base = 0; base < nP; base += 32) {
+                    int q = base + lane;
+                    int x = q < nP ? S.lpre[q] : 0;
+                    int incl = x;
+                    for (int o = 1; o < 32; o <<= 1) {
+                        int y = __shfl_up_sync(FULL, incl, o);
+                        if (lane >= o) incl += y;
+                    }
+                    __syncwarp();
+                    if (q < nP) S.lpre[q] = pairs + incl - x;
+                    pairs += __shfl_sync(FULL, incl, 31);
+                }
+                if (lane == 0) S.lpre[nP] = pairs;
+                __syncwarp();
+                // pass 1: windows on the opposite edges + edge-path proposals, one (vertex, face) pair per lane
+                for (int p = lane; p < pairs; p += 32) {
+                    int lo = 0, hi = nP - 1;  // last entry with lpre <= p
+                    while (lo < hi) {
+                        int mid = (lo + hi + 1) >> 1;
+                        if (S.lpre[mid] <= p) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    const int q = lo;
+                    const int v = S.lB[q];
+                    const double d = S.ld[3 * q], tx = S.ld[3 * q + 1], ty = S.ld[3 * q + 2];
+                    const int f = M.vfList[M.vfStart[v] + (p - S.lpre[q])];
+                    if (!in_domain(M, S, C, src, f)) continue;
+                    int k = 0;
+                    while (M.F[3 * f + k] != v) ++k;
+                    int e = (k + 1) % 3;
+                    VRec r1, r2;
+                    propose(S, C, ctl, M.F[3 * f + e], d + M.geom[9 * f + 3 * k], tx, ty, r1);
+                    propose(S, C, ctl, M.F[3 * f + (k + 2) % 3], d + M.geom[9 * f + 3 * ((k + 2) % 3)], tx, ty, r2);
+                    int t = M.twin[3 * f + e];
+                    if (t < 0) continue;
+                    Win c;
+                    c.he = (t / 3) * 4 + t % 3;
+                    c.sigma = d;
+                    double L = M.geom[9 * f + 3 * e];
+                    c.sx = L - M.geom[9 * f + 3 * e + 1];
+                    c.sy = -M.geom[9 * f + 3 * e + 2];
+                    c.b0 = 0;
+                    c.b1 = L;
+                    c.c = tx;
+                    c.s = ty;
+                    push_win(M, S, C, src, ctl, c);
+                }
+                __syncwarp();
+                // pass 2: surviving edge-path proposals take the start direction their launcher had
+                for (int p = lane; p < pairs; p += 32) {
+                    int lo = 0, hi = nP - 1;
+                    while (lo < hi) {
+                        int mid = (lo + hi + 1) >> 1;
+                        if (S.lpre[mid] <= p) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    const int q = lo;
+                    const int v = S.lB[q];
+                    const double d = S.ld[3 * q], tx = S.ld[3 * q + 1], ty = S.ld[3 * q + 2];
+                    const int f = M.vfList[M.vfStart[v] + (p - S.lpre[q])];
+                    if (!in_domain(M, S, C, src, f)) continue;
+                    int k = 0;
+                    while (M.F[3 * f + k] != v) ++k;
+                    VRec r;
+                    r.dx = tx;
+                    r.dy = ty;
+                    r.v = M.F[3 * f + (k + 1) % 3];
+                    r.d = d + M.geom[9 * f + 3 * k];
+                    r.slot = vfind(S, C.CV, r.v);
+                    resolve(M, S, C, src, ctl, r);
+                    r.v = M.F[3 * f + (k + 2) % 3];
+                    r.d = d + M.geom[9 * f + 3 * ((k + 2) % 3)];
+                    r.slot = vfind(S, C.CV, r.v);
+                    resolve(M, S, C, src, ctl, r);
+                }
                 __syncwarp();
             }
-            for (int p0 = 0; p0 < nCT; p0 += 32) {
-                Win c;
-                int dest = 0;
-                if (p0 + lane < nCT) {
-                    child_task(M, S, C, src, S.taskC[p0 + lane], c);
-                    dest = window_dest(M, S, C, src, ctl, c);
+            // the band queue, 32 windows at a time: each lane classifies one window, then the vertex proposals and
+            // the child windows of the batch are spread over all lanes (FP64 instructions cost the same with 1 or
+            // 32 lanes); children inside the band join the queue, so the queue runs until the band is empty
+            while (true) {
+                __syncwarp();
+                const int head = ctl->qHead;
+                const int tail = min(ctl->qTail, head + C.CW);
+                if (head >= tail || ctl->err) break;
+                if (ctl->nProc > Lp.maxWindows) {
+                    if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
+                    break;
                 }
-                const int pr = warp_append(&ctl->qTail, dest == 1, lane);
-                const int pb = warp_append(&ctl->nB, dest == 2, lane);
-                if (dest == 1) {
-                    if (pr - head >= C.CW) atomicExch(&ctl->err, CSSG_ST_CAPACITY);
-                    else S.wA[pr % C.CW] = c;
-                } else if (dest == 2) {
-                    if (pb < C.CW) S.wB[pb] = c;
-                    else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                const int cnt = min(32, tail - head);
+                const int q = (head + lane) % C.CW;
+                __syncwarp();
+                if (lane == 0) {
+                    ctl->nPT = 0;
+                    ctl->nCT = 0;
                 }
+                __syncwarp();
+                int tmask = 0;
+                bool defer = false;
+                Win w;
+                if (lane < cnt) {
+                    w = S.wA[q];
+                    defer = (double)w.key > thr;
+                    if (!defer) tmask = classify(M, S, C, ctl, w, q);
+                }
+                {
+                    const int pos = warp_append(&ctl->nB, defer, lane);  // beyond the band: next frontier
+                    if (defer) {
+                        if (pos < C.CW) S.wB[pos] = w;
+                        else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                    }
+                }
+                {
+                    const unsigned pm = __ballot_sync(FULL, tmask & 32);
+                    processed += (tmask & 32) ? 1 : 0;
+                    if (lane == 0) ctl->nProc += __popc(pm);
+                }
+                for (int k = 0; k < 3; ++k) {
+                    const int pos = warp_append(&ctl->nPT, (tmask >> k) & 1, lane);
+                    if (pos >= 0) S.taskP[pos] = (q << 2) | k;
+                }
+                for (int k = 0; k < 2; ++k) {
+                    const int pos = warp_append(&ctl->nCT, (tmask >> (3 + k)) & 1, lane);
+                    if (pos >= 0) S.taskC[pos] = (q << 2) | (k << 1) | ((tmask >> (6 + k)) & 1);
+                }
+                __syncwarp();
+                const int nPT = ctl->nPT, nCT = ctl->nCT;
+                for (int p0 = 0; p0 < nPT; p0 += 32) {
+                    VRec r;
+                    r.slot = -1;
+                    if (p0 + lane < nPT) proposal_task(M, S, C, ctl, S.taskP[p0 + lane], r);
+                    __syncwarp();
+                    resolve(M, S, C, src, ctl, r);
+                    __syncwarp();
+                }
+                for (int p0 = 0; p0 < nCT; p0 += 32) {
+                    Win c;
+                    int dest = 0;
+                    if (p0 + lane < nCT) {
+                        child_task(M, S, C, src, S.taskC[p0 + lane], c);
+                        dest = window_dest(M, S, C, src, ctl, c);
+                    }
+                    const int pr = warp_append(&ctl->qTail, dest == 1, lane);
+                    const int pb = warp_append(&ctl->nB, dest == 2, lane);
+                    if (dest == 1) {
+                        if (pr - head >= C.CW) atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                        else S.wA[pr % C.CW] = c;
+                    } else if (dest == 2) {
+                        if (pb < C.CW) S.wB[pb] = c;
+                        else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) ctl->qHead = head + cnt;
             }
             __syncwarp();
-            if (lane == 0) ctl->qHead = head + cnt;
+            if (ctl->err) break;
+            const int nL = min(ctl->nLA, C.CL);
+            bool inBand = false;
+            for (int q = lane; q < nL; q += 32) inBand |= vlabel(S, C.CV, S.lA[q]) <= thr;
+            if (!__any_sync(FULL, inBand)) break;
+            for (int q = lane; q < nL; q += 32) S.lB[q] = S.lA[q];
+            __syncwarp();
+            if (lane == 0) ctl->nLA = 0;
+            __syncwarp();
+            nPc = nL;
         }
         if (lane == 0) ctl->thr = -CUDART_INF;
     }
