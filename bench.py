@@ -305,8 +305,15 @@ def run_ours(args, cfg):
     if bits:
         raise RuntimeError(f"per-item errors during warm-up: {bits:#x} {cnt}")
     tune = None
-    if not args.no_autotune:
-        tune = S.autotune(reps=2)
+    if args.tuning:
+        d, w, m, cap, lpt = args.tuning.split(",")
+        S.set_tuning(float(d), int(w), int(m), int(cap), bool(int(lpt)))
+        tune = {"delta_scale": float(d), "warps_per_block": int(w), "mid_slots": int(m), "warps_per_sm": int(cap),
+                "lpt_order": bool(int(lpt)), "source": "--tuning"}
+        S.step(1, graph=not args.profile)
+        torch.cuda.synchronize()
+    elif not args.no_autotune:
+        tune = S.autotune(reps=3)
         S.step(1, graph=not args.profile)
         torch.cuda.synchronize()
         bits, cnt = S.check()
@@ -483,7 +490,7 @@ def run_screen(args, cfg):
     for name, S in (("plain", plain), ("screened", scr)):
         S.step(max(args.warmup, 1), graph=True)
         if not args.no_autotune:
-            tunes[name] = S.autotune(reps=2)
+            tunes[name] = S.autotune(reps=3)
             S.step(1, graph=True)
     torch.cuda.synchronize()
     for name, S in (("plain", plain), ("screened", scr)):
@@ -582,6 +589,9 @@ def main():
     ap.add_argument("--workload", default="torus_nvt")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (band width 1, 8 warps)")
+    ap.add_argument("--tuning", default="",
+                    help="explicit tuning instead of the autotuner: delta_scale,warps_per_block,mid_slots,"
+                         "warps_per_sm,lpt (e.g. 4,8,0,8,1)")
     ap.add_argument("--profile", action="store_true",
                     help="minimal run for ncu: warm-up steps, then one step without graph replay, no other legs")
     args = ap.parse_args()
