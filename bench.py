@@ -306,10 +306,12 @@ def run_ours(args, cfg):
         raise RuntimeError(f"per-item errors during warm-up: {bits:#x} {cnt}")
     tune = None
     if args.tuning:
-        d, w, m, cap, lpt = args.tuning.split(",")
-        S.set_tuning(float(d), int(w), int(m), int(cap), bool(int(lpt)))
+        fields = args.tuning.split(",")
+        d, w, m, cap, lpt = fields[:5]
+        g = int(fields[5]) if len(fields) > 5 else 1
+        S.set_tuning(float(d), int(w), int(m), int(cap), bool(int(lpt)), g)
         tune = {"delta_scale": float(d), "warps_per_block": int(w), "mid_slots": int(m), "warps_per_sm": int(cap),
-                "lpt_order": bool(int(lpt)), "source": "--tuning"}
+                "lpt_order": bool(int(lpt)), "warps_per_source": g, "source": "--tuning"}
         S.step(1, graph=not args.profile)
         torch.cuda.synchronize()
     elif not args.no_autotune:
@@ -591,7 +593,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (band width 1, 8 warps)")
     ap.add_argument("--tuning", default="",
                     help="explicit tuning instead of the autotuner: delta_scale,warps_per_block,mid_slots,"
-                         "warps_per_sm,lpt (e.g. 4,8,0,8,1)")
+                         "warps_per_sm,lpt[,warps_per_source] (e.g. 4,8,0,8,1,1)")
     ap.add_argument("--profile", action="store_true",
                     help="minimal run for ncu: warm-up steps, then one step without graph replay, no other legs")
     args = ap.parse_args()

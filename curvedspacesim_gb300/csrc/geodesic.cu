@@ -67,6 +67,8 @@ struct WarpCtl {
     int nPT, nCT;       // task counts of the current batch of windows
     int qHead, qTail;   // band queue: a ring over S.wA (absolute counts; slot = count % CW)
     double thr;         // upper edge of the current distance band (-inf outside the rounds)
+    double maxChord2;   // largest squared chord to a candidate (cell / all-to-all search)
+    int item;           // the work item the group is on
 };
 
 // Task lists of one batch of up to 32 windows (per warp, shared memory): vertex proposals (window << 2 | vertex:
@@ -725,12 +727,74 @@ __device__ __noinline__ double target_query(const DevMesh& M, const Slot& S, con
     return best;
 }
 
+// A source group: the G warps that solve one source together (G = 1, 2 or 4).  With G = 1 the group is a warp and
+// synchronises with __syncwarp; otherwise with a named barrier of 32 G threads (ids 1..8, one per group of the block).
+template <int G>
+struct Grp {
+    static constexpr int NT = 32 * G;
+    int t;        // thread in the group
+    int lane;     // lane in its warp
+    int wig;      // warp in the group
+    int bar;      // named barrier id
+    double* redD; // G doubles of shared scratch for reductions
+    int* redI;    // G ints
+    __device__ __forceinline__ void sync() const
+    {
+        if (G == 1) __syncwarp();
+        else asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(NT) : "memory");
+    }
+    __device__ __forceinline__ double min(double x) const
+    {
+        for (int o = 16; o > 0; o >>= 1) x = fmin(x, __shfl_xor_sync(FULL, x, o));
+        if (G == 1) return x;
+        if (lane == 0) redD[wig] = x;
+        sync();
+        double r = redD[0];
+        for (int k = 1; k < G; ++k) r = fmin(r, redD[k]);
+        sync();
+        return r;
+    }
+    __device__ __forceinline__ double sum(double x) const
+    {
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+        if (G == 1) return x;
+        if (lane == 0) redD[wig] = x;
+        sync();
+        double r = redD[0];
+        for (int k = 1; k < G; ++k) r += redD[k];
+        sync();
+        return r;
+    }
+    __device__ __forceinline__ int sumi(int x) const
+    {
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+        if (G == 1) return x;
+        if (lane == 0) redI[wig] = x;
+        sync();
+        int r = redI[0];
+        for (int k = 1; k < G; ++k) r += redI[k];
+        sync();
+        return r;
+    }
+    __device__ __forceinline__ bool any(bool p) const
+    {
+        if (G == 1) return __any_sync(FULL, p);
+        return sumi(__any_sync(FULL, p) && lane == 0 ? 1 : 0) > 0;
+    }
+    __device__ __forceinline__ bool all(bool p) const
+    {
+        if (G == 1) return __all_sync(FULL, p);
+        return sumi(__all_sync(FULL, p) || lane != 0 ? 0 : 1) == 0;
+    }
+};
+
 // candidate-based early exit: no queued window can improve any target any more
-__device__ __noinline__ bool settled(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int nT, double minKey,
-                        int lane)
+template <int G>
+__device__ __noinline__ bool settled(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int nT,
+                                    double minKey, const Grp<G>& gp)
 {
     bool ok = true;
-    for (int t = lane; t < nT; t += 32) {
+    for (int t = gp.t; t < nT; t += Grp<G>::NT) {
         if (S.tface[t] == src.f0 || S.tidx[t] < 0) continue;
         double b = bitsd(__ldcg(&S.tbest[t]));
         const double* P = &S.tp[3 * t];
@@ -749,18 +813,23 @@ __device__ __noinline__ bool settled(const DevMesh& M, const Slot& S, const GeoC
         }
         if (!(b <= minKey || minKey > src.cutoff)) ok = false;
     }
-    return __all_sync(FULL, ok);
+    return gp.all(ok);
 }
 
-// The per-source solve (whole warp).  Returns the number of targets; leaves results in the slot.
-__device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, int lane, unsigned long long* cnt)
+// The per-source solve (one source group).  Leaves results in the slot and the outputs.
+template <int G>
+__device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, const Grp<G>& gp,
+                             unsigned long long* cnt)
 {
+    constexpr int NT = Grp<G>::NT;
+    const int lane = gp.lane;
+    const int t0 = gp.t;
     const GeoCaps& C = Lp.caps;
     const SysDesc& D = Lp.sys[Lp.sysOf ? Lp.sysOf[si] : 0];
     const DevMesh& M = D.mesh;
     if (D.bigBin && Lp.routeBig && Lp.failList) {
         // binned to the large-table pass
-        if (lane == 0) {
+        if (t0 == 0) {
             Lp.status[si] = 0;
             Lp.failList[atomicAdd(Lp.failCount, 1)] = si;
         }
@@ -771,22 +840,23 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     src.cutoff = D.cutoff;
     double b0[3] = {Lp.srcBary[3 * si], Lp.srcBary[3 * si + 1], Lp.srcBary[3 * si + 2]};
     load_pt(M, src.f0, b0, src.S);
-    if (lane == 0) {
+    if (t0 == 0) {
         ctl->nA = ctl->nB = ctl->nLA = ctl->nLB = ctl->nLog = ctl->nV = ctl->nF = ctl->nT = ctl->err = 0;
         ctl->nBA = ctl->nBB = ctl->nProc = 0;
         ctl->qHead = ctl->qTail = 0;
+        ctl->maxChord2 = 0;
         ctl->thr = -CUDART_INF;
     }
-    __syncwarp();
+    gp.sync();
     // ---- targets ---------------------------------------------------------------------------------------------
     double maxChord2 = 0;
     if (D.searchMode == 0 || D.searchMode == 3) {
         int beg = Lp.candOff[si], nT = Lp.candOff[si + 1] - beg;
         if (nT > C.CT) {
-            if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
+            if (t0 == 0) ctl->err = CSSG_ST_CAPACITY;
             nT = 0;
         }
-        for (int t = lane; t < nT; t += 32) {
+        for (int t = t0; t < nT; t += NT) {
             if (D.searchMode == 0) {
                 S.tface[t] = Lp.candFace[beg + t];
                 S.tidx[t] = beg + t;
@@ -799,10 +869,11 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                 for (int c = 0; c < 3; ++c) S.tb[3 * t + c] = Lp.partBary[3 * jj + c];
             }
         }
-        if (lane == 0) ctl->nT = nT;
-        if (D.searchMode == 3 && Lp.pairCount && lane == 0) Lp.pairCount[si] = nT;
-    } else {
-        // candidates j != i with chord^2 < range2 (cell list: 27 cells in (x, y, z) loop order; or all particles)
+        if (t0 == 0) ctl->nT = nT;
+        if (D.searchMode == 3 && Lp.pairCount && t0 == 0) Lp.pairCount[si] = nT;
+    } else if (gp.wig == 0) {
+        // candidates j != i with chord^2 < range2 (cell list: 27 cells in (x, y, z) loop order; or all particles);
+        // the first warp of the group searches, in the reference's order
         const double* Pi = &Lp.srcPos[3 * si];
         int count = 0;
         auto consider = [&](int jj, bool valid) {
@@ -850,32 +921,36 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
             count = 0;
         }
-        if (lane == 0) ctl->nT = count;
+        if (lane == 0) {
+            ctl->nT = count;
+            ctl->maxChord2 = maxChord2;
+        }
         if (Lp.pairCount && lane == 0) Lp.pairCount[si] = count;
     }
-    __syncwarp();
+    gp.sync();
+    maxChord2 = ctl->maxChord2;
     const int nT = ctl->nT;
     if (ctl->err == CSSG_ST_CAPACITY && Lp.failList) {
-        if (lane == 0) {
+        if (t0 == 0) {
             Lp.status[si] = 0;
             Lp.failList[atomicAdd(Lp.failCount, 1)] = si;
         }
         return;
     }
     if (nT == 0) {
-        if (Lp.srcCost && lane == 0) Lp.srcCost[si] = 1;
-        if (Lp.force && lane == 0) {
+        if (Lp.srcCost && t0 == 0) Lp.srcCost[si] = 1;
+        if (Lp.force && t0 == 0) {
             Lp.force[3 * si] = Lp.force[3 * si + 1] = Lp.force[3 * si + 2] = 0;
         }
-        if (lane == 0) Lp.status[si] = ctl->err;
+        if (t0 == 0) Lp.status[si] = ctl->err;
         return;
     }
-    for (int t = lane; t < nT; t += 32) {
+    for (int t = t0; t < nT; t += NT) {
         load_pt(M, S.tface[t], &S.tb[3 * t], &S.tp[3 * t]);
         S.tbest[t] = INF_BITS;
         S.tnext[t] = -1;
     }
-    __syncwarp();
+    gp.sync();
     // ---- domain: whole mesh or the reference patch ---------------------------------------------------------------
     src.full = !D.submesh;
     double r = D.maxDist;
@@ -894,26 +969,26 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             int t = M.twin[3 * src.f0 + k];
             nb[k] = t < 0 ? -1 : t / 3;
         }
-        for (int t = lane; t < nT; t += 32) {
+        for (int t = t0; t < nT; t += NT) {
             int f = S.tface[t];
             if (f != src.f0) {
                 notInF0 = true;
                 if (f != nb[0] && f != nb[1] && f != nb[2]) notInSeeds = true;
             }
         }
-        notInF0 = __any_sync(FULL, notInF0);
-        notInSeeds = __any_sync(FULL, notInSeeds);
-        if (lane == 0) finsert(S, C.CF, src.f0, ctl, &fresh);
-        __syncwarp();
+        notInF0 = gp.any(notInF0);
+        notInSeeds = gp.any(notInSeeds);
+        if (t0 == 0) finsert(S, C.CF, src.f0, ctl, &fresh);
+        gp.sync();
         if (notInF0) {
-            if (lane < 3 && nb[lane] >= 0) {
-                int h = finsert(S, C.CF, nb[lane], ctl, &fresh);
+            if (t0 < 3 && nb[t0] >= 0) {
+                int h = finsert(S, C.CF, nb[t0], ctl, &fresh);
                 if (fresh && notInSeeds) {
                     int pos = atomicAdd(&ctl->nBA, 1);
-                    S.bA[pos] = nb[lane];
+                    S.bA[pos] = nb[t0];
                 }
             }
-            __syncwarp();
+            gp.sync();
             if (notInSeeds) {
                 const double r2 = r * r;
                 int* cur = S.bA;
@@ -921,10 +996,10 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                 int nCur = ctl->nBA;
                 int guard = 0;
                 while (nCur > 0 && guard++ < 100000) {
-                    __syncwarp();  // every lane has read nCur / err before lane 0 resets the counter
-                    if (lane == 0) ctl->nBB = 0;
-                    __syncwarp();
-                    for (int q = lane; q < 3 * nCur; q += 32) {
+                    gp.sync();  // every lane has read nCur / err before lane 0 resets the counter
+                    if (t0 == 0) ctl->nBB = 0;
+                    gp.sync();
+                    for (int q = t0; q < 3 * nCur; q += NT) {
                         int f = cur[q / 3], k = q % 3;
                         int t = M.twin[3 * f + k];
                         if (t < 0) continue;
@@ -944,7 +1019,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                             else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
                         }
                     }
-                    __syncwarp();
+                    gp.sync();
                     nCur = ctl->err ? 0 : min(ctl->nBB, C.CF);
                     int* tmp = cur;
                     cur = nxt;
@@ -953,16 +1028,16 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             }
         }
         // goal faces (targets) complete the patch
-        for (int t = lane; t < nT; t += 32) finsert(S, C.CF, S.tface[t], ctl, &fresh);
-        __syncwarp();
+        for (int t = t0; t < nT; t += NT) finsert(S, C.CF, S.tface[t], ctl, &fresh);
+        gp.sync();
     }
     // target lists per face (full mode: the face table holds only target faces)
-    for (int t = lane; t < nT; t += 32) {
+    for (int t = t0; t < nT; t += NT) {
         int fresh;
         int h = finsert(S, C.CF, S.tface[t], ctl, &fresh);
         if (h >= 0) S.tnext[t] = atomicExch(&S.fhead[h], t);
     }
-    __syncwarp();
+    gp.sync();
     // ---- source: frame, face-vertex labels, initial windows -------------------------------------------------------
     const int f0 = src.f0;
     const double L0 = M.geom[9 * f0], cx0 = M.geom[9 * f0 + 1], cy0 = M.geom[9 * f0 + 2];
@@ -977,8 +1052,8 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     const double S2x = b0[1] * L0 + b0[2] * cx0, S2y = b0[2] * cy0;
     VRec rec[3];
     rec[0].slot = rec[1].slot = rec[2].slot = -1;
-    if (lane < 3) {
-        int k = lane;
+    if (t0 < 3) {
+        int k = t0;
         int v = M.F[3 * f0 + k];
         double dx = P2[k][0] - S2x, dy = P2[k][1] - S2y;
         double l = len2(dx, dy);
@@ -986,11 +1061,11 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
         double u[3] = {pv[0] - src.S[0], pv[1] - src.S[1], pv[2] - src.S[2]};
         propose(S, C, ctl, v, sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]), dx / l, dy / l, rec[0]);
     }
-    __syncwarp();
+    gp.sync();
     resolve(M, S, C, src, ctl, rec[0]);
-    __syncwarp();
-    if (lane < 3) {
-        int k = lane;
+    gp.sync();
+    if (t0 < 3) {
+        int k = t0;
         int t = M.twin[3 * f0 + k];
         if (t >= 0) {
             double L = M.geom[9 * f0 + 3 * k];
@@ -1010,7 +1085,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             push_win(M, S, C, src, ctl, w);
         }
     }
-    __syncwarp();
+    gp.sync();
     // ---- rounds ---------------------------------------------------------------------------------------------------
     // Distance-banded rounds: each round takes the smallest key among queued windows and queued pseudo-source
     // launches (mk) and handles only what lies within mk + delta, deferring the rest, so labels are close to final
@@ -1019,12 +1094,12 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     int processed = 0, launches = 0;
     int round = 0;
     while (true) {
-        __syncwarp();
+        gp.sync();
         const int nA = min(ctl->nB, C.CW);
         const int nP = min(ctl->nLA, C.CL);
         if (ctl->err || (nA == 0 && nP == 0)) break;
         if (++round > Lp.maxRounds || ctl->nProc > Lp.maxWindows) {
-            if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
+            if (t0 == 0) ctl->err = CSSG_ST_CAPACITY;
             break;
         }
         {
@@ -1032,26 +1107,26 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             S.wA = S.wB;
             S.wB = t;
         }
-        for (int q = lane; q < nP; q += 32) S.lB[q] = S.lA[q];
-        __syncwarp();
-        if (lane == 0) {
+        for (int q = t0; q < nP; q += NT) S.lB[q] = S.lA[q];
+        gp.sync();
+        if (t0 == 0) {
             ctl->nB = 0;
             ctl->nLA = 0;
         }
         double mk = CUDART_INF;
-        for (int q = lane; q < nA; q += 32) mk = fmin(mk, (double)S.wA[q].key);
-        for (int q = lane; q < nP; q += 32) mk = fmin(mk, vlabel(S, C.CV, S.lB[q]));
-        mk = warp_min(mk);
-        __syncwarp();
-        if (settled(M, S, C, src, nT, mk, lane)) break;
+        for (int q = t0; q < nA; q += NT) mk = fmin(mk, (double)S.wA[q].key);
+        for (int q = t0; q < nP; q += NT) mk = fmin(mk, vlabel(S, C.CV, S.lB[q]));
+        mk = gp.min(mk);
+        gp.sync();
+        if (settled<G>(M, S, C, src, nT, mk, gp)) break;
         const double thr = mk + (Lp.deltaScale > 0 ? Lp.deltaScale : 1.0) * (D.delta > 0 ? D.delta : Lp.delta);
         // the band queue starts with this round's frontier; windows created inside the band join it
-        if (lane == 0) {
+        if (t0 == 0) {
             ctl->qHead = 0;
             ctl->qTail = nA;
             ctl->thr = thr;
         }
-        __syncwarp();
+        gp.sync();
         // The band: pseudo-source launches within it, then its window queue until empty; launches queued meanwhile
         // whose labels fall inside the band are launched in the same round, then the queue runs again.
         int nPc = nP;
@@ -1060,7 +1135,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                 const int nP = nPc;
                 // pseudo-source launches within the band; the rest stay queued.  Decide per queued vertex, then
                 // spread the (vertex, incident face) pairs over the lanes.
-                for (int q = lane; q < nP; q += 32) {
+                for (int q = t0; q < nP; q += NT) {
                     int v = S.lB[q];
                     int h = vfind(S, C.CV, v);
                     S.ld[3 * q] = -1.0;
@@ -1082,25 +1157,28 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                     }
                     S.lpre[q] = deg;
                 }
-                __syncwarp();
+                gp.sync();
                 // exclusive prefix of the face counts (warp scan over chunks of 32 entries)
-                int pairs = 0;
-                for (int base = 0; base < nP; base += 32) {
-                    int q = base + lane;
-                    int x = q < nP ? S.lpre[q] : 0;
-                    int incl = x;
-                    for (int o = 1; o < 32; o <<= 1) {
-                        int y = __shfl_up_sync(FULL, incl, o);
-                        if (lane >= o) incl += y;
+                if (gp.wig == 0) {
+                    int run = 0;
+                    for (int base = 0; base < nP; base += 32) {
+                        int q = base + lane;
+                        int x = q < nP ? S.lpre[q] : 0;
+                        int incl = x;
+                        for (int o = 1; o < 32; o <<= 1) {
+                            int y = __shfl_up_sync(FULL, incl, o);
+                            if (lane >= o) incl += y;
+                        }
+                        gp.sync();
+                        if (q < nP) S.lpre[q] = run + incl - x;
+                        run += __shfl_sync(FULL, incl, 31);
                     }
-                    __syncwarp();
-                    if (q < nP) S.lpre[q] = pairs + incl - x;
-                    pairs += __shfl_sync(FULL, incl, 31);
+                    if (t0 == 0) S.lpre[nP] = run;
                 }
-                if (lane == 0) S.lpre[nP] = pairs;
-                __syncwarp();
+                gp.sync();
+                const int pairs = S.lpre[nP];
                 // pass 1: windows on the opposite edges + edge-path proposals, one (vertex, face) pair per lane
-                for (int p = lane; p < pairs; p += 32) {
+                for (int p = t0; p < pairs; p += NT) {
                     int lo = 0, hi = nP - 1;  // last entry with lpre <= p
                     while (lo < hi) {
                         int mid = (lo + hi + 1) >> 1;
@@ -1132,9 +1210,9 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                     c.s = ty;
                     push_win(M, S, C, src, ctl, c);
                 }
-                __syncwarp();
+                gp.sync();
                 // pass 2: surviving edge-path proposals take the start direction their launcher had
-                for (int p = lane; p < pairs; p += 32) {
+                for (int p = t0; p < pairs; p += NT) {
                     int lo = 0, hi = nP - 1;
                     while (lo < hi) {
                         int mid = (lo + hi + 1) >> 1;
@@ -1160,32 +1238,32 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                     r.slot = vfind(S, C.CV, r.v);
                     resolve(M, S, C, src, ctl, r);
                 }
-                __syncwarp();
+                gp.sync();
             }
             // the band queue, 32 windows at a time: each lane classifies one window, then the vertex proposals and
             // the child windows of the batch are spread over all lanes (FP64 instructions cost the same with 1 or
             // 32 lanes); children inside the band join the queue, so the queue runs until the band is empty
             while (true) {
-                __syncwarp();
+                gp.sync();
                 const int head = ctl->qHead;
                 const int tail = min(ctl->qTail, head + C.CW);
                 if (head >= tail || ctl->err) break;
                 if (ctl->nProc > Lp.maxWindows) {
-                    if (lane == 0) ctl->err = CSSG_ST_CAPACITY;
+                    if (t0 == 0) ctl->err = CSSG_ST_CAPACITY;
                     break;
                 }
-                const int cnt = min(32, tail - head);
-                const int q = (head + lane) % C.CW;
-                __syncwarp();
-                if (lane == 0) {
+                const int cnt = min(NT, tail - head);
+                const int q = (head + t0) % C.CW;
+                gp.sync();
+                if (t0 == 0) {
                     ctl->nPT = 0;
                     ctl->nCT = 0;
                 }
-                __syncwarp();
+                gp.sync();
                 int tmask = 0;
                 bool defer = false;
                 Win w;
-                if (lane < cnt) {
+                if (t0 < cnt) {
                     w = S.wA[q];
                     defer = (double)w.key > thr;
                     if (!defer) tmask = classify(M, S, C, ctl, w, q);
@@ -1200,7 +1278,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                 {
                     const unsigned pm = __ballot_sync(FULL, tmask & 32);
                     processed += (tmask & 32) ? 1 : 0;
-                    if (lane == 0) ctl->nProc += __popc(pm);
+                    if (t0 == 0) atomicAdd(&ctl->nProc, __popc(pm));
                 }
                 for (int k = 0; k < 3; ++k) {
                     const int pos = warp_append(&ctl->nPT, (tmask >> k) & 1, lane);
@@ -1210,21 +1288,21 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                     const int pos = warp_append(&ctl->nCT, (tmask >> (3 + k)) & 1, lane);
                     if (pos >= 0) S.taskC[pos] = (q << 2) | (k << 1) | ((tmask >> (6 + k)) & 1);
                 }
-                __syncwarp();
+                gp.sync();
                 const int nPT = ctl->nPT, nCT = ctl->nCT;
-                for (int p0 = 0; p0 < nPT; p0 += 32) {
+                for (int p0 = 0; p0 < nPT; p0 += NT) {
                     VRec r;
                     r.slot = -1;
-                    if (p0 + lane < nPT) proposal_task(M, S, C, ctl, S.taskP[p0 + lane], r);
-                    __syncwarp();
+                    if (p0 + t0 < nPT) proposal_task(M, S, C, ctl, S.taskP[p0 + t0], r);
+                    gp.sync();
                     resolve(M, S, C, src, ctl, r);
-                    __syncwarp();
+                    gp.sync();
                 }
-                for (int p0 = 0; p0 < nCT; p0 += 32) {
+                for (int p0 = 0; p0 < nCT; p0 += NT) {
                     Win c;
                     int dest = 0;
-                    if (p0 + lane < nCT) {
-                        child_task(M, S, C, src, S.taskC[p0 + lane], c);
+                    if (p0 + t0 < nCT) {
+                        child_task(M, S, C, src, S.taskC[p0 + t0], c);
                         dest = window_dest(M, S, C, src, ctl, c);
                     }
                     const int pr = warp_append(&ctl->qTail, dest == 1, lane);
@@ -1237,30 +1315,30 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                         else atomicExch(&ctl->err, CSSG_ST_CAPACITY);
                     }
                 }
-                __syncwarp();
-                if (lane == 0) ctl->qHead = head + cnt;
+                gp.sync();
+                if (t0 == 0) ctl->qHead = head + cnt;
             }
-            __syncwarp();
+            gp.sync();
             if (ctl->err) break;
             const int nL = min(ctl->nLA, C.CL);
             bool inBand = false;
-            for (int q = lane; q < nL; q += 32) inBand |= vlabel(S, C.CV, S.lA[q]) <= thr;
-            if (!__any_sync(FULL, inBand)) break;
-            for (int q = lane; q < nL; q += 32) S.lB[q] = S.lA[q];
-            __syncwarp();
-            if (lane == 0) ctl->nLA = 0;
-            __syncwarp();
+            for (int q = t0; q < nL; q += NT) inBand |= vlabel(S, C.CV, S.lA[q]) <= thr;
+            if (!gp.any(inBand)) break;
+            for (int q = t0; q < nL; q += NT) S.lB[q] = S.lA[q];
+            gp.sync();
+            if (t0 == 0) ctl->nLA = 0;
+            gp.sync();
             nPc = nL;
         }
-        if (lane == 0) ctl->thr = -CUDART_INF;
+        if (t0 == 0) ctl->thr = -CUDART_INF;
     }
-    __syncwarp();
+    gp.sync();
     // ---- results -------------------------------------------------------------------------------------------------
     const int nLog = min(ctl->nLog, C.CLOG);
     const int err = ctl->err;
     if (err == CSSG_ST_CAPACITY && Lp.failList) {
         // tables too small for this source: queue it for the large-table pass, which writes all its outputs
-        if (lane == 0) {
+        if (t0 == 0) {
             Lp.status[si] = 0;
             Lp.failList[atomicAdd(Lp.failCount, 1)] = si;
         }
@@ -1268,7 +1346,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     }
     double fx = 0, fy = 0, fz = 0;
     int inRange = 0;
-    for (int t = lane; t < nT; t += 32) {
+    for (int t = t0; t < nT; t += NT) {
         double ts[3], te[3];
         const bool screened = S.tidx[t] < 0;
         double d = (err || screened) ? CUDART_INF : target_query(M, S, C, src, t, nLog, ts, te);
@@ -1313,26 +1391,26 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
         }
     }
     if (Lp.force) {
-        fx = warp_sum(fx);
-        fy = warp_sum(fy);
-        fz = warp_sum(fz);
-        if (lane == 0) {
+        fx = gp.sum(fx);
+        fy = gp.sum(fy);
+        fz = gp.sum(fz);
+        if (t0 == 0) {
             Lp.force[3 * si] = fx;
             Lp.force[3 * si + 1] = fy;
             Lp.force[3 * si + 2] = fz;
         }
     }
-    inRange = warp_sum_i(inRange);
-    processed = warp_sum_i(processed);
-    launches = warp_sum_i(launches);
-    if (lane == 0 && Lp.srcCost) Lp.srcCost[si] = processed + launches + 8 * round + 1;
-    if (lane == 0 && Lp.stats) {
+    inRange = gp.sumi(inRange);
+    processed = gp.sumi(processed);
+    launches = gp.sumi(launches);
+    if (t0 == 0 && Lp.srcCost) Lp.srcCost[si] = processed + launches + 8 * round + 1;
+    if (t0 == 0 && Lp.stats) {
         Lp.stats[4 * si] = processed;
         Lp.stats[4 * si + 1] = launches;
         Lp.stats[4 * si + 2] = round;
         Lp.stats[4 * si + 3] = nT;
     }
-    if (lane == 0) {
+    if (t0 == 0) {
         Lp.status[si] = err;
         cnt[0] += processed;
         cnt[1] += launches;
@@ -1341,18 +1419,21 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     }
 }
 
-__device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, int lane)
+template <int G>
+__device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, const Grp<G>& gp)
 {
-    __syncwarp();
+    constexpr int NT = Grp<G>::NT;
+    const int lane = gp.t;
+    gp.sync();
     int nV = min(ctl->nV, C.CV), nF = min(ctl->nF, C.CF);
-    for (int q = lane; q < nV; q += 32) {
+    for (int q = lane; q < nV; q += NT) {
         int h = S.vlist[q];
         S.vkey[h] = -1;
         S.vlab[h] = INF_BITS;
         S.vtok[h] = ~0ull;
         S.vlaunched[h] = ~0ull;
     }
-    for (int q = lane; q < nF; q += 32) {
+    for (int q = lane; q < nF; q += NT) {
         int h = S.flist[q];
         S.fkey[h] = -1;
         S.fhead[h] = -1;
@@ -1360,60 +1441,72 @@ __device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, int la
     }
     if (ctl->nV > C.CV || ctl->nF > C.CF) {
         // a table overflowed its touched list: clear it whole
-        for (int q = lane; q < C.CV; q += 32) {
+        for (int q = lane; q < C.CV; q += NT) {
             S.vkey[q] = -1;
             S.vlab[q] = INF_BITS;
             S.vtok[q] = ~0ull;
             S.vlaunched[q] = ~0ull;
         }
-        for (int q = lane; q < C.CF; q += 32) {
+        for (int q = lane; q < C.CF; q += NT) {
             S.fkey[q] = -1;
             S.fhead[q] = -1;
             S.flog[q] = -1;
         }
     }
-    __syncwarp();
+    gp.sync();
 }
 
+// One source group (G warps) per slot; groups pull sources from the work counter until none are left.
+template <int G>
 __global__ void __launch_bounds__(256) geodesic_kernel(GeoLaunch L)
 {
+    constexpr int NT = 32 * G;
     __shared__ WarpCtl ctls[8];
-    __shared__ int tasks[8][kTaskP + kTaskC];
+    __shared__ int tasks[8 * (kTaskP + kTaskC)];
+    __shared__ double redD[8][4];
+    __shared__ int redI[8][4];
     extern __shared__ __align__(16) char dyn[];
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const int warp = blockIdx.x * (blockDim.x >> 5) + wib;
-    if (warp >= L.nSlots) return;
-    WarpCtl* ctl = &ctls[wib];
+    const int gib = threadIdx.x / NT;
+    const int group = blockIdx.x * (blockDim.x / NT) + gib;
+    if (group >= L.nSlots) return;
+    Grp<G> gp;
+    gp.t = threadIdx.x % NT;
+    gp.lane = threadIdx.x & 31;
+    gp.wig = gp.t >> 5;
+    gp.bar = 1 + gib;
+    gp.redD = redD[gib];
+    gp.redI = redI[gib];
+    WarpCtl* ctl = &ctls[gib];
     Slot S;
-    carve(L.caps, (char*)L.scratch + (size_t)warp * L.slotBytes, &S);
-    S.taskP = &tasks[wib][0];
-    S.taskC = &tasks[wib][kTaskP];
+    carve(L.caps, (char*)L.scratch + (size_t)group * L.slotBytes, &S);
+    S.taskP = &tasks[gib * G * (kTaskP + kTaskC)];
+    S.taskC = S.taskP + G * kTaskP;
     if (L.smemTables) {
-        carve_smem(L.caps, dyn + (size_t)wib * smem_per_warp(L.caps), &S);
-        for (int q = lane; q < L.caps.CV; q += 32) {
+        carve_smem(L.caps, dyn + (size_t)gib * smem_per_warp(L.caps), &S);
+        for (int q = gp.t; q < L.caps.CV; q += NT) {
             S.vkey[q] = -1;
             S.vlab[q] = INF_BITS;
         }
-        for (int q = lane; q < L.caps.CF; q += 32) {
+        for (int q = gp.t; q < L.caps.CF; q += NT) {
             S.fkey[q] = -1;
             S.fhead[q] = -1;
         }
     }
-    __syncwarp();
+    gp.sync();
     unsigned long long cnt[4] = {0, 0, 0, 0};
     while (true) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(L.workCounter, 1);
-        item = __shfl_sync(FULL, item, 0);
+        if (gp.t == 0) ctl->item = atomicAdd(L.workCounter, 1);
+        gp.sync();
+        const int item = ctl->item;
+        gp.sync();
         int nItems = L.nSrc;
         if (L.itemCountDev) nItems = min(nItems, *(volatile const int*)L.itemCountDev);
         if (item >= nItems) break;
         int si = L.order ? L.order[item] : item;
-        solve_source(L, S, ctl, si, lane, cnt);
-        reset_slot(S, L.caps, ctl, lane);
+        solve_source<G>(L, S, ctl, si, gp, cnt);
+        reset_slot<G>(S, L.caps, ctl, gp);
     }
-    if (lane == 0 && L.counters) {
+    if (gp.t == 0 && L.counters) {
         for (int k = 0; k < 4; ++k)
             if (cnt[k]) atomicAdd(&L.counters[k], cnt[k]);
     }
@@ -1529,42 +1622,51 @@ void cssg_geo_init_scratch(void* scratch, size_t slotBytes, int nSlots, const Ge
 
 size_t cssg_geo_smem_per_warp(const GeoCaps& c) { return smem_per_warp(c); }
 
-void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
+template <int G>
+void launch_groups(GeoLaunch L, cudaStream_t s)
 {
-    const size_t per = smem_per_warp(L.caps);
+    // groups of G warps, each solving one source at a time in its own slot; a block holds gpb groups
+    const size_t per = smem_per_warp(L.caps);  // tables of one group
     const size_t budget = 200 * 1024;
     const int wmax = (L.wpbMax > 0 && L.wpbMax < 8) ? L.wpbMax : 8;
-    int wpb = wmax;
+    int gpb = std::max(1, wmax / G);
     size_t smem = 0;
     L.smemTables = per <= budget ? 1 : 0;
     if (L.smemTables) {
-        wpb = (int)std::min<size_t>(wmax, budget / per);
-        smem = per * wpb;
+        gpb = (int)std::max<size_t>(1, std::min<size_t>(gpb, budget / per));
+        smem = per * gpb;
         static size_t configured = 48 * 1024;
         if (smem > configured) {
-            cudaFuncSetAttribute(geodesic_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
+            cudaFuncSetAttribute(geodesic_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
             configured = budget;
         }
     }
-    // spread the warps evenly over the SMs: sources are FP64-pipe bound per SM, so an SM holding two blocks while
+    // spread the groups evenly over the SMs: sources are FP64-pipe bound per SM, so an SM holding two blocks while
     // another holds one would take twice as long.  Full occupancy = sms * bps blocks; fewer slots than that get
-    // fewer warps per block, not fewer blocks.
+    // fewer groups per block, not fewer blocks.
     int dev = 0, sms = 1, bps = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (L.warpsPerSM > 0) L.nSlots = std::min<long long>(L.nSlots, (long long)sms * L.warpsPerSM);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, geodesic_kernel, 32 * wpb, smem);
+    if (L.warpsPerSM > 0) L.nSlots = (int)std::min<long long>(L.nSlots, std::max<long long>(1, (long long)sms * L.warpsPerSM / G));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, geodesic_kernel<G>, 32 * G * gpb, smem);
     bps = std::max(bps, 1);
     const long long full = (long long)sms * bps;
     int blocks;
-    if ((long long)L.nSlots >= full * wpb) {
-        blocks = (L.nSlots + wpb - 1) / wpb;
+    if ((long long)L.nSlots >= full * gpb) {
+        blocks = (L.nSlots + gpb - 1) / gpb;
     } else {
-        wpb = (int)((L.nSlots + full - 1) / full);  // warps per block; warps past nSlots return at once
-        if (L.smemTables) smem = per * wpb;
+        gpb = (int)((L.nSlots + full - 1) / full);  // groups per block; groups past nSlots return at once
+        if (L.smemTables) smem = per * gpb;
         blocks = (int)full;
     }
-    geodesic_kernel<<<blocks, 32 * wpb, smem, s>>>(L);
+    geodesic_kernel<G><<<blocks, 32 * G * gpb, smem, s>>>(L);
+}
+
+void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
+{
+    if (L.groupWarps == 4) launch_groups<4>(L, s);
+    else if (L.groupWarps == 2) launch_groups<2>(L, s);
+    else launch_groups<1>(L, s);
 }
 
 // --------------------------------------------------------------------------------------------------------------------

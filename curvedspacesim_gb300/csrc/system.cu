@@ -378,6 +378,7 @@ struct cssg_system {
     double tuneDelta = 1.0;
     int tuneWpb = 8;
     int tuneWarpsPerSM = 0;  // 0: every slot
+    int tuneGroup = 1;       // warps per source (1, 2, 4)
     bool tuneLpt = false;    // sources in decreasing order of their last cost (longest first) instead of cell order
     int* srcCost = nullptr;  // n: work of each source in the last force evaluation
     int* lptOrder = nullptr; // n
@@ -502,6 +503,7 @@ void launch_forces(cssg_system* s)
     L.deltaScale = s->tuneDelta;
     L.wpbMax = s->tuneWpb;
     L.warpsPerSM = s->tuneWarpsPerSM;
+    L.groupWarps = s->tuneGroup;
     L.srcCost = s->srcCost;
     if (s->tuneLpt) {
         cudaMemsetAsync(s->lptBuckets, 0, 64 * sizeof(int), st);
@@ -999,13 +1001,15 @@ void drop_graph(cssg_system* s)
 }  // namespace
 
 extern "C" int cssg_system_set_tuning(cssg_system* s, double delta_scale, int warps_per_block, int mid_slots,
-                                      int warps_per_sm, int lpt_order)
+                                      int warps_per_sm, int lpt_order, int warps_per_source)
 {
-    if (!s || !(delta_scale > 0) || warps_per_block < 1 || warps_per_block > 8 || warps_per_sm < 0) {
+    if (!s || !(delta_scale > 0) || warps_per_block < 1 || warps_per_block > 8 || warps_per_sm < 0 ||
+        (warps_per_source != 1 && warps_per_source != 2 && warps_per_source != 4)) {
         cssg_set_error("cssg_system_set_tuning: bad arguments (delta_scale > 0, 1 <= warps_per_block <= 8, "
-                       "warps_per_sm >= 0)");
+                       "warps_per_sm >= 0, warps_per_source in {1, 2, 4})");
         return CSSG_ERR_ARG;
     }
+    s->tuneGroup = warps_per_source;
     s->tuneDelta = delta_scale;
     s->tuneWpb = warps_per_block;
     if (mid_slots > 0) s->nMidSlots = std::min(mid_slots, s->midSlotsMax);
@@ -1026,15 +1030,16 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     int sms = 0;
     CSSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->ctx->device));
     const double deltas[] = {0.5, 1.0, 2.0, 4.0};
-    // (warps per block, warps per SM cap, longest-first order)
-    const int shapes[][3] = {{8, 0, 0}, {4, 0, 0}, {8, 0, 1}, {8, 8, 1}, {8, 4, 1}};
+    // (warps per block, warps per SM cap, longest-first order, warps per source)
+    const int shapes[][4] = {{8, 0, 0, 1}, {4, 0, 0, 1}, {8, 0, 1, 1}, {8, 8, 1, 1},
+                             {8, 4, 1, 1}, {8, 0, 1, 2}, {8, 0, 1, 4}};
     std::vector<int> mids{s->midSlotsMax};
     if (s->midSlotsMax > sms * 8) mids.push_back(sms * 8);
     cudaEvent_t e0, e1;
     CSSG_CUDA(cudaEventCreate(&e0));
     CSSG_CUDA(cudaEventCreate(&e1));
     double best = 1e300, bd = s->tuneDelta;
-    int bw = s->tuneWpb, bm = s->nMidSlots, bc = s->tuneWarpsPerSM;
+    int bw = s->tuneWpb, bm = s->nMidSlots, bc = s->tuneWarpsPerSM, bg = s->tuneGroup;
     bool bl = s->tuneLpt;
     const bool timing = s->timing;
     s->timing = false;
@@ -1049,6 +1054,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
                 s->tuneWpb = sh[0];
                 s->tuneWarpsPerSM = sh[1];
                 s->tuneLpt = sh[2] != 0;
+                s->tuneGroup = sh[3];
                 s->nMidSlots = m;
                 launch_forces(s);  // warm-up of this configuration
                 cudaEventRecord(e0, st);
@@ -1071,6 +1077,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
                     bw = sh[0];
                     bc = sh[1];
                     bl = sh[2] != 0;
+                    bg = sh[3];
                     bm = m;
                 }
             }
@@ -1081,6 +1088,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     s->tuneWpb = bw;
     s->tuneWarpsPerSM = bc;
     s->tuneLpt = bl;
+    s->tuneGroup = bg;
     s->nMidSlots = bm;
     drop_graph(s);
     // leave the forces of the current state computed with the chosen configuration
@@ -1100,6 +1108,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
         result_host[3] = bc;
         result_host[4] = bl ? 1 : 0;
         result_host[5] = best / reps;
+        result_host[6] = bg;
     }
     return CSSG_OK;
 }

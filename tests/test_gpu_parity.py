@@ -111,12 +111,15 @@ def _system(api, ctx, V, F, n, seed, integrator, sigma, submesh, range_, dt, T):
     return S, f, b, vel
 
 
-def test_nve_all_to_all_matches_oracle(gpu, oracle_mod):
-    """Icosphere-4, N=100, sigma=0.2, all-to-all, velocity Verlet dt=0.005, 100 steps: positions within 1e-5."""
+@pytest.mark.parametrize("group", [1, 4])
+def test_nve_all_to_all_matches_oracle(gpu, oracle_mod, group):
+    """Icosphere-4, N=100, sigma=0.2, all-to-all, velocity Verlet dt=0.005, 100 steps: positions within 1e-5
+    (one warp per source, and four warps per source)."""
     api, ctx = gpu
     V, F = ms.icosphere(4)
     n, sigma, dt = 100, 0.2, 0.005
     S, f, b, vel = _system(api, ctx, V, F, n, 1, "nve", sigma, False, 0.0, dt, 0.1)
+    S.set_tuning(1.0, 8, 0, 0, False, group)
     S.step(100, graph=True)
     bits, cnt = S.check()
     assert bits == 0, cnt
@@ -226,7 +229,8 @@ def test_autotune_keeps_results(gpu, oracle_mod):
     assert tune["delta_scale"] in (0.5, 1.0, 2.0, 4.0) and tune["warps_per_block"] in (4, 8)
     f1 = S.get_state()[3]
     np.testing.assert_allclose(f1, f0, rtol=0, atol=1e-12)
-    for args in ((0.5, 4, 0, 0, False), (2.0, 8, 0, 2, True), (1.0, 8, 0, 4, True)):
+    for args in ((0.5, 4, 0, 0, False, 1), (2.0, 8, 0, 2, True, 1), (1.0, 8, 0, 4, True, 1), (1.0, 8, 0, 0, True, 2),
+                 (4.0, 8, 0, 0, False, 4), (0.5, 4, 0, 8, True, 4)):
         S.set_tuning(*args)
         S.compute_forces()
         S.compute_forces()  # the second evaluation uses the longest-first order built from the first
