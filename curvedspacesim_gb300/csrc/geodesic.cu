@@ -729,6 +729,10 @@ __device__ __noinline__ double target_query(const DevMesh& M, const Slot& S, con
 
 // A source group: the G warps that solve one source together (G = 1, 2 or 4).  With G = 1 the group is a warp and
 // synchronises with __syncwarp; otherwise with a named barrier of 32 G threads (ids 1..8, one per group of the block).
+// The barrier is the non-aligned form (barrier.sync): the groups of one block run different sources and so reach
+// their barriers at different instructions, which the aligned form (bar.sync) does not allow.  Every thread of a
+// group executes the same sequence of group barriers: all loops and early exits around them test values that the
+// group read from its shared control block after the previous barrier.
 template <int G>
 struct Grp {
     static constexpr int NT = 32 * G;
@@ -740,8 +744,12 @@ struct Grp {
     int* redI;    // G ints
     __device__ __forceinline__ void sync() const
     {
-        if (G == 1) __syncwarp();
-        else asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(NT) : "memory");
+        if (G == 1) {
+            __syncwarp();
+        } else {
+            __syncwarp();
+            asm volatile("barrier.sync %0, %1;" ::"r"(bar), "r"(NT) : "memory");
+        }
     }
     __device__ __forceinline__ double min(double x) const
     {
