@@ -1177,7 +1177,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                             int y = __shfl_up_sync(FULL, incl, o);
                             if (lane >= o) incl += y;
                         }
-                        gp.sync();
+                        __syncwarp();  // the first warp alone: a warp barrier, not the group's
                         if (q < nP) S.lpre[q] = run + incl - x;
                         run += __shfl_sync(FULL, incl, 31);
                     }
