@@ -162,7 +162,7 @@ struct GeoLaunch {
     double deltaScale;           // band width = deltaScale * the system's delta (<= 0: 1)
     int wpbMax;                  // largest warps per block (CTA size / 32; <= 0: 8)
     int warpsPerSM;              // > 0: at most this many source warps per SM (the rest of the slots stay idle)
-    int groupWarps;              // warps that solve one source together: 1 (default), 2 or 4
+    int groupWarps;              // warps that solve one source together: 1 (default), 2, 4 or 8
     int* srcCost;                // nullable: work of each source (windows + launches + rounds), for the next order
     int smemTables;              // set by cssg_launch_geodesic: hash tables in shared memory
 };

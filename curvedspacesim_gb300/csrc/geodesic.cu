@@ -727,7 +727,7 @@ __device__ __noinline__ double target_query(const DevMesh& M, const Slot& S, con
     return best;
 }
 
-// A source group: the G warps that solve one source together (G = 1, 2 or 4).  With G = 1 the group is a warp and
+// A source group: the G warps that solve one source together (G = 1, 2, 4 or 8).  With G = 1 the group is a warp and
 // synchronises with __syncwarp; otherwise with a named barrier of 32 G threads (ids 1..8, one per group of the block).
 // The barrier is the non-aligned form (barrier.sync): the groups of one block run different sources and so reach
 // their barriers at different instructions, which the aligned form (bar.sync) does not allow.  Every thread of a
@@ -1471,8 +1471,8 @@ __global__ void __launch_bounds__(256) geodesic_kernel(GeoLaunch L)
     constexpr int NT = 32 * G;
     __shared__ WarpCtl ctls[8];
     __shared__ int tasks[8 * (kTaskP + kTaskC)];
-    __shared__ double redD[8][4];
-    __shared__ int redI[8][4];
+    __shared__ double redD[8][8];
+    __shared__ int redI[8][8];
     extern __shared__ __align__(16) char dyn[];
     const int gib = threadIdx.x / NT;
     const int group = blockIdx.x * (blockDim.x / NT) + gib;
@@ -1672,7 +1672,8 @@ void launch_groups(GeoLaunch L, cudaStream_t s)
 
 void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
 {
-    if (L.groupWarps == 4) launch_groups<4>(L, s);
+    if (L.groupWarps == 8) launch_groups<8>(L, s);
+    else if (L.groupWarps == 4) launch_groups<4>(L, s);
     else if (L.groupWarps == 2) launch_groups<2>(L, s);
     else launch_groups<1>(L, s);
 }

@@ -1004,9 +1004,9 @@ extern "C" int cssg_system_set_tuning(cssg_system* s, double delta_scale, int wa
                                       int warps_per_sm, int lpt_order, int warps_per_source)
 {
     if (!s || !(delta_scale > 0) || warps_per_block < 1 || warps_per_block > 8 || warps_per_sm < 0 ||
-        (warps_per_source != 1 && warps_per_source != 2 && warps_per_source != 4)) {
+        (warps_per_source != 1 && warps_per_source != 2 && warps_per_source != 4 && warps_per_source != 8)) {
         cssg_set_error("cssg_system_set_tuning: bad arguments (delta_scale > 0, 1 <= warps_per_block <= 8, "
-                       "warps_per_sm >= 0, warps_per_source in {1, 2, 4})");
+                       "warps_per_sm >= 0, warps_per_source in {1, 2, 4, 8})");
         return CSSG_ERR_ARG;
     }
     s->tuneGroup = warps_per_source;
@@ -1032,7 +1032,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     const double deltas[] = {0.5, 1.0, 2.0, 4.0};
     // (warps per block, warps per SM cap, longest-first order, warps per source)
     const int shapes[][4] = {{8, 0, 0, 1}, {4, 0, 0, 1}, {8, 0, 1, 1}, {8, 8, 1, 1},
-                             {8, 4, 1, 1}, {8, 0, 1, 2}, {8, 0, 1, 4}};
+                             {8, 4, 1, 1}, {8, 0, 1, 2}, {8, 0, 1, 4}, {8, 0, 1, 8}};
     std::vector<int> mids{s->midSlotsMax};
     if (s->midSlotsMax > sms * 8) mids.push_back(sms * 8);
     cudaEvent_t e0, e1;

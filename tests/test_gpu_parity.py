@@ -111,7 +111,7 @@ def _system(api, ctx, V, F, n, seed, integrator, sigma, submesh, range_, dt, T):
     return S, f, b, vel
 
 
-@pytest.mark.parametrize("group", [1, 4])
+@pytest.mark.parametrize("group", [1, 4, 8])
 def test_nve_all_to_all_matches_oracle(gpu, oracle_mod, group):
     """Icosphere-4, N=100, sigma=0.2, all-to-all, velocity Verlet dt=0.005, 100 steps: positions within 1e-5
     (one warp per source, and four warps per source)."""
@@ -230,7 +230,7 @@ def test_autotune_keeps_results(gpu, oracle_mod):
     f1 = S.get_state()[3]
     np.testing.assert_allclose(f1, f0, rtol=0, atol=1e-12)
     for args in ((0.5, 4, 0, 0, False, 1), (2.0, 8, 0, 2, True, 1), (1.0, 8, 0, 4, True, 1), (1.0, 8, 0, 0, True, 2),
-                 (4.0, 8, 0, 0, False, 4), (0.5, 4, 0, 8, True, 4)):
+                 (4.0, 8, 0, 0, False, 4), (0.5, 4, 0, 8, True, 4), (2.0, 8, 0, 0, True, 8)):
         S.set_tuning(*args)
         S.compute_forces()
         S.compute_forces()  # the second evaluation uses the longest-first order built from the first
