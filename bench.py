@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 
 from curvedspacesim_gb300 import meshes as ms  # noqa: E402
 
-# algorithmic work constants of the geodesic+force kernel ("Roofline accounting")
+# algorithmic work constants of the geodesic+force kernel (roofline accounting of the propagation)
 FLOPS_PER_WINDOW = 250          # FP64 flops of one window step (trim, target/vertex updates, two children)
 BYTES_PER_SOURCE = 4 + 24 + 24 + 24   # read face, barycentrics, R3 position; write force
 BYTES_PER_CANDIDATE = 4 + 4 + 24 + 24  # read index, face, barycentrics, R3 position
