@@ -341,6 +341,13 @@ extern "C" int cssg_ctx_create(int device, void* stream, cssg_ctx** out)
         return CSSG_ERR_ARG;
     }
     CSSG_CUDA(cudaSetDevice(device));
+    {
+        // the propagation kernels call out-of-line helpers and need close to 1 KB of stack per thread (ptxas
+        // reports up to ~1000 bytes cumulative); give them headroom above the 1 KB default
+        size_t stack = 0;
+        CSSG_CUDA(cudaDeviceGetLimit(&stack, cudaLimitStackSize));
+        if (stack < 4096) CSSG_CUDA(cudaDeviceSetLimit(cudaLimitStackSize, 4096));
+    }
     cssg_ctx* c = new cssg_ctx();
     c->device = device;
     if (stream) {
