@@ -35,8 +35,10 @@ def test_oracle_fire_converges_and_stress_is_symmetric(oracle_mod):
 
 
 @pytest.mark.gpu
-def test_fire_matches_oracle(gpu, oracle_mod):
-    """20 iterations step for step (sums differ only in order: tolerance 1e-9), then a full minimisation converges."""
+@pytest.mark.parametrize("group", [1, 2])
+def test_fire_matches_oracle(gpu, oracle_mod, group):
+    """20 iterations step for step (sums differ only in order: tolerance 1e-9), then a full minimisation converges
+    (one and two warps per source)."""
     api, ctx = gpu
     V, F, f, b, vel = _setup()
     n, sigma = len(f), 0.4
@@ -47,6 +49,7 @@ def test_fire_matches_oracle(gpu, oracle_mod):
                         cutoff=sigma, dt=0.01)
     S = api.System(ctx, M, n, p)
     S.set_state(f, b, vel, np.zeros((n, 3)))
+    S.set_tuning(1.0, 8, 0, 0, False, group)
     res = S.fire(maximum_iterations=20, force_cutoff=1e-300, reset=True)
     fo, bo, vo, fco, st, it, fmax, err = OM.fire(f, b, vel, np.zeros((n, 3)), prm, maximum_iterations=20,
                                                  force_cutoff=1e-300)

@@ -180,9 +180,10 @@ def test_pair_sets_identical(gpu, oracle_mod):
     np.testing.assert_allclose(fg, fo, atol=1e-11)
 
 
-def test_batched_systems_match_oracle(gpu, oracle_mod):
+@pytest.mark.parametrize("group", [1, 4])
+def test_batched_systems_match_oracle(gpu, oracle_mod, group):
     """Three independent systems (different meshes, counts and ranges) in one system object: each must evolve
-    exactly as it does alone (velocity Verlet, cell lists, patches, 20 steps)."""
+    exactly as it does alone (velocity Verlet, cell lists, patches, 20 steps; one and four warps per source)."""
     api, ctx = gpu
     rng = np.random.default_rng(7)
     specs = [ms.icosphere(3), ms.torus(50, 25, 3.0, 1.0), ms.ellipsoid(3, (1.5, 1.0, 0.7))]
@@ -199,6 +200,7 @@ def test_batched_systems_match_oracle(gpu, oracle_mod):
     S = api.System(ctx, meshes, counts, params)
     S.set_state(np.concatenate([s[2] for s in states]), np.concatenate([s[3] for s in states]),
                 np.concatenate([s[4] for s in states]), np.zeros((sum(counts), 3)))
+    S.set_tuning(2.0, 8, 0, 0, True, group)
     S.step(20, graph=True)
     bits, cnt = S.check()
     assert bits == 0, cnt
