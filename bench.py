@@ -309,9 +309,10 @@ def run_ours(args, cfg):
         fields = args.tuning.split(",")
         d, w, m, cap, lpt = fields[:5]
         g = int(fields[5]) if len(fields) > 5 else 1
-        S.set_tuning(float(d), int(w), int(m), int(cap), bool(int(lpt)), g)
+        wide = bool(int(fields[6])) if len(fields) > 6 else False
+        S.set_tuning(float(d), int(w), int(m), int(cap), bool(int(lpt)), g, wide)
         tune = {"delta_scale": float(d), "warps_per_block": int(w), "mid_slots": int(m), "warps_per_sm": int(cap),
-                "lpt_order": bool(int(lpt)), "warps_per_source": g, "source": "--tuning"}
+                "lpt_order": bool(int(lpt)), "warps_per_source": g, "wide_registers": wide, "source": "--tuning"}
         S.step(1, graph=not args.profile)
         torch.cuda.synchronize()
     elif not args.no_autotune:
@@ -593,7 +594,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (band width 1, 8 warps)")
     ap.add_argument("--tuning", default="",
                     help="explicit tuning instead of the autotuner: delta_scale,warps_per_block,mid_slots,"
-                         "warps_per_sm,lpt[,warps_per_source] (e.g. 4,8,0,8,1,1)")
+                         "warps_per_sm,lpt[,warps_per_source[,wide_registers]] (e.g. 4,8,0,0,1,2,0)")
     ap.add_argument("--profile", action="store_true",
                     help="minimal run for ncu: warm-up steps, then one step without graph replay, no other legs")
     args = ap.parse_args()

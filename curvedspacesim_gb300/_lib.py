@@ -107,7 +107,7 @@ def load(build_if_missing: bool = True):
     L.cssg_system_device_state.argtypes = [P, PP, PP, PP, PP]
     L.cssg_system_step.argtypes = [P, I, I]
     L.cssg_system_compute_forces.argtypes = [P]
-    L.cssg_system_set_tuning.argtypes = [P, D, I, I, I, I, I]
+    L.cssg_system_set_tuning.argtypes = [P, D, I, I, I, I, I, I]
     L.cssg_system_autotune.argtypes = [P, I, P]
     L.cssg_system_fire.argtypes = [P, ctypes.POINTER(cssg_fire_params), I, P]
     L.cssg_system_stress.argtypes = [P, P]

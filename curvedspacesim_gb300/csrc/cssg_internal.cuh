@@ -163,6 +163,7 @@ struct GeoLaunch {
     int wpbMax;                  // largest warps per block (CTA size / 32; <= 0: 8)
     int warpsPerSM;              // > 0: at most this many source warps per SM (the rest of the slots stay idle)
     int groupWarps;              // warps that solve one source together: 1 (default), 2, 4 or 8
+    int wideRegs;                // 1: the kernel build with up to 255 registers per thread (fewer warps per SM)
     int* srcCost;                // nullable: work of each source (windows + launches + rounds), for the next order
     int smemTables;              // set by cssg_launch_geodesic: hash tables in shared memory
 };

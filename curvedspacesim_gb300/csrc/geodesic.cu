@@ -1465,8 +1465,10 @@ __device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, const 
 }
 
 // One source group (G warps) per slot; groups pull sources from the work counter until none are left.
-template <int G>
-__global__ void __launch_bounds__(256) geodesic_kernel(GeoLaunch L)
+// MINB = 2 lets ptxas use up to 128 registers per thread (two full blocks per SM); MINB = 1 up to 255 (no spills,
+// at most 8 warps per SM).  The autotuner picks.
+template <int G, int MINB>
+__global__ void __launch_bounds__(256, MINB) geodesic_kernel(GeoLaunch L)
 {
     constexpr int NT = 32 * G;
     __shared__ WarpCtl ctls[8];
@@ -1630,7 +1632,7 @@ void cssg_geo_init_scratch(void* scratch, size_t slotBytes, int nSlots, const Ge
 
 size_t cssg_geo_smem_per_warp(const GeoCaps& c) { return smem_per_warp(c); }
 
-template <int G>
+template <int G, int MINB>
 void launch_groups(GeoLaunch L, cudaStream_t s)
 {
     // groups of G warps, each solving one source at a time in its own slot; a block holds gpb groups
@@ -1645,7 +1647,7 @@ void launch_groups(GeoLaunch L, cudaStream_t s)
         smem = per * gpb;
         static size_t configured = 48 * 1024;
         if (smem > configured) {
-            cudaFuncSetAttribute(geodesic_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
+            cudaFuncSetAttribute(geodesic_kernel<G, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
             configured = budget;
         }
     }
@@ -1656,7 +1658,7 @@ void launch_groups(GeoLaunch L, cudaStream_t s)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (L.warpsPerSM > 0) L.nSlots = (int)std::min<long long>(L.nSlots, std::max<long long>(1, (long long)sms * L.warpsPerSM / G));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, geodesic_kernel<G>, 32 * G * gpb, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, geodesic_kernel<G, MINB>, 32 * G * gpb, smem);
     bps = std::max(bps, 1);
     const long long full = (long long)sms * bps;
     int blocks;
@@ -1667,15 +1669,22 @@ void launch_groups(GeoLaunch L, cudaStream_t s)
         if (L.smemTables) smem = per * gpb;
         blocks = (int)full;
     }
-    geodesic_kernel<G><<<blocks, 32 * G * gpb, smem, s>>>(L);
+    geodesic_kernel<G, MINB><<<blocks, 32 * G * gpb, smem, s>>>(L);
 }
 
 void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
 {
-    if (L.groupWarps == 8) launch_groups<8>(L, s);
-    else if (L.groupWarps == 4) launch_groups<4>(L, s);
-    else if (L.groupWarps == 2) launch_groups<2>(L, s);
-    else launch_groups<1>(L, s);
+    if (L.wideRegs) {
+        if (L.groupWarps == 8) launch_groups<8, 1>(L, s);
+        else if (L.groupWarps == 4) launch_groups<4, 1>(L, s);
+        else if (L.groupWarps == 2) launch_groups<2, 1>(L, s);
+        else launch_groups<1, 1>(L, s);
+    } else {
+        if (L.groupWarps == 8) launch_groups<8, 2>(L, s);
+        else if (L.groupWarps == 4) launch_groups<4, 2>(L, s);
+        else if (L.groupWarps == 2) launch_groups<2, 2>(L, s);
+        else launch_groups<1, 2>(L, s);
+    }
 }
 
 // --------------------------------------------------------------------------------------------------------------------

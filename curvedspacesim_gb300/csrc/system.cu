@@ -378,7 +378,8 @@ struct cssg_system {
     double tuneDelta = 1.0;
     int tuneWpb = 8;
     int tuneWarpsPerSM = 0;  // 0: every slot
-    int tuneGroup = 1;       // warps per source (1, 2, 4)
+    int tuneGroup = 1;       // warps per source (1, 2, 4, 8)
+    int tuneWide = 0;        // 1: the 255-register kernel build
     bool tuneLpt = false;    // sources in decreasing order of their last cost (longest first) instead of cell order
     int* srcCost = nullptr;  // n: work of each source in the last force evaluation
     int* lptOrder = nullptr; // n
@@ -504,6 +505,7 @@ void launch_forces(cssg_system* s)
     L.wpbMax = s->tuneWpb;
     L.warpsPerSM = s->tuneWarpsPerSM;
     L.groupWarps = s->tuneGroup;
+    L.wideRegs = s->tuneWide;
     L.srcCost = s->srcCost;
     if (s->tuneLpt) {
         cudaMemsetAsync(s->lptBuckets, 0, 64 * sizeof(int), st);
@@ -1001,7 +1003,7 @@ void drop_graph(cssg_system* s)
 }  // namespace
 
 extern "C" int cssg_system_set_tuning(cssg_system* s, double delta_scale, int warps_per_block, int mid_slots,
-                                      int warps_per_sm, int lpt_order, int warps_per_source)
+                                      int warps_per_sm, int lpt_order, int warps_per_source, int wide_registers)
 {
     if (!s || !(delta_scale > 0) || warps_per_block < 1 || warps_per_block > 8 || warps_per_sm < 0 ||
         (warps_per_source != 1 && warps_per_source != 2 && warps_per_source != 4 && warps_per_source != 8)) {
@@ -1010,6 +1012,7 @@ extern "C" int cssg_system_set_tuning(cssg_system* s, double delta_scale, int wa
         return CSSG_ERR_ARG;
     }
     s->tuneGroup = warps_per_source;
+    s->tuneWide = wide_registers != 0;
     s->tuneDelta = delta_scale;
     s->tuneWpb = warps_per_block;
     if (mid_slots > 0) s->nMidSlots = std::min(mid_slots, s->midSlotsMax);
@@ -1030,16 +1033,17 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     int sms = 0;
     CSSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->ctx->device));
     const double deltas[] = {0.5, 1.0, 2.0, 4.0};
-    // (warps per block, warps per SM cap, longest-first order, warps per source)
-    const int shapes[][4] = {{8, 0, 0, 1}, {4, 0, 0, 1}, {8, 0, 1, 1}, {8, 8, 1, 1},
-                             {8, 4, 1, 1}, {8, 0, 1, 2}, {8, 0, 1, 4}, {8, 0, 1, 8}};
+    // (warps per block, warps per SM cap, longest-first order, warps per source, wide registers)
+    const int shapes[][5] = {{8, 0, 0, 1, 0}, {4, 0, 0, 1, 0}, {8, 0, 1, 1, 0}, {8, 8, 1, 1, 0}, {8, 4, 1, 1, 0},
+                             {8, 0, 1, 2, 0}, {8, 0, 1, 4, 0}, {8, 0, 1, 8, 0}, {8, 0, 1, 1, 1}, {8, 0, 1, 2, 1},
+                             {8, 0, 1, 4, 1}};
     std::vector<int> mids{s->midSlotsMax};
     if (s->midSlotsMax > sms * 8) mids.push_back(sms * 8);
     cudaEvent_t e0, e1;
     CSSG_CUDA(cudaEventCreate(&e0));
     CSSG_CUDA(cudaEventCreate(&e1));
     double best = 1e300, bd = s->tuneDelta;
-    int bw = s->tuneWpb, bm = s->nMidSlots, bc = s->tuneWarpsPerSM, bg = s->tuneGroup;
+    int bw = s->tuneWpb, bm = s->nMidSlots, bc = s->tuneWarpsPerSM, bg = s->tuneGroup, bx = s->tuneWide;
     bool bl = s->tuneLpt;
     const bool timing = s->timing;
     s->timing = false;
@@ -1055,6 +1059,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
                 s->tuneWarpsPerSM = sh[1];
                 s->tuneLpt = sh[2] != 0;
                 s->tuneGroup = sh[3];
+                s->tuneWide = sh[4];
                 s->nMidSlots = m;
                 launch_forces(s);  // warm-up of this configuration
                 cudaEventRecord(e0, st);
@@ -1078,6 +1083,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
                     bc = sh[1];
                     bl = sh[2] != 0;
                     bg = sh[3];
+                    bx = sh[4];
                     bm = m;
                 }
             }
@@ -1089,6 +1095,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     s->tuneWarpsPerSM = bc;
     s->tuneLpt = bl;
     s->tuneGroup = bg;
+    s->tuneWide = bx;
     s->nMidSlots = bm;
     drop_graph(s);
     // leave the forces of the current state computed with the chosen configuration
@@ -1109,6 +1116,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
         result_host[4] = bl ? 1 : 0;
         result_host[5] = best / reps;
         result_host[6] = bg;
+        result_host[7] = bx;
     }
     return CSSG_OK;
 }

@@ -185,16 +185,18 @@ int cssg_system_stress(cssg_system* sys, double* stress_host);
  * (<= the number allocated at creation; <= 0 keeps the current value); warps_per_sm: > 0 caps the source warps of
  * the regular pass per SM (0: all slots); lpt_order: 1 processes sources longest first by their cost in the last
  * force evaluation, 0 in cell order; warps_per_source: 1, 2, 4 or 8 warps solve one source together (a few sources
- * on many SMs want more).  Results do not depend on these, only the work and its balance do.  Drops the captured step
- * graph. */
+ * on many SMs want more); wide_registers: 1 selects the kernel build with up to 255 registers per thread (no
+ * register spills, at most 8 warps per SM).  Results do not depend on these, only the work and its balance do.
+ * Drops the captured step graph. */
 int cssg_system_set_tuning(cssg_system* sys, double delta_scale, int warps_per_block, int mid_slots, int warps_per_sm,
-                           int lpt_order, int warps_per_source);
+                           int lpt_order, int warps_per_source, int wide_registers);
 /* Autotuner: times `reps` force evaluations on the current state for each candidate (delta_scale in {0.5, 1, 2, 4}
- * x (warps_per_block, warps_per_sm, lpt_order, warps_per_source) in {(8,0,0,1), (4,0,0,1), (8,0,1,1), (8,8,1,1),
- * (8,4,1,1), (8,0,1,2), (8,0,1,4), (8,0,1,8)} x medium slots in {allocated, 8 per SM}), rejects candidates that overflow a
- * table, keeps the fastest and recomputes the forces with it.  result_host (nullable, 7 doubles) = {delta_scale,
- * warps_per_block, mid_slots, warps_per_sm, lpt_order, ms per force evaluation, warps_per_source}.  Synchronises
- * the context's stream. */
+ * x (warps_per_block, warps_per_sm, lpt_order, warps_per_source, wide_registers) in {(8,0,0,1,0), (4,0,0,1,0),
+ * (8,0,1,1,0), (8,8,1,1,0), (8,4,1,1,0), (8,0,1,2,0), (8,0,1,4,0), (8,0,1,8,0), (8,0,1,1,1), (8,0,1,2,1),
+ * (8,0,1,4,1)} x medium slots in {allocated, 8 per SM}), rejects candidates that overflow a table, keeps the fastest
+ * and recomputes the forces with it.  result_host (nullable, 8 doubles) = {delta_scale, warps_per_block, mid_slots,
+ * warps_per_sm, lpt_order, ms per force evaluation, warps_per_source, wide_registers}.  Synchronises the context's
+ * stream. */
 int cssg_system_autotune(cssg_system* sys, int reps, double* result_host);
 /* Error summary since the last call (synchronises): OR of (1 << CSSG_ST_*) over walks and sources, and counters
  * out_host[4] = {walk crossings, windows processed, vertex launches, in-range pairs} (nullable). */
