@@ -1,4 +1,5 @@
-// Exact geodesic distances + start tangents + pair forces: one warp per source particle, persistent warps.
+// Exact geodesic distances + start tangents + pair forces: one source group (1, 2, 4 or 8 warps) per source
+// particle, persistent groups.
 //
 // Replaces, per timestep, the reference's per-source loop in simpleModel::findNeighbors
 // (src/models/simpleModel.cpp:68-112): candidate search (cellListNeighborStructure::constructCandidateNeighborList,
@@ -22,12 +23,15 @@
 //     improves; windows never re-enter the source face (the chord inside it is optimal);
 //   * start tangents ride along: windows from the source carry the rotation of their frame into the source face
 //     frame, windows from a vertex pseudo-source carry that vertex's start direction.
-// The lanes of a warp process a round of windows in parallel; vertex labels are updated with 64-bit atomicMin on
-// the bit patterns of non-negative doubles and the start direction of a label is written, after a __syncwarp, by
-// the lane whose proposal survived.  Processing order only affects how much gets pruned, not the result.
+// Order: distance-banded rounds.  A round processes every window and pseudo-source launch whose key (a lower bound of
+// its distances) lies within a band above the smallest queued key, including those created inside the band, then
+// moves to the next band.  The threads of a group process batches of windows in parallel; vertex labels are
+// updated with 64-bit atomicMin on the bit patterns of non-negative doubles and the start direction of a label is
+// written, after a group barrier, by the thread whose proposal survived.  Processing order only affects how much
+// gets pruned, not the result.
 //
-// Roofline: this kernel is FP64 latency/issue bound (scalar double arithmetic on irregular, data-dependent work);
-// its memory footprint per source is a few KB of L2-resident scratch plus mesh reads.
+// Roofline: this kernel is bound by the FP64 pipe and latency (scalar double arithmetic on irregular,
+// data-dependent work); its per-source footprint is a few KB of scratch plus mesh reads, mostly L2-resident.
 #include <math_constants.h>
 
 #include <algorithm>
@@ -622,24 +626,9 @@ __device__ void child_task(const DevMesh& M, const Slot& S, const GeoCaps& C, co
     }
 }
 
-__device__ __forceinline__ double warp_min(double x)
-{
-    for (int o = 16; o > 0; o >>= 1) x = fmin(x, __shfl_xor_sync(FULL, x, o));
-    return x;
-}
 __device__ __forceinline__ double warp_max(double x)
 {
     for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(FULL, x, o));
-    return x;
-}
-__device__ __forceinline__ double warp_sum(double x)
-{
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
-    return x;
-}
-__device__ __forceinline__ int warp_sum_i(int x)
-{
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
     return x;
 }
 
