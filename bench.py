@@ -467,6 +467,24 @@ def run_screen(args, cfg):
     def mesh_fn(seed):
         return ms.bumpy_sphere(sub, amplitude=0.05, seed=seed)
 
+    if args.profile:
+        # minimal run for ncu: the screened path with untrained weights (the tensor-core work per pair is the same),
+        # a margin that skips nothing, three steps without graph replay
+        V, F, f, b, vel = build_inputs(cfg)
+        M = api.Mesh(V, F, device=local)
+        prm = api.make_params(cfg["integrator"], "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=cfg["range_"],
+                              submesh=cfg["submesh"], max_dist=sigma, cutoff=sigma, dt=cfg["dt"],
+                              temperature=cfg["T"])
+        S = api.System(ctx, M, n, prm)
+        S.set_screen(screen.init_params(0), 1e6)
+        S.set_state(f, b, vel, np.zeros((n, 3)))
+        S.step(max(args.warmup, 1), graph=False)
+        torch.cuda.synchronize()
+        bits, cnt = S.check()
+        print(json.dumps({"profile_run": cfg["workload"], "status_bits": bits, "counters": cnt,
+                          "screen": S.screen_counters()}), flush=True)
+        return
+
     t0 = time.perf_counter()
     X, y, _, _ = screen.generate(ctx, mesh_fn, cfg["train_seeds"], n, sigma, configs_per_seed=cfg["configs_per_seed"])
     params, _ = screen.train(ctx, X, y, steps=cfg["train_steps"], batch=8192, lr=3e-3)
