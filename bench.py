@@ -56,6 +56,8 @@ def workload_config(name):
         return dict(workload="noisy_torus1000x500_N100000_nvt_patch", mesh=("noisy_torus", 1000, 500), n=100000,
                     phi=0.5, sigma=None, integrator="nvt", submesh=True, range_=None, dt=0.001, T=0.05, seed=5,
                     cpu_subset=1000)
+    if name == "mlp_infer":
+        return dict(workload="mlp14x64x64x64x1_bf16_4M_pairs", pairs=1 << 22, mlp=True)
     if name == "torus_nvt":
         return dict(workload="torus200x100_N2000_nvt_patch", mesh=("torus", 200, 100), n=2000, sigma=0.3,
                     integrator="nvt", submesh=True, range_=0.3, dt=0.002, T=0.05, seed=2)
@@ -601,6 +603,75 @@ def run_screen(args, cfg):
         print(json.dumps(line), flush=True)
 
 
+def run_mlp(args, cfg):
+    """The screen's tensor-core inference kernel on its own: 4M feature rows (BF16, 14 features padded to 16) through
+    14->64->64->64->1 with GELU.  The input (128 MB) exceeds L2, so no flush is needed between launches.  Reports
+    pairs/s and the tensor roofline (2 * (16*64 + 64*64 + 64*64 + 64) FLOP per pair as executed)."""
+    import torch
+    from curvedspacesim_gb300 import _lib, api, screen
+    world, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    ctx = api.Context(local)
+    n = cfg["pairs"]
+    dev = f"cuda:{local}"
+    g = torch.Generator(device="cpu").manual_seed(7)
+    X = torch.randn((n, 16), generator=g).to(torch.bfloat16)
+    X[:, 14:] = 0
+    X = X.to(dev)
+    params = torch.tensor(screen.init_params(0), device=dev)
+    with ctx.use():
+        y = torch.empty(n, dtype=torch.float32, device=dev)
+        err = torch.zeros(1, dtype=torch.int32, device=dev)
+    L = _lib.load()
+    P = _lib.ctypes.c_void_p
+    torch.cuda.synchronize()
+
+    def launch():
+        rc = L.cssg_mlp_infer(ctx.h, P(X.data_ptr()), n, P(params.data_ptr()), P(y.data_ptr()), P(err.data_ptr()))
+        if rc:
+            raise RuntimeError(L.cssg_last_error().decode())
+
+    for _ in range(max(args.warmup, 1)):
+        launch()
+    torch.cuda.synchronize()
+    stream = ctx.tstream
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
+    sampler = ClockSampler(local)
+    sampler.start()
+    for k in range(args.steps):
+        ev[2 * k].record(stream)
+        launch()
+        ev[2 * k + 1].record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    if int(err.item()):
+        raise RuntimeError("tensor-core completion wait timed out")
+    ms_each = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(args.steps)]
+    t_ms = max_over_ranks(pg, sum(ms_each))
+    value = world * n * args.steps / (t_ms * 1e-3)
+    flops_pair = 2 * (16 * 64 + 64 * 64 + 64 * 64 + 64)
+    achieved = value / world * flops_pair / 1e12
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    peak = peaks.get("bf16_tflops", 1900.0)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "screened pairs/s", "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic",
+            "config": {"workload": cfg["workload"], "pairs_per_launch": n,
+                       "l2": "inputs (128 MB) larger than L2", "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "mlp_infer_tc",
+                         "flops_per_pair": flops_pair,
+                         "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)" if peaks else "of fallback"},
+            "gpu_launches": args.steps, "clocks": clocks}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -623,6 +694,8 @@ def main():
         run_reference(args, cfg)
     elif cfg.get("screen"):
         run_screen(args, cfg)
+    elif cfg.get("mlp"):
+        run_mlp(args, cfg)
     else:
         run_ours(args, cfg)
 
