@@ -108,12 +108,20 @@ def build_inputs(cfg):
 
 
 class ClockSampler:
-    """nvidia-smi samples during the timed region (SM clock, max clock, throttle reasons)."""
+    """nvidia-smi samples during the timed region (SM clock, max clock, throttle reasons).
+
+    start() returns once the first sample has arrived, so the sampler's own start-up stays outside the timed region;
+    begin() / end() bracket that region, and stop() keeps the samples that arrived inside it (plus the first one after
+    it, which covers its last interval)."""
+
+    PERIOD_MS = 100
 
     def __init__(self, index):
         self.index = index
         self.proc = None
         self.lines = []
+        self.t_begin = self.t_end = None
+        self.first = threading.Event()
 
     def start(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -121,27 +129,47 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(timeout=10.0)
         except OSError:
             self.proc = None
 
     def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
+        try:
+            for line in self.proc.stdout:
+                self.lines.append((time.perf_counter(), line.strip()))
+                self.first.set()
+        finally:
+            self.first.set()  # nvidia-smi ended (or failed): nothing more to wait for
+
+    def begin(self):
+        self.t_begin = time.perf_counter()
+
+    def end(self):
+        self.t_end = time.perf_counter()
 
     def stop(self):
         if self.proc is None:
             return None
+        if self.t_end is not None:  # wait for the sample that covers the end of the region
+            deadline = time.perf_counter() + 3 * self.PERIOD_MS * 1e-3
+            while time.perf_counter() < deadline and not any(t > self.t_end for t, _ in self.lines):
+                time.sleep(0.01)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        keep = list(self.lines)
+        if self.t_begin is not None and self.t_end is not None:
+            inside = [x for x in keep if self.t_begin <= x[0] <= self.t_end]
+            after = [x for x in keep if x[0] > self.t_end][:1]
+            keep = inside + after
         sm, mx, reasons = [], [], set()
-        for ln in self.lines:
+        for _, ln in keep:
             p = [x.strip() for x in ln.split(",")]
             if len(p) < 9:
                 continue
@@ -156,8 +184,11 @@ class ClockSampler:
                     reasons.add(name)
         if not sm:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+               "samples": len(sm), "period_ms": self.PERIOD_MS}
+        if self.t_begin is not None and self.t_end is not None:
+            out["region_s"] = round(self.t_end - self.t_begin, 4)
+        return out
 
 
 def dist_setup():
@@ -335,9 +366,10 @@ def run_ours(args, cfg):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     sampler = ClockSampler(local)
+    sampler.start()
     barrier(pg)
     torch.cuda.synchronize()
-    sampler.start()
+    sampler.begin()
     for k in range(args.steps):
         with ctx.use():
             flush.zero_()
@@ -345,6 +377,7 @@ def run_ours(args, cfg):
         S.step(1, graph=True)
         ends[k].record(stream)
     torch.cuda.synchronize()
+    sampler.end()
     clocks = sampler.stop()
     barrier(pg)
     ms_steps = [a.elapsed_time(e) for a, e in zip(starts, ends)]
@@ -522,10 +555,13 @@ def run_screen(args, cfg):
             raise RuntimeError(f"{name}: per-item errors during warm-up: {bits:#x} {cnt}")
 
     sampler = ClockSampler(local)
-    barrier(pg)
     sampler.start()
+    barrier(pg)
+    torch.cuda.synchronize()
+    sampler.begin()
     ms_plain = _timed_steps(ctx, plain, args.steps, flush, stream)
     ms_scr = _timed_steps(ctx, scr, args.steps, flush, stream)
+    sampler.end()
     clocks = sampler.stop()
     barrier(pg)
     t_plain = max_over_ranks(pg, sum(ms_plain))
@@ -638,11 +674,14 @@ def run_mlp(args, cfg):
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
     sampler = ClockSampler(local)
     sampler.start()
+    torch.cuda.synchronize()
+    sampler.begin()
     for k in range(args.steps):
         ev[2 * k].record(stream)
         launch()
         ev[2 * k + 1].record(stream)
     torch.cuda.synchronize()
+    sampler.end()
     clocks = sampler.stop()
     if int(err.item()):
         raise RuntimeError("tensor-core completion wait timed out")
@@ -675,7 +714,7 @@ def run_mlp(args, cfg):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="torus_nvt")
