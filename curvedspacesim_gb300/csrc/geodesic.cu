@@ -1275,7 +1275,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                 {
                     const unsigned pm = __ballot_sync(FULL, tmask & 32);
                     processed += (tmask & 32) ? 1 : 0;
-                    if (t0 == 0) atomicAdd(&ctl->nProc, __popc(pm));
+                    if (lane == 0 && pm) atomicAdd(&ctl->nProc, __popc(pm));  // every warp of the group
                 }
                 for (int k = 0; k < 3; ++k) {
                     const int pos = warp_append(&ctl->nPT, (tmask >> k) & 1, lane);
