@@ -688,6 +688,45 @@ def run_mlp(args, cfg):
     ms_each = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(args.steps)]
     t_ms = max_over_ranks(pg, sum(ms_each))
     value = world * n * args.steps / (t_ms * 1e-3)
+
+    # ---- e2e: pinned host features in, host predictions out, through the C ABI call, every step ----
+    Xh = X.cpu().pin_memory()
+    yh = torch.empty(n, dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        with torch.cuda.stream(stream):
+            X.copy_(Xh, non_blocking=True)
+        launch()
+        with torch.cuda.stream(stream):
+            yh.copy_(y, non_blocking=True)
+    torch.cuda.synchronize()
+    barrier(pg)
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            X.copy_(Xh, non_blocking=True)
+        launch()
+        with torch.cuda.stream(stream):
+            yh.copy_(y, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t1)
+    e2e = world * n * args.steps / e2e_s
+
+    # ---- CPU baseline (rank 0): the oracle's FP64 forward with the kernel's BF16 roundings on a 65,536-row sample
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, ROOT)
+        from oracle import mlp_ref
+        Xs = X[:65536].float().cpu().numpy()
+        ps = params.cpu().numpy()
+        mlp_ref.forward(Xs[:1024], ps)
+        reps, t2 = 0, time.perf_counter()
+        while reps < 3 or time.perf_counter() - t2 < 2.0:
+            mlp_ref.forward(Xs, ps)
+            reps += 1
+        cpu = {"value": reps * len(Xs) / (time.perf_counter() - t2), "unit": "pairs/s",
+               "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{reps} passes over 65,536 of the rows (oracle/mlp_ref.forward, numpy FP64 with BF16 "
+                         f"roundings; BLAS threads as numpy sets them)"}
     flops_pair = 2 * (16 * 64 + 64 * 64 + 64 * 64 + 64)
     achieved = value / world * flops_pair / 1e12
     peaks = {}
@@ -708,7 +747,8 @@ def run_mlp(args, cfg):
                          "frac": achieved / peak, "traffic": None, "kernel": "mlp_infer_tc",
                          "flops_per_pair": flops_pair,
                          "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)" if peaks else "of fallback"},
-            "gpu_launches": args.steps, "clocks": clocks}), flush=True)
+            "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": n * 16 * 2, "d2h_bytes_per_step": n * 4},
+            "cpu_baseline": cpu, "gpu_launches": args.steps, "clocks": clocks}), flush=True)
 
 
 def main():
