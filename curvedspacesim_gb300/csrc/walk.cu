@@ -562,7 +562,12 @@ void cssg_launch_transport(const DevMesh* meshes, const int* meshOf, int n, int*
                            cudaStream_t s, const int* skip)
 {
     if (n <= 0) return;
-    int threads = 128;
+    // A warp's FP64 instructions share its SM sub-partition's FP64 pipe with the other warps there.  While the
+    // particles fit one warp per SM, blocks of one warp spread them over the SMs; beyond that, blocks of four warps.
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = (n <= 32 * sms) ? 32 : 128;
     transport_kernel<<<(n + threads - 1) / threads, threads, 0, s>>>(meshes, meshOf, n, face, bary, disp, transport, nT,
                                                                      status, crossings, pos_out, skip);
 }
