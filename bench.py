@@ -9,8 +9,9 @@ walks with velocity transport, one neighbour + exact-geodesic + force pass, the 
 Metric: particle-steps/s (N x steps / time).
   value : inputs resident in HBM; K steps, each one CUDA-graph replay, timed with CUDA events on the launching
           stream; L2 flushed (a 512 MB write) before every timed step.
-  e2e   : the same steps through the C ABI with host buffers: per step the state (face, barycentrics, velocities,
-          forces) is copied from pinned host memory to the device, stepped, and copied back; wall clock.
+  e2e   : the same steps through the C ABI with host buffers: per step one cssg_system_step_host call copies the
+          state (face, barycentrics, velocities, forces) from pinned host memory to the device, steps, and copies it
+          back; wall clock.
 The reference arm (--impl reference) times the CPU oracle (the C++ restatement of the reference path; the CGAL-based
 reference itself cannot be built here) with all host threads on the same workload.
 Multi-GPU: one process per GPU, each an independent replica of the system (weak scaling, no collective).
@@ -429,10 +430,7 @@ def run_ours(args, cfg):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        S.set_state(hf, hb, hv, hfo)
-        S.step(1, graph=True)
-        a, bb, c, d = S.get_state()
-        hf[:], hb[:], hv[:], hfo[:] = a, bb, c, d
+        S.step_host(1, hf, hb, hv, hfo)  # host state in, one step, host state out: one C-ABI call
     e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
     e2e = world * n * args.steps / e2e_s
     io_bytes = n * (4 + 24 + 24 + 24)
@@ -604,10 +602,7 @@ def run_screen(args, cfg):
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     for _ in range(args.steps):
-        scr.set_state(hf, hb, hv, hfo)
-        scr.step(1, graph=True)
-        a, bb, c, d = scr.get_state()
-        hf[:], hb[:], hv[:], hfo[:] = a, bb, c, d
+        scr.step_host(1, hf, hb, hv, hfo)  # host state in, one step, host state out: one C-ABI call
     e2e = world * n * args.steps / max_over_ranks(pg, time.perf_counter() - t1)
     io_bytes = n * (4 + 24 + 24 + 24)
 

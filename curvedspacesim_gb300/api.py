@@ -266,6 +266,18 @@ class System:
     def step(self, steps: int = 1, graph: bool = True):
         check(_lib.load().cssg_system_step(self.h, int(steps), int(bool(graph))), "cssg_system_step")
 
+    def step_host(self, steps, face, bary, vel, force, out=None):
+        """cssg_system_step_host: host state in, `steps` graph-replayed steps, host state out (into `out`, a tuple of
+        four arrays, or into the input arrays when out is None), one synchronisation."""
+        arrs = [np.asarray(a) for a in (face, bary, vel, force)]
+        for a, dt in zip(arrs, (np.int32, np.float64, np.float64, np.float64)):
+            if a.dtype != dt or not a.flags.c_contiguous:
+                raise ValueError("step_host wants C-contiguous int32 face and float64 bary, vel, force arrays")
+        outs = arrs if out is None else [np.asarray(a) for a in out]
+        check(_lib.load().cssg_system_step_host(self.h, int(steps), *[_np_ptr(a) for a in arrs],
+                                                *[_np_ptr(a) for a in outs]), "cssg_system_step_host")
+        return outs
+
     def compute_forces(self):
         check(_lib.load().cssg_system_compute_forces(self.h), "cssg_system_compute_forces")
 

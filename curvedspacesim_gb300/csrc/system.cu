@@ -983,6 +983,36 @@ extern "C" int cssg_system_step(cssg_system* s, int steps, int use_graph)
     return CSSG_OK;
 }
 
+extern "C" int cssg_system_step_host(cssg_system* s, int steps, const int* face_in, const double* bary_in,
+                                     const double* vel_in, const double* force_in, int* face_out, double* bary_out,
+                                     double* vel_out, double* force_out)
+{
+    if (!s || steps < 0) return CSSG_ERR_ARG;
+    cudaStream_t st = s->ctx->stream;
+    const int n = s->n;
+    if (face_in) {
+        for (int k = 0; k < s->K; ++k)
+            for (int i = s->partBase[k]; i < s->partBase[k + 1]; ++i)
+                if (face_in[i] < 0 || face_in[i] >= s->meshes[k]->d.nF) {
+                    cssg_set_error("cssg_system_step_host: face index out of range");
+                    return CSSG_ERR_ARG;
+                }
+        CSSG_CUDA(cudaMemcpyAsync(s->face, face_in, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    }
+    if (bary_in) CSSG_CUDA(cudaMemcpyAsync(s->bary, bary_in, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+    if (vel_in) CSSG_CUDA(cudaMemcpyAsync(s->vel, vel_in, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+    if (force_in) CSSG_CUDA(cudaMemcpyAsync(s->force, force_in, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+    if (face_in || bary_in) cssg_launch_positions(s->dmeshes, s->sysOf, n, s->face, s->bary, s->pos, st);
+    const int rc = cssg_system_step(s, steps, 1);
+    if (rc != CSSG_OK) return rc;
+    if (face_out) CSSG_CUDA(cudaMemcpyAsync(face_out, s->face, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    if (bary_out) CSSG_CUDA(cudaMemcpyAsync(bary_out, s->bary, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+    if (vel_out) CSSG_CUDA(cudaMemcpyAsync(vel_out, s->vel, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+    if (force_out) CSSG_CUDA(cudaMemcpyAsync(force_out, s->force, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+    CSSG_CUDA(cudaStreamSynchronize(st));
+    return CSSG_OK;
+}
+
 extern "C" int cssg_system_compute_forces(cssg_system* s)
 {
     if (!s) return CSSG_ERR_ARG;

@@ -404,6 +404,30 @@ public:
         throwIf(cssg_system_step(sys_, steps, 1), "cssg_system_step");
         checkItems();
     }
+    //! simulation::performTimestep, `steps` times, for a caller that keeps the state in the public vectors: pushes
+    //! them, steps on the device and pulls them back in one library call (one synchronisation)
+    void performTimestepFromHost(int steps = 1)
+    {
+        std::vector<int> f(N);
+        std::vector<double> b(3 * (size_t)N), v(3 * (size_t)N), fo(3 * (size_t)N);
+        for (int i = 0; i < N; ++i) {
+            f[i] = positions[i].faceIndex;
+            for (int c = 0; c < 3; ++c) {
+                b[3 * i + c] = positions[i].x[c];
+                v[3 * i + c] = velocities[i][c];
+                fo[3 * i + c] = forces[i][c];
+            }
+        }
+        throwIf(cssg_system_step_host(sys_, steps, f.data(), b.data(), v.data(), fo.data(), f.data(), b.data(),
+                                      v.data(), fo.data()),
+                "cssg_system_step_host");
+        for (int i = 0; i < N; ++i) {
+            positions[i] = meshPosition(point3(b[3 * i], b[3 * i + 1], b[3 * i + 2]), f[i]);
+            velocities[i] = vector3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+            forces[i] = vector3(fo[3 * i], fo[3 * i + 1], fo[3 * i + 2]);
+        }
+        checkItems();
+    }
     //! simulation::computeForces
     void computeForces()
     {

@@ -46,6 +46,11 @@ int main(int argc, char** argv)
     sim.push();
     sim.performTimestep(10);
     sim.pull();
+    // the same 10 steps with the state kept in the public vectors (one library call)
+    cssg::gpuSimulation sim2(space, n, force, cssg::gpuSimulation::NVE, 0.005, 0.0, 1.0, 2, false);
+    sim2.positions = pos;
+    sim2.velocities = vel;
+    sim2.performTimestepFromHost(10);
     printf("{\"area\": %.17g, \"d\": [", space.getArea());
     for (size_t i = 0; i < d.size(); ++i) printf("%s%.17g", i ? ", " : "", d[i]);
     printf("], \"ts\": [");
@@ -57,6 +62,12 @@ int main(int argc, char** argv)
     printf("], \"bary\": [");
     for (int i = 0; i < n; ++i)
         printf("%s%.17g, %.17g, %.17g", i ? ", " : "", sim.positions[i].x[0], sim.positions[i].x[1], sim.positions[i].x[2]);
+    printf("], \"face2\": [");
+    for (int i = 0; i < n; ++i) printf("%s%d", i ? ", " : "", sim2.positions[i].faceIndex);
+    printf("], \"bary2\": [");
+    for (int i = 0; i < n; ++i)
+        printf("%s%.17g, %.17g, %.17g", i ? ", " : "", sim2.positions[i].x[0], sim2.positions[i].x[1],
+               sim2.positions[i].x[2]);
     printf("]}\n");
     return 0;
 }

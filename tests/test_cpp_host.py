@@ -66,3 +66,7 @@ def test_host_classes_match_oracle(tmp_path, oracle_mod):
     assert err == 0
     pg = OM.r3(np.array(res["face"]), np.array(res["bary"]).reshape(-1, 3))
     np.testing.assert_allclose(pg, OM.r3(fs, bs), atol=1e-9)
+    # gpuSimulation::performTimestepFromHost (cssg_system_step_host): the same device steps, state in and out of the
+    # public vectors in one call
+    assert res["face2"] == res["face"]
+    np.testing.assert_allclose(res["bary2"], res["bary"], atol=1e-13)
