@@ -73,9 +73,13 @@ int cssg_cuda_fail(cudaError_t e, const char* what);
 // Launches the batched transport kernel; pos_out (nullable) receives the final R3 positions, crossings (nullable)
 // accumulates the launch's crossings.
 // meshes: device array of meshes; meshOf (nullable): per-particle index into it (null: all on meshes[0])
+// kick_force (nullable): velocity-Verlet first half folded into the walk, from the velocity in transport vector 0:
+// disp = dt v + dt^2 f / 2, v += dt f / 2 (velocityVerletNVE.cpp:14-21).  status_bits (nullable): OR of
+// (1 << status) over the walks that failed.
 void cssg_launch_transport(const DevMesh* meshes, const int* meshOf, int n, int* face, double* bary, double* disp,
                            double* transport, int nT, int* status, unsigned long long* crossings, double* pos_out,
-                           cudaStream_t s, const int* skip = nullptr);
+                           cudaStream_t s, const int* skip = nullptr, int* status_bits = nullptr,
+                           const double* kick_force = nullptr, double kick_dt = 0.0);
 void cssg_launch_positions(const DevMesh* meshes, const int* meshOf, int n, const int* face, const double* bary,
                            double* pos, cudaStream_t s);
 
@@ -143,6 +147,9 @@ struct GeoLaunch {
     int pairCap;                 // system mode: pair slots per source
     double* force;               // system mode: force per source (nullable)
     int* status;                 // per source
+    int* statusBits;             // nullable: OR of (1 << status) over the sources whose final status is an error
+    double* kickVel;             // nullable: velocity-Verlet second half kick v += 0.5 dt f where the force is written
+    double kickDt;
     long long* stats;            // nullable: per source {windows processed, launches, rounds, targets}
     unsigned long long* counters;  // [0] windows processed, [1] vertex launches, [2] in-range pairs, [3] capacity hits
     int patchDisconnected;       // CSR mode with cutoff = inf: unreached -> 2*maxDist, tangent (0,0,1)

@@ -937,9 +937,12 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     if (nT == 0) {
         if (Lp.srcCost && t0 == 0) Lp.srcCost[si] = 1;
         if (Lp.force && t0 == 0) {
-            Lp.force[3 * si] = Lp.force[3 * si + 1] = Lp.force[3 * si + 2] = 0;
+            Lp.force[3 * si] = Lp.force[3 * si + 1] = Lp.force[3 * si + 2] = 0;  // no kick: zero force
         }
-        if (t0 == 0) Lp.status[si] = ctl->err;
+        if (t0 == 0) {
+            Lp.status[si] = ctl->err;
+            if (ctl->err && Lp.statusBits) atomicOr(Lp.statusBits, 1 << ctl->err);
+        }
         return;
     }
     for (int t = t0; t < nT; t += NT) {
@@ -1395,6 +1398,11 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             Lp.force[3 * si] = fx;
             Lp.force[3 * si + 1] = fy;
             Lp.force[3 * si + 2] = fz;
+            if (Lp.kickVel) {  // velocityVerletNVE second half (velocityVerletNVE.cpp:23-29) for this particle
+                Lp.kickVel[3 * si] += 0.5 * Lp.kickDt * fx;
+                Lp.kickVel[3 * si + 1] += 0.5 * Lp.kickDt * fy;
+                Lp.kickVel[3 * si + 2] += 0.5 * Lp.kickDt * fz;
+            }
         }
     }
     inRange = gp.sumi(inRange);
@@ -1409,6 +1417,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     }
     if (t0 == 0) {
         Lp.status[si] = err;
+        if (err && Lp.statusBits) atomicOr(Lp.statusBits, 1 << err);
         cnt[0] += processed;
         cnt[1] += launches;
         cnt[2] += inRange;

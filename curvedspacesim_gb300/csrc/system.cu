@@ -133,22 +133,6 @@ __global__ void cell_sort(int n, const int* __restrict__ cellOf, const int* __re
 }
 
 // ---- integrators ------------------------------------------------------------------------------------------------
-__global__ void nve_first_half(int n, double* __restrict__ v, const double* __restrict__ f, double* __restrict__ disp,
-                               double dt)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= 3 * n) return;
-    disp[i] = dt * v[i] + 0.5 * dt * dt * f[i];
-    v[i] += 0.5 * dt * f[i];
-}
-
-__global__ void nve_second_half(int n, double* __restrict__ v, const double* __restrict__ f, double dt)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= 3 * n) return;
-    v[i] += 0.5 * dt * f[i];
-}
-
 // One thread per system: noseHooverNVT::propagateChain.  Chain k occupies len = 4 (M+1) + 2 doubles:
 // (M+1) x {pos, vel, accel, mass}, then kineticEnergy, scale.
 __global__ void nh_chain(double* chains, int K, int Mc, double T, double dt)
@@ -270,14 +254,6 @@ __global__ void count_screened(int m, const int* __restrict__ total, const unsig
         atomicAdd(&out[1], (unsigned long long)b);
     }
     (void)m;
-}
-
-__global__ void status_or(int n, const int* __restrict__ st, int* __restrict__ bits)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int b = (i < n && st[i]) ? (1 << st[i]) : 0;
-    for (int o = 16; o > 0; o >>= 1) b |= __shfl_xor_sync(0xffffffffu, b, o);
-    if ((threadIdx.x & 31) == 0 && b) atomicOr(bits, b);
 }
 
 int next_pow2(long long x)
@@ -450,8 +426,33 @@ __global__ void lpt_scatter(int n, const int* __restrict__ order, const int* __r
     out[atomicAdd(&buckets[32 + cost_bucket(cost[si])], 1)] = si;
 }
 
-// findNeighbors + computeForces into s->force
-void launch_forces(cssg_system* s)
+// the three passes above in one block, for source counts one block sorts quickly
+constexpr int kLptSmallMax = 16384;
+__global__ void __launch_bounds__(1024) lpt_small(int n, const int* __restrict__ order, const int* __restrict__ cost,
+                                                   int* __restrict__ out)
+{
+    __shared__ int count[32], cursor[32];
+    if (threadIdx.x < 32) count[threadIdx.x] = 0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) atomicAdd(&count[cost_bucket(cost[order ? order[k] : k])], 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int b = 0; b < 32; ++b) {
+            cursor[b] = acc;
+            acc += count[b];
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int si = order ? order[k] : k;
+        out[atomicAdd(&cursor[cost_bucket(cost[si])], 1)] = si;
+    }
+}
+
+// findNeighbors + computeForces into s->force; kick: the velocity-Verlet second half kick of every particle is
+// applied where its force is written (velocityVerletNVE.cpp:23-29)
+void launch_forces(cssg_system* s, bool kick = false)
 {
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
@@ -489,6 +490,9 @@ void launch_forces(cssg_system* s)
     L.pairCap = s->pairCap;
     L.force = s->force;
     L.status = s->srcStatus;
+    L.statusBits = s->statusBits;
+    L.kickVel = kick ? s->vel : nullptr;
+    L.kickDt = s->P.dt;
     L.counters = s->counters + 1;
     L.delta = s->delta;
     L.maxRounds = 4096;
@@ -508,10 +512,14 @@ void launch_forces(cssg_system* s)
     L.wideRegs = s->tuneWide;
     L.srcCost = s->srcCost;
     if (s->tuneLpt) {
-        cudaMemsetAsync(s->lptBuckets, 0, 64 * sizeof(int), st);
-        lpt_count<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->srcCost, s->lptBuckets);
-        lpt_scan<<<1, 32, 0, st>>>(s->lptBuckets);
-        lpt_scatter<<<(n + tb - 1) / tb, tb, 0, st>>>(n, L.order, s->srcCost, s->lptBuckets, s->lptOrder);
+        if (n <= kLptSmallMax) {
+            lpt_small<<<1, 1024, 0, st>>>(n, L.order, s->srcCost, s->lptOrder);
+        } else {
+            cudaMemsetAsync(s->lptBuckets, 0, 64 * sizeof(int), st);
+            lpt_count<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->srcCost, s->lptBuckets);
+            lpt_scan<<<1, 32, 0, st>>>(s->lptBuckets);
+            lpt_scatter<<<(n + tb - 1) / tb, tb, 0, st>>>(n, L.order, s->srcCost, s->lptBuckets, s->lptOrder);
+        }
         L.order = s->lptOrder;
     }
     if (s->screen) {
@@ -567,17 +575,17 @@ void launch_forces(cssg_system* s)
     B.maxWindows = s->bigMaxWindows;
     cssg_launch_geodesic(B, st);
     record(s);
-    status_or<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->srcStatus, s->statusBits);
 }
 
-void launch_walk(cssg_system* s)
+// moveParticles with the velocity transported; kick: the velocity-Verlet first half (disp = dt v + dt^2 f / 2,
+// v += dt f / 2, velocityVerletNVE.cpp:14-21) is done by the walk kernel itself
+void launch_walk(cssg_system* s, bool kick = false)
 {
     cudaStream_t st = s->ctx->stream;
     record(s);
     cssg_launch_transport(s->dmeshes, s->sysOf, s->n, s->face, s->bary, s->disp, s->vel, 1, s->walkStatus,
-                          s->counters, s->pos, st);
+                          s->counters, s->pos, st, nullptr, s->statusBits, kick ? s->force : nullptr, s->P.dt);
     record(s);
-    status_or<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, s->walkStatus, s->statusBits);
 }
 
 void launch_step(cssg_system* s)
@@ -587,10 +595,10 @@ void launch_step(cssg_system* s)
     const int tb = 256;
     const double dt = s->P.dt;
     if (s->P.integrator == 0) {
-        nve_first_half<<<(3 * n + tb - 1) / tb, tb, 0, st>>>(n, s->vel, s->force, s->disp, dt);
-        launch_walk(s);
-        launch_forces(s);
-        nve_second_half<<<(3 * n + tb - 1) / tb, tb, 0, st>>>(n, s->vel, s->force, dt);
+        // velocityVerletNVE::performUpdate (velocityVerletNVE.cpp:3-29): first half kick + drift inside the walk
+        // kernel, second half kick where each force is written
+        launch_walk(s, true);
+        launch_forces(s, true);
     } else {
         const int Mc = s->P.chain_length;
         const double T = s->P.temperature;
@@ -919,9 +927,12 @@ extern "C" int cssg_system_reset_thermostat(cssg_system* s)
 extern "C" int cssg_system_kernels_per_step(cssg_system* s, int* count)
 {
     if (!s || !count) return CSSG_ERR_ARG;
-    // walk + status_or ; [cell list: assign, scan x3, scatter, sort] + geodesic + retry + status_or
-    int walk = 2, forces = (s->useCells ? 6 : 0) + 3 + (s->screen ? 10 : 0);
-    *count = s->P.integrator == 0 ? (1 + walk + forces + 1) : (2 + walk + forces + 2 + walk + 2);
+    // forces: [cell list: assign, scan x3, scatter, sort] + [screen: candidates, clamp, scan x3, compact, features,
+    // inference, decisions, counts] + [longest-first order: 1 or 3] + three geodesic passes; NVE: walk (with both
+    // kicks folded in) + forces; NVT: chain, scale, walk, forces, kick, KE, walk, chain, scale
+    const int lpt = s->tuneLpt ? (s->n <= kLptSmallMax ? 1 : 3) : 0;
+    const int forces = (s->useCells ? 6 : 0) + (s->screen ? 10 : 0) + lpt + 3;
+    *count = s->P.integrator == 0 ? 1 + forces : 8 + forces;
     return CSSG_OK;
 }
 
@@ -1506,8 +1517,7 @@ void fire_iteration(cssg_system* s, FireState* dst, int nBlocks)
     double* partialMax = s->firePartials + 3 * nBlocks;
     fire_first_half<<<nBlocks, kFireBlock, 0, st>>>(n, s->vel, s->force, s->disp, s->fireTrans, dst);
     cssg_launch_transport(s->dmeshes, s->sysOf, n, s->face, s->bary, s->disp, s->fireTrans, 2, s->walkStatus,
-                          s->counters, s->pos, st, &dst->done);
-    status_or<<<(n + 255) / 256, 256, 0, st>>>(n, s->walkStatus, s->statusBits);
+                          s->counters, s->pos, st, &dst->done, s->statusBits);
     fire_unpack<<<nBlocks, kFireBlock, 0, st>>>(n, s->fireTrans, s->vel, dst);
     launch_forces(s);
     fire_second_half<<<nBlocks, kFireBlock, 0, st>>>(n, s->vel, s->force, dst, partials);

@@ -507,19 +507,31 @@ __global__ void __launch_bounds__(128) transport_kernel(const DevMesh* __restric
                                                         double* __restrict__ bary, double* __restrict__ disp,
                                                         double* __restrict__ transport, int ntv, int* __restrict__ status,
                                                         unsigned long long* crossings, double* __restrict__ posOut,
-                                                        const int* __restrict__ skip)
+                                                        const int* __restrict__ skip, int* __restrict__ statusBits,
+                                                        const double* __restrict__ kickForce, double kickDt)
 {
     if (skip && *skip) return;  // a device-side stop flag (FIRE after convergence): nothing moves
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int cr = 0;
+    int cr = 0, bits = 0;
     if (i < n) {
         const DevMesh& M = meshes[meshOf ? meshOf[i] : 0];
         int f = face[i];
         double b[3] = {bary[3 * i], bary[3 * i + 1], bary[3 * i + 2]};
-        double d[3] = {disp[3 * i], disp[3 * i + 1], disp[3 * i + 2]};
+        double d[3];
         double tv[WALK_MAX_TRANSPORT][3];
         for (int t = 0; t < ntv; ++t)
             for (int c = 0; c < 3; ++c) tv[t][c] = transport[3 * (ntv * (size_t)i + t) + c];
+        if (kickForce) {
+            // velocityVerletNVE first half (the velocity is transported vector 0)
+            for (int c = 0; c < 3; ++c) {
+                const double fc = kickForce[3 * i + c];
+                d[c] = kickDt * tv[0][c] + 0.5 * kickDt * kickDt * fc;
+                tv[0][c] += 0.5 * kickDt * fc;
+            }
+        } else {
+            for (int c = 0; c < 3; ++c) d[c] = disp[3 * i + c];
+        }
+        double kicked[3] = {tv[0][0], tv[0][1], tv[0][2]};
         double pos[3];
         int st = transport_one(M, f, b, d, tv, ntv, 100000, &cr, posOut ? pos : nullptr);
         status[i] = st;
@@ -530,14 +542,22 @@ __global__ void __launch_bounds__(128) transport_kernel(const DevMesh* __restric
                 for (int c = 0; c < 3; ++c) transport[3 * (ntv * (size_t)i + t) + c] = tv[t][c];
             if (posOut)
                 for (int c = 0; c < 3; ++c) posOut[3 * i + c] = pos[c];
+        } else {
+            bits = 1 << st;
+            if (kickForce)  // the kick stands even where the walk failed
+                for (int c = 0; c < 3; ++c) transport[3 * (ntv * (size_t)i) + c] = kicked[c];
         }
         for (int c = 0; c < 3; ++c) disp[3 * i + c] = d[c];
     }
-    if (crossings) {
-        // warp-aggregated count of crossings
-        unsigned mask = 0xffffffffu;
-        for (int o = 16; o > 0; o >>= 1) cr += __shfl_xor_sync(mask, cr, o);
-        if ((threadIdx.x & 31) == 0 && cr) atomicAdd(crossings, (unsigned long long)cr);
+    // warp-aggregated crossing count and failure bits
+    const unsigned mask = 0xffffffffu;
+    for (int o = 16; o > 0; o >>= 1) {
+        cr += __shfl_xor_sync(mask, cr, o);
+        bits |= __shfl_xor_sync(mask, bits, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (crossings && cr) atomicAdd(crossings, (unsigned long long)cr);
+        if (statusBits && bits) atomicOr(statusBits, bits);
     }
 }
 
@@ -559,7 +579,7 @@ __global__ void positions_kernel(const DevMesh* __restrict__ meshes, const int* 
 
 void cssg_launch_transport(const DevMesh* meshes, const int* meshOf, int n, int* face, double* bary, double* disp,
                            double* transport, int nT, int* status, unsigned long long* crossings, double* pos_out,
-                           cudaStream_t s, const int* skip)
+                           cudaStream_t s, const int* skip, int* status_bits, const double* kick_force, double kick_dt)
 {
     if (n <= 0) return;
     // A warp's FP64 instructions share its SM sub-partition's FP64 pipe with the other warps there.  While the
@@ -568,8 +588,10 @@ void cssg_launch_transport(const DevMesh* meshes, const int* meshOf, int n, int*
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int threads = (n <= 32 * sms) ? 32 : 128;
+    if (nT < 1) kick_force = nullptr;  // the kick needs the velocity as transported vector 0
     transport_kernel<<<(n + threads - 1) / threads, threads, 0, s>>>(meshes, meshOf, n, face, bary, disp, transport, nT,
-                                                                     status, crossings, pos_out, skip);
+                                                                     status, crossings, pos_out, skip, status_bits,
+                                                                     kick_force, kick_dt);
 }
 
 void cssg_launch_positions(const DevMesh* meshes, const int* meshOf, int n, const int* face, const double* bary,
