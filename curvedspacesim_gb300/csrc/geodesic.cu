@@ -641,9 +641,10 @@ __device__ __forceinline__ void load_pt(const DevMesh& M, int f, const double* b
     for (int c = 0; c < 3; ++c) out[c] = (b[0] * p0[c] + b[1] * p1[c] + b[2] * p2[c]) / s;
 }
 
-// final distance of target t: source face, logged windows and face-vertex labels
+// final distance of target t: source face, logged windows and face-vertex labels.  te (the direction of arrival) is
+// filled only when wantTe: the force path uses the start direction alone.
 __device__ __noinline__ double target_query(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int t, int nLog,
-                               double* ts, double* te)
+                               double* ts, double* te, bool wantTe)
 {
     const int f = S.tface[t];
     const double* P = &S.tp[3 * t];
@@ -653,7 +654,7 @@ __device__ __noinline__ double target_query(const DevMesh& M, const Slot& S, con
         double u[3] = {P[0] - src.S[0], P[1] - src.S[1], P[2] - src.S[2]};
         double d = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
         if (d > 0)
-            for (int c = 0; c < 3; ++c) ts[c] = te[c] = u[c] / d;
+            for (int c = 0; c < 3; ++c) ts[c] = te[c] = u[c] / d;  // one division serves both
         return d;
     }
     double best = CUDART_INF, bdx = 0, bdy = 0;
@@ -680,7 +681,7 @@ __device__ __noinline__ double target_query(const DevMesh& M, const Slot& S, con
             }
         }
     }
-    if (bw >= 0) {
+    if (bw >= 0 && wantTe) {
         const Win w = S.wlog[bw];
         const int g = w.he >> 2, j = w.he & 3;
         const double L = M.geom[9 * g + 3 * j], cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
@@ -708,7 +709,8 @@ __device__ __noinline__ double target_query(const DevMesh& M, const Slot& S, con
             best = d;
             bdx = S.vtx[h];
             bdy = S.vty[h];
-            for (int q = 0; q < 3; ++q) te[q] = l > 0 ? u[q] / l : 0;
+            if (wantTe)
+                for (int q = 0; q < 3; ++q) te[q] = l > 0 ? u[q] / l : 0;
         }
     }
     if (best < CUDART_INF)
@@ -1346,10 +1348,11 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     }
     double fx = 0, fy = 0, fz = 0;
     int inRange = 0;
+    const bool wantTe = D.searchMode == 0 && Lp.teOut;
     for (int t = t0; t < nT; t += NT) {
-        double ts[3], te[3];
+        double ts[3], te[3] = {0, 0, 0};
         const bool screened = S.tidx[t] < 0;
-        double d = (err || screened) ? CUDART_INF : target_query(M, S, C, src, t, nLog, ts, te);
+        double d = (err || screened) ? CUDART_INF : target_query(M, S, C, src, t, nLog, ts, te, wantTe);
         if (screened) ts[0] = ts[1] = ts[2] = te[0] = te[1] = te[2] = 0;
         if (d > src.cutoff) {
             d = CUDART_INF;
