@@ -637,8 +637,11 @@ __device__ __forceinline__ void load_pt(const DevMesh& M, int f, const double* b
     const double* p0 = &M.V[3 * M.F[3 * f]];
     const double* p1 = &M.V[3 * M.F[3 * f + 1]];
     const double* p2 = &M.V[3 * M.F[3 * f + 2]];
-    double s = b[0] + b[1] + b[2];
-    for (int c = 0; c < 3; ++c) out[c] = (b[0] * p0[c] + b[1] * p1[c] + b[2] * p2[c]) / s;
+    const double s = b[0] + b[1] + b[2];
+    for (int c = 0; c < 3; ++c) {
+        const double x = b[0] * p0[c] + b[1] * p1[c] + b[2] * p2[c];
+        out[c] = s == 1.0 ? x : x / s;  // normalised weights usually sum to exactly 1: skip the FP64 division
+    }
 }
 
 // final distance of target t: source face, logged windows and face-vertex labels.  te (the direction of arrival) is

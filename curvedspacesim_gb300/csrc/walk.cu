@@ -64,11 +64,18 @@ __device__ void bary_of(const FacePts& P, const double* x, double* out)
     out[2] = w;
 }
 
+// Divisions by a weight sum below: normalised weights usually sum to exactly 1 (about 80-97% of the sums in a walk
+// step), and x / 1 == x exactly, so the division (the costliest FP64 operation of the walk, ~10 FP64-pipe
+// instructions) is skipped then.  The results are the same bits either way.
+
 // barycenter of three weighted points (PMP::construct_point)
 __device__ __forceinline__ void construct_pt(const FacePts& P, const double* b, double* out)
 {
-    double s = b[0] + b[1] + b[2];
-    for (int c = 0; c < 3; ++c) out[c] = (b[0] * P.p[0][c] + b[1] * P.p[1][c] + b[2] * P.p[2][c]) / s;
+    const double s = b[0] + b[1] + b[2];
+    for (int c = 0; c < 3; ++c) {
+        const double x = b[0] * P.p[0][c] + b[1] * P.p[1][c] + b[2] * P.p[2][c];
+        out[c] = s == 1.0 ? x : x / s;
+    }
 }
 
 __device__ __forceinline__ void below_zero_clamp(double* b)
@@ -79,7 +86,8 @@ __device__ __forceinline__ void below_zero_clamp(double* b)
         b[i] = fmax(b[i], tol);
         s += b[i];
     }
-    for (int i = 0; i < 3; ++i) b[i] = b[i] / s;
+    if (s != 1.0)
+        for (int i = 0; i < 3; ++i) b[i] = b[i] / s;
 }
 
 __device__ __forceinline__ void near_zero_clamp(double* b)
@@ -90,7 +98,8 @@ __device__ __forceinline__ void near_zero_clamp(double* b)
         if (b[i] > -tol && b[i] < tol) b[i] = tol;
         s += b[i];
     }
-    for (int i = 0; i < 3; ++i) b[i] = b[i] / s;
+    if (s != 1.0)
+        for (int i = 0; i < 3; ++i) b[i] = b[i] / s;
 }
 
 __device__ bool hit_v1v2(const double* s, const double* e, double* ip)
