@@ -42,7 +42,7 @@ BYTES_PER_CANDIDATE = 4 + 4 + 24 + 24  # read index, face, barycentrics, R3 posi
 BYTES_PER_FACE = 12 + 12 + 72         # patch face: vertex ids, neighbours, edge frames
 # DRAM bytes (read + write) of one launch of the regular propagation pass, from a full ncu capture of that workload
 # (profiles/geodesic_kernel_torus200x100_N2000_nvt.txt); workloads without a capture report null
-TRAFFIC_BYTES = {"torus200x100_N2000_nvt_patch": 56_376_832 + 127_459_072}
+TRAFFIC_BYTES = {"torus200x100_N2000_nvt_patch": 47_415_808 + 112_837_888}
 
 
 def workload_config(name):
