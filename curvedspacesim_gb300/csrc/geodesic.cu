@@ -1745,7 +1745,6 @@ extern "C" int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSr
     if (nSlots > fit) nSlots = std::max<long long>(1, fit);
     void* scratch = nullptr;
     int* work = nullptr;
-    unsigned long long* counters = nullptr;
     CSSG_CUDA(cudaMallocAsync(&scratch, slotBytes * nSlots, s));
     CSSG_CUDA(cudaMallocAsync((void**)&work, sizeof(int), s));
     CSSG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));

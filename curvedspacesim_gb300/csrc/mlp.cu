@@ -351,12 +351,11 @@ __global__ void __launch_bounds__(TB) mlp_train_fwd_bwd(const __nv_bfloat16* __r
         atomicAdd(&grad[OFF_W3 + e], acc);
     }
     if (t < NH) {
-        float accb = 0, accw = 0;
+        float accb = 0;
         for (int s = 0; s < TB; ++s) {
             accb += G[s * NH + t];
         }
         atomicAdd(&grad[OFF_B3 + t], accb);
-        (void)accw;
     }
     // head: dW4[o] = sum dy gelu(Z3), dB4 = sum dy
     __syncthreads();

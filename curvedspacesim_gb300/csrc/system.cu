@@ -256,13 +256,6 @@ __global__ void count_screened(int m, const int* __restrict__ total, const unsig
     (void)m;
 }
 
-int next_pow2(long long x)
-{
-    int p = 1;
-    while (p < x && p < (1 << 30)) p <<= 1;
-    return p;
-}
-
 }  // namespace
 
 struct cssg_system {
