@@ -63,6 +63,8 @@ __device__ __forceinline__ double rcp_nr(double d)
 // error plumbing
 void cssg_set_error(const std::string& msg);
 int cssg_cuda_fail(cudaError_t e, const char* what);
+// records "<fn>: bad arguments" as the last error and returns CSSG_ERR_ARG
+int cssg_bad_args(const char* fn);
 #define CSSG_CUDA(call)                                      \
     do {                                                     \
         cudaError_t e__ = (call);                            \

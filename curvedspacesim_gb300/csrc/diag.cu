@@ -27,7 +27,7 @@ __global__ void __launch_bounds__(256) fp64_fma_chain(double* out, int iters, do
 
 extern "C" int cssg_diag_fp64_peak(cssg_ctx* ctx, double* gflops)
 {
-    if (!ctx || !gflops) return CSSG_ERR_ARG;
+    if (!ctx || !gflops) return cssg_bad_args("cssg_diag_fp64_peak");
     int sms = 0;
     CSSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     double* out = nullptr;

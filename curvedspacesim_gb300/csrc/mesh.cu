@@ -18,6 +18,12 @@ static thread_local std::string g_lastError;
 
 void cssg_set_error(const std::string& msg) { g_lastError = msg; }
 
+int cssg_bad_args(const char* fn)
+{
+    g_lastError = std::string(fn) + ": bad arguments (null handle or pointer, or a value out of range)";
+    return CSSG_ERR_ARG;
+}
+
 int cssg_cuda_fail(cudaError_t e, const char* what)
 {
     g_lastError = std::string(what) + ": " + cudaGetErrorString(e);
@@ -376,7 +382,7 @@ extern "C" int cssg_ctx_destroy(cssg_ctx* c)
 
 extern "C" int cssg_ctx_synchronize(cssg_ctx* c)
 {
-    if (!c) return CSSG_ERR_ARG;
+    if (!c) return cssg_bad_args("cssg_ctx_synchronize");
     CSSG_CUDA(cudaStreamSynchronize(c->stream));
     return CSSG_OK;
 }

@@ -891,7 +891,7 @@ extern "C" int cssg_system_destroy(cssg_system* s)
 extern "C" int cssg_system_set_state(cssg_system* s, const int* face, const double* bary, const double* vel,
                                      const double* force)
 {
-    if (!s) return CSSG_ERR_ARG;
+    if (!s) return cssg_bad_args("cssg_system_set_state");
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
     if (face) {
@@ -913,13 +913,13 @@ extern "C" int cssg_system_set_state(cssg_system* s, const int* face, const doub
 
 extern "C" int cssg_system_reset_thermostat(cssg_system* s)
 {
-    if (!s) return CSSG_ERR_ARG;
+    if (!s) return cssg_bad_args("cssg_system_reset_thermostat");
     return reset_chain(s);
 }
 
 extern "C" int cssg_system_kernels_per_step(cssg_system* s, int* count)
 {
-    if (!s || !count) return CSSG_ERR_ARG;
+    if (!s || !count) return cssg_bad_args("cssg_system_kernels_per_step");
     // forces: [cell list: assign, scan x3, scatter, sort] + [screen: candidates, clamp, scan x3, compact, features,
     // inference, decisions, counts] + [longest-first order: 1 or 3] + three geodesic passes; NVE: walk (with both
     // kicks folded in) + forces; NVT: chain, scale, walk, forces, kick, KE, walk, chain, scale
@@ -931,7 +931,7 @@ extern "C" int cssg_system_kernels_per_step(cssg_system* s, int* count)
 
 extern "C" int cssg_system_get_state(cssg_system* s, int* face, double* bary, double* vel, double* force)
 {
-    if (!s) return CSSG_ERR_ARG;
+    if (!s) return cssg_bad_args("cssg_system_get_state");
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
     if (face) CSSG_CUDA(cudaMemcpyAsync(face, s->face, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
@@ -944,7 +944,7 @@ extern "C" int cssg_system_get_state(cssg_system* s, int* face, double* bary, do
 
 extern "C" int cssg_system_device_state(cssg_system* s, int** face, double** bary, double** vel, double** force)
 {
-    if (!s) return CSSG_ERR_ARG;
+    if (!s) return cssg_bad_args("cssg_system_device_state");
     if (face) *face = s->face;
     if (bary) *bary = s->bary;
     if (vel) *vel = s->vel;
@@ -954,7 +954,7 @@ extern "C" int cssg_system_device_state(cssg_system* s, int** face, double** bar
 
 extern "C" int cssg_system_step(cssg_system* s, int steps, int use_graph)
 {
-    if (!s || steps < 0) return CSSG_ERR_ARG;
+    if (!s || steps < 0) return cssg_bad_args("cssg_system_step");
     cudaStream_t st = s->ctx->stream;
     s->eventsUsed = 0;
     if (use_graph && !s->timing) {
@@ -991,7 +991,7 @@ extern "C" int cssg_system_step_host(cssg_system* s, int steps, const int* face_
                                      const double* vel_in, const double* force_in, int* face_out, double* bary_out,
                                      double* vel_out, double* force_out)
 {
-    if (!s || steps < 0) return CSSG_ERR_ARG;
+    if (!s || steps < 0) return cssg_bad_args("cssg_system_step_host");
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
     if (face_in) {
@@ -1019,7 +1019,7 @@ extern "C" int cssg_system_step_host(cssg_system* s, int steps, const int* face_
 
 extern "C" int cssg_system_compute_forces(cssg_system* s)
 {
-    if (!s) return CSSG_ERR_ARG;
+    if (!s) return cssg_bad_args("cssg_system_compute_forces");
     s->eventsUsed = 0;
     launch_forces(s);
     CSSG_CUDA(cudaGetLastError());
@@ -1061,7 +1061,7 @@ extern "C" int cssg_system_set_tuning(cssg_system* s, double delta_scale, int wa
 // not change; the result differs between candidates only in the work done.
 extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_host)
 {
-    if (!s) return CSSG_ERR_ARG;
+    if (!s) return cssg_bad_args("cssg_system_autotune");
     if (reps < 1) reps = 1;
     cudaStream_t st = s->ctx->stream;
     int sms = 0;
@@ -1157,7 +1157,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
 
 extern "C" int cssg_system_check(cssg_system* s, int* bits, unsigned long long* counters)
 {
-    if (!s) return CSSG_ERR_ARG;
+    if (!s) return cssg_bad_args("cssg_system_check");
     cudaStream_t st = s->ctx->stream;
     int hb = 0;
     unsigned long long hc[8];
@@ -1174,7 +1174,7 @@ extern "C" int cssg_system_check(cssg_system* s, int* bits, unsigned long long* 
 
 extern "C" int cssg_system_pairs(cssg_system* s, int cap, int* ih, int* jh, double* dh, double* th, int* count)
 {
-    if (!s) return CSSG_ERR_ARG;
+    if (!s) return cssg_bad_args("cssg_system_pairs");
     cudaStream_t st = s->ctx->stream;
     if (!s->pairD) {
         // enable pair output for subsequent force evaluations
@@ -1221,7 +1221,7 @@ extern "C" int cssg_system_pairs(cssg_system* s, int cap, int* ih, int* jh, doub
 
 extern "C" int cssg_system_chain(cssg_system* s, double* chain, int capacity)
 {
-    if (!s || !chain) return CSSG_ERR_ARG;
+    if (!s || !chain) return cssg_bad_args("cssg_system_chain");
     int len = chain_len(s) * s->K;
     if (capacity < len) {
         cssg_set_error("cssg_system_chain: capacity too small");
@@ -1236,7 +1236,7 @@ extern "C" int cssg_system_chain(cssg_system* s, double* chain, int capacity)
 // skipped when |chord| / sigma + yhat > 1 + margin.  Requires the cell-list neighbour structure.
 extern "C" int cssg_system_set_screen(cssg_system* s, const float* params_host, double margin, int enable)
 {
-    if (!s) return CSSG_ERR_ARG;
+    if (!s) return cssg_bad_args("cssg_system_set_screen");
     cudaStream_t st = s->ctx->stream;
     if (enable) {
         if (!s->useCells || !params_host) {
@@ -1286,7 +1286,7 @@ extern "C" int cssg_system_set_screen(cssg_system* s, const float* params_host, 
 // {candidate pairs, screened-out pairs, tensor-core wait failures} since the last call (synchronises, resets)
 extern "C" int cssg_system_screen_counters(cssg_system* s, unsigned long long* out_host)
 {
-    if (!s || !out_host) return CSSG_ERR_ARG;
+    if (!s || !out_host) return cssg_bad_args("cssg_system_screen_counters");
     out_host[0] = out_host[1] = out_host[2] = 0;
     if (!s->screenCounters) return CSSG_OK;
     cudaStream_t st = s->ctx->stream;
@@ -1305,7 +1305,7 @@ extern "C" int cssg_system_screen_counters(cssg_system* s, unsigned long long* o
 
 extern "C" int cssg_system_timing(cssg_system* s, int enable)
 {
-    if (!s) return CSSG_ERR_ARG;
+    if (!s) return cssg_bad_args("cssg_system_timing");
     s->timing = enable != 0;
     return CSSG_OK;
 }
@@ -1313,7 +1313,7 @@ extern "C" int cssg_system_timing(cssg_system* s, int enable)
 // ms[0] = geodesic/force kernel total, ms[1] = walk kernel total over the last step() call
 extern "C" int cssg_system_last_times(cssg_system* s, double* ms, int capacity)
 {
-    if (!s || !ms || capacity < 2) return CSSG_ERR_ARG;
+    if (!s || !ms || capacity < 2) return cssg_bad_args("cssg_system_last_times");
     CSSG_CUDA(cudaStreamSynchronize(s->ctx->stream));
     double geo = 0, walk = 0;
     // events are recorded in pairs: (geo start, geo end) and (walk start, walk end) in launch order

@@ -41,3 +41,34 @@ def test_no_cpu_fallback():
     from curvedspacesim_gb300 import api
     with pytest.raises(Exception):
         api.Context(0)
+
+
+def test_null_handles_are_argument_errors_without_gpu():
+    """Every entry point rejects a null handle with CSSG_ERR_ARG and a message naming it, before touching a device;
+    destroying a null handle is a no-op (CSSG_OK)."""
+    from curvedspacesim_gb300 import _lib
+    L = _lib.load()
+    N = None
+    calls = {
+        "cssg_system_step": (N, 1, 1),
+        "cssg_system_step_host": (N, 1, N, N, N, N, N, N, N, N),
+        "cssg_system_set_state": (N, N, N, N, N),
+        "cssg_system_get_state": (N, N, N, N, N),
+        "cssg_system_compute_forces": (N,),
+        "cssg_system_check": (N, N, N),
+        "cssg_system_set_tuning": (N, 1.0, 8, 0, 0, 0, 1, 0),
+        "cssg_system_autotune": (N, 1, N),
+        "cssg_system_fire": (N, N, 0, N),
+        "cssg_system_stress": (N, N),
+        "cssg_system_kernels_per_step": (N, N),
+        "cssg_transport_batch": (N, N, 0, N, N, N, N, 0, N, N),
+        "cssg_distance_batch": (N, N, 1, N, N, N, N, N, 0, 1.0, N, 1.0, N, N, N, N, N),
+        "cssg_distance_batch_noalloc": (N, N, 1, N, N, N, N, N, 0, 1.0, N, 1.0, N, N, N, N, N),
+        "cssg_mesh_set_boundary": (N, 1),
+        "cssg_system_create": (N, N, 0, N, N),
+    }
+    for name, args in calls.items():
+        assert getattr(L, name)(*args) == 1, name  # CSSG_ERR_ARG
+        assert name.encode() in L.cssg_last_error(), (name, L.cssg_last_error())
+    for name in ("cssg_system_destroy", "cssg_mesh_destroy", "cssg_ctx_destroy"):
+        assert getattr(L, name)(N) == 0, name
