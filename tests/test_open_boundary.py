@@ -125,3 +125,31 @@ def test_open_system_nve_matches_oracle(gpu, oracle_mod, boundary):
     assert err == 0
     np.testing.assert_allclose(OM.r3(fg, bg), OM.r3(fo, bo), atol=1e-8)
     np.testing.assert_allclose(vg, vo, atol=1e-8)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("integrator", ["nve", "nvt"])
+def test_closed_rule_on_open_mesh_reports_border(gpu, integrator):
+    """A system on the open silo with the closed-mesh rule: walks that reach the rim fail with CSSG_ST_BORDER, and
+    the failure reaches System.check() (the walk kernel reduces the failure bits itself)."""
+    api, ctx = gpu
+    V, F = ms.silo(nsides=32, ncap=8, nz=12)
+    rng = np.random.default_rng(8)
+    n, sigma = 200, 0.3
+    f, b = ms.area_weighted_positions(V, F, n, rng)
+    vel = ms.tangent_velocities(V, F, f, 50.0, rng)
+    M = api.Mesh(V, F)  # closed rule
+    p = api.make_params(integrator, "harmonic", k=1 / sigma ** 2, sigma=sigma, range_=sigma, submesh=True,
+                        max_dist=sigma, cutoff=sigma, dt=0.05, temperature=1.0)
+    S = api.System(ctx, M, n, p)
+    S.set_state(f, b, vel, np.zeros((n, 3)))
+    S.step(5, graph=True)
+    bits, _ = S.check()
+    assert bits & (1 << 1), bits
+    # the same system with the tangential rule: no failure
+    M2 = api.Mesh(V, F, boundary="tangential")
+    S2 = api.System(ctx, M2, n, p)
+    S2.set_state(f, b, vel, np.zeros((n, 3)))
+    S2.step(5, graph=True)
+    bits2, _ = S2.check()
+    assert bits2 == 0, bits2
