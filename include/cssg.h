@@ -154,11 +154,11 @@ int cssg_system_device_state(cssg_system* sys, int** face, double** bary, double
 /* simulation::performTimestep x steps (simulation.cpp:84-95); asynchronous on the context stream.  use_graph=1
  * replays one captured CUDA graph per step. */
 int cssg_system_step(cssg_system* sys, int steps, int use_graph);
-/* simulation::performTimestep x steps (simulation.cpp:84-95) from and to host state, in one call: the state arrays given in *_in (nullable;
- * host memory, pinned for overlap) are copied in, the steps run as graph replays, the state is copied out to *_out
- * (nullable; may alias *_in), then the call synchronises once.  Same checks as cssg_system_set_state.  A caller that
- * keeps its state on the host (the reference's simpleModel owns host vectors) pays one synchronisation per call
- * instead of one per set_state, get_state and step. */
+/* simulation::performTimestep x steps (simulation.cpp:84-95) from and to host state, in one call: the state arrays
+ * given in *_in (nullable; host memory, pinned for overlap) are copied in, the steps run as graph replays, the state
+ * is copied out to *_out (nullable; may alias *_in), then the call synchronises once.  Same checks as
+ * cssg_system_set_state.  A caller that keeps its state on the host (the reference's simpleModel owns host vectors)
+ * pays one synchronisation per call instead of one per set_state, get_state and step. */
 int cssg_system_step_host(cssg_system* sys, int steps, const int* face_in, const double* bary_in, const double* vel_in,
                           const double* force_in, int* face_out, double* bary_out, double* vel_out, double* force_out);
 /* simulation::computeForces (simulation.cpp:61-70 -> baseForce.cpp:12-28): neighbours, geodesics, forces. */
