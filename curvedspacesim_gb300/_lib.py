@@ -27,6 +27,7 @@ EXPORTS = [
     "cssg_mlp_adam", "cssg_system_set_screen", "cssg_system_screen_counters", "cssg_distance_batch_noalloc",
     "cssg_system_set_tuning", "cssg_system_autotune", "cssg_system_fire", "cssg_system_stress",
     "cssg_mesh_set_boundary", "cssg_diag_reciprocal", "cssg_system_step_host",
+    "cssg_system_gradient_descent",
 ]
 
 
@@ -107,6 +108,7 @@ def load(build_if_missing: bool = True):
     L.cssg_system_device_state.argtypes = [P, PP, PP, PP, PP]
     L.cssg_system_step.argtypes = [P, I, I]
     L.cssg_system_step_host.argtypes = [P, I, P, P, P, P, P, P, P, P]
+    L.cssg_system_gradient_descent.argtypes = [P, I, D, I]
     L.cssg_system_compute_forces.argtypes = [P]
     L.cssg_system_set_tuning.argtypes = [P, D, I, I, I, I, I, I]
     L.cssg_system_autotune.argtypes = [P, I, P]

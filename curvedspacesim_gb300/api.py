@@ -278,6 +278,11 @@ class System:
                                                 *[_np_ptr(a) for a in outs]), "cssg_system_step_host")
         return outs
 
+    def gradient_descent(self, steps: int, delta_t: float, transport_velocity: bool = False):
+        """gradientDescent::performUpdate x steps: forces, then every particle moved by delta_t * force."""
+        rc = _lib.load().cssg_system_gradient_descent(self.h, int(steps), float(delta_t), int(bool(transport_velocity)))
+        check(rc, "cssg_system_gradient_descent")
+
     def compute_forces(self):
         check(_lib.load().cssg_system_compute_forces(self.h), "cssg_system_compute_forces")
 

@@ -1652,6 +1652,32 @@ extern "C" int cssg_system_fire(cssg_system* s, const cssg_fire_params* fp, int 
     return CSSG_OK;
 }
 
+namespace {
+// gradientDescent::performUpdate's displacement (gradientDescent.cpp:12-16): deltaT * force, per component
+__global__ void gd_displacement(int n3, const double* __restrict__ f, double* __restrict__ disp, double dt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n3) disp[i] = dt * f[i];
+}
+}  // namespace
+
+extern "C" int cssg_system_gradient_descent(cssg_system* s, int steps, double delta_t, int transport_velocity)
+{
+    if (!s || steps < 0 || !(delta_t >= 0)) return cssg_bad_args("cssg_system_gradient_descent");
+    cudaStream_t st = s->ctx->stream;
+    const int n = s->n;
+    s->eventsUsed = 0;
+    for (int k = 0; k < steps; ++k) {
+        launch_forces(s);
+        gd_displacement<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, s->force, s->disp, delta_t);
+        cssg_launch_transport(s->dmeshes, s->sysOf, n, s->face, s->bary, s->disp, transport_velocity ? s->vel : nullptr,
+                              transport_velocity ? 1 : 0, s->walkStatus, s->counters, s->pos, st, nullptr,
+                              s->statusBits);
+    }
+    CSSG_CUDA(cudaGetLastError());
+    return CSSG_OK;
+}
+
 extern "C" int cssg_system_stress(cssg_system* s, double* stress_host)
 {
     if (!s || !stress_host || s->K != 1) {

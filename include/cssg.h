@@ -180,6 +180,14 @@ typedef struct cssg_fire_params {
 } cssg_fire_params;
 int cssg_system_fire(cssg_system* sys, const cssg_fire_params* params, int reset, double* result_host);
 
+/* ---- gradient descent: gradientDescent::performUpdate (src/updaters/gradientDescent.cpp:6-18) x steps --------------
+ * Each step computes the forces at the current positions, then moves every particle by deltaT * force with the walk
+ * (simpleModel::moveParticles, simpleModel.cpp:44-66).  transport_velocity = 1 carries the velocities along
+ * (the model's particleShiftsRequireVelocityTransport, set when an NVE/NVT/FIRE updater was attached before); the
+ * reference's gradient-descent updater sets no transport flag itself.  The forces left in the state are the last
+ * ones computed (before the last move).  Asynchronous on the context stream; failures via cssg_system_check. */
+int cssg_system_gradient_descent(cssg_system* sys, int steps, double delta_t, int transport_velocity);
+
 /* simulation::computeMonodisperseStress (src/simulation/simulation.cpp:104-173): recomputes the neighbour pairs on the
  * current positions and returns stress_host[9] (row-major 3x3) = rho <v (x) v> / (2N) + <f_ij (x) t_ij> / (4 A N),
  * rho = N / A, kB = 1; like the reference, v_i (x) v_i is summed once per neighbour pair of i.  Enables pair output.

@@ -428,6 +428,14 @@ public:
         }
         checkItems();
     }
+    //! gradientDescent::performUpdate (gradientDescent.cpp:6-18), `steps` times: forces, then every particle moved by
+    //! deltaT * force; the velocities are carried along when transportVelocities (the model's transport flag)
+    void gradientDescent(double deltaT, int steps = 1, bool transportVelocities = false)
+    {
+        throwIf(cssg_system_gradient_descent(sys_, steps, deltaT, transportVelocities ? 1 : 0),
+                "cssg_system_gradient_descent");
+        checkItems();
+    }
     //! simulation::computeForces
     void computeForces()
     {

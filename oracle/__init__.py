@@ -242,6 +242,25 @@ class OracleMesh:
                                 _p(st), int(threads), _p(out))
         return face, bary, vel, force, st, int(out[0]), float(out[1]), err
 
+    def gradient_descent(self, face, bary, params, steps, delta_t, vel=None, threads=0):
+        """gradientDescent::performUpdate (src/updaters/gradientDescent.cpp:6-18), `steps` times: the forces at the
+        current positions, then every particle moved by delta_t * force through the walk (simpleModel::moveParticles,
+        simpleModel.cpp:44-66), the velocity carried along when `vel` is given.  Returns (face, bary, vel, force, err)
+        with the last forces computed (before the last move); err = 1 when a walk failed."""
+        face = np.array(face, dtype=np.int32, copy=True)
+        bary = np.array(bary, dtype=np.float64, copy=True)
+        vel = None if vel is None else np.array(vel, dtype=np.float64, copy=True)
+        f = np.zeros((len(face), 3))
+        for _ in range(int(steps)):
+            f, _, _ = self.forces(face, bary, params, threads)
+            fo, bo, _, tv, st, _ = self.transport(face, bary, delta_t * f, None if vel is None else vel[:, None, :])
+            if np.any(st != 0):
+                return face, bary, vel, f, 1
+            face, bary = fo, bo
+            if vel is not None:
+                vel = tv[:, 0]
+        return face, bary, vel, f, 0
+
     def stress(self, face, bary, vel, params):
         face = np.ascontiguousarray(face, dtype=np.int32)
         bary = np.ascontiguousarray(bary, dtype=np.float64)

@@ -87,3 +87,43 @@ def test_stress_matches_oracle(gpu, oracle_mod):
         sg = S.stress()
         so = OM.stress(f, b, vel, prm)
         np.testing.assert_allclose(sg, so, rtol=1e-9, atol=1e-14)
+
+
+def test_oracle_gradient_descent_lowers_energy(oracle_mod):
+    """gradientDescent::performUpdate in the oracle: with a small step the energy of an overlapping configuration
+    falls every step."""
+    V, F, f, b, vel = _setup()
+    OM = oracle_mod.OracleMesh(V, F)
+    prm = OM.params(0, k=1 / 0.16, sigma=0.4, rng=0.4, submesh=1, max_dist=0.4, cutoff=0.4, dt=0.01)
+    energies = []
+    face, bary = f, b
+    for _ in range(5):
+        energies.append(OM.forces(face, bary, prm)[1])
+        face, bary, _, _, err = OM.gradient_descent(face, bary, prm, 1, 0.01)
+        assert err == 0
+    assert all(e1 < e0 for e0, e1 in zip(energies, energies[1:])), energies
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("transport_velocity", [False, True])
+def test_gradient_descent_matches_oracle(gpu, oracle_mod, transport_velocity):
+    """20 gradient-descent updates (forces, then a move by dt * force through the walk) against the oracle."""
+    api, ctx = gpu
+    V, F, f, b, vel = _setup(T=0.1)
+    n, sigma, dt = len(f), 0.4, 0.01
+    OM = oracle_mod.OracleMesh(V, F)
+    prm = OM.params(0, k=1 / sigma ** 2, sigma=sigma, rng=sigma, submesh=1, max_dist=sigma, cutoff=sigma, dt=dt)
+    M = api.Mesh(V, F)
+    p = api.make_params("nve", "harmonic", k=1 / sigma ** 2, sigma=sigma, range_=sigma, submesh=True, max_dist=sigma,
+                        cutoff=sigma, dt=dt)
+    S = api.System(ctx, M, n, p)
+    S.set_state(f, b, vel, np.zeros((n, 3)))
+    S.gradient_descent(20, dt, transport_velocity)
+    bits, _ = S.check()
+    assert bits == 0
+    fg, bg, vg, fcg = S.get_state()
+    fo, bo, vo, fco, err = OM.gradient_descent(f, b, prm, 20, dt, vel if transport_velocity else None)
+    assert err == 0
+    np.testing.assert_allclose(OM.r3(fg, bg), OM.r3(fo, bo), atol=1e-9)
+    np.testing.assert_allclose(fcg, fco, atol=1e-9)
+    np.testing.assert_allclose(vg, vo if transport_velocity else vel, atol=1e-9)
