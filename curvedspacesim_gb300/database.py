@@ -101,6 +101,51 @@ class SimpleModelDatabase:
         return out
 
 
+VV_MAGIC = b"CSSGVV01"
+
+
+class ValueVectorDatabase:
+    """valueVectorDatabase (src/databases/vectorValueDatabase.cpp:4-43): per record one float64 value and a float64
+    vector of fixed size, in the flat layout of include/curvedSpaceSimDatabase.hpp:
+
+        header (24 bytes): b"CSSGVV01", int64 vectorSize, int64 reserved
+        record:            float64 value, float64 vector[vectorSize]
+    """
+
+    def __init__(self, filename: str, vector_size: int, mode: str = READONLY):
+        self.filename = filename
+        self.size = int(vector_size)
+        self.mode = mode
+        if mode == REPLACE or (mode == READWRITE and not os.path.exists(filename)):
+            with open(filename, "wb") as fh:
+                fh.write(VV_MAGIC + np.array([self.size, 0], dtype="<i8").tobytes())
+        else:
+            with open(filename, "rb") as fh:
+                head = fh.read(24)
+            if len(head) != 24 or head[:8] != VV_MAGIC or int(np.frombuffer(head[8:16], "<i8")[0]) != self.size:
+                raise ValueError(f"{filename} is not a value/vector database of vectors of size {self.size}")
+
+    def current_number_of_records(self) -> int:
+        return max(0, (os.path.getsize(self.filename) - 24) // (8 * (1 + self.size)))
+
+    def write_state(self, value: float, vector):
+        if self.mode == READONLY:
+            raise PermissionError("database opened read-only")
+        vec = np.asarray(vector, "<f8").reshape(-1)
+        if vec.size < self.size:
+            raise ValueError("vector shorter than the record")
+        with open(self.filename, "ab") as fh:
+            fh.write(np.array([value], "<f8").tobytes() + vec[: self.size].tobytes())
+
+    def read_state(self, rec: int):
+        if not 0 <= rec < self.current_number_of_records():
+            raise IndexError(f"no record {rec}")
+        with open(self.filename, "rb") as fh:
+            fh.seek(24 + rec * 8 * (1 + self.size))
+            raw = np.frombuffer(fh.read(8 * (1 + self.size)), "<f8")
+        return float(raw[0]), raw[1:].copy()
+
+
 def write_system(db: SimpleModelDatabase, system, mesh_V, mesh_F, time: float):
     """Append the state of an api.System (one record)."""
     from . import meshes as ms

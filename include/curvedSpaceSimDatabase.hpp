@@ -8,7 +8,8 @@
 //   record:            double time, double R3position[3N], double barycentricPosition[3N], int32 faceIndex[N],
 //                      [double velocity[3N]], [double force[3N]], [int32 type[N]]
 //
-// curvedspacesim_gb300/database.py reads and writes the same layout.
+// curvedspacesim_gb300/database.py reads and writes the same layout.  valueVectorDatabase (below) does the same for
+// the reference's value + vector records (vectorValueDatabase.cpp).
 #ifndef CURVED_SPACE_SIM_DATABASE_HPP
 #define CURVED_SPACE_SIM_DATABASE_HPP
 
@@ -150,6 +151,91 @@ private:
 
     fileMode::Enum mode_;
     bool velocity, type, force;
+};
+
+//! valueVectorDatabase (src/databases/vectorValueDatabase.cpp:4-43): per record one double ("value") and a vector of
+//! a fixed size ("vector"), both appended by writeState.  Flat little-endian layout like simpleModelDatabase:
+//!
+//!   header (24 bytes): char magic[8] = "CSSGVV01", int64 vectorSize, int64 reserved
+//!   record:            double value, double vector[vectorSize]
+class valueVectorDatabase {
+public:
+    valueVectorDatabase(const std::string& fn, unsigned long vectorSize, fileMode::Enum mode = fileMode::readonly)
+        : filename(fn), maximumVectorSize(vectorSize), mode_(mode)
+    {
+        valueVector.resize(1);
+        dataVector.resize(maximumVectorSize);
+        FILE* f = std::fopen(fn.c_str(), "rb");
+        if (mode == fileMode::replace || (mode == fileMode::readwrite && !f)) {
+            if (f) std::fclose(f);
+            write_header();
+            return;
+        }
+        if (!f) throw std::runtime_error("valueVectorDatabase: cannot open " + fn);
+        char magic[8];
+        int64_t size = 0, reserved = 0;
+        bool ok = std::fread(magic, 1, 8, f) == 8 && std::fread(&size, 8, 1, f) == 1 &&
+                  std::fread(&reserved, 8, 1, f) == 1;
+        std::fclose(f);
+        if (!ok || std::memcmp(magic, "CSSGVV01", 8) != 0 || (unsigned long)size != maximumVectorSize)
+            throw std::runtime_error("valueVectorDatabase: " + fn + " is not a database of vectors of size " +
+                                     std::to_string(maximumVectorSize));
+    }
+
+    unsigned long currentNumberOfRecords() const
+    {
+        FILE* f = std::fopen(filename.c_str(), "rb");
+        if (!f) return 0;
+        std::fseek(f, 0, SEEK_END);
+        long size = std::ftell(f);
+        std::fclose(f);
+        const size_t rec = 8 * (1 + maximumVectorSize);
+        return size < 24 ? 0 : (unsigned long)((size - 24) / rec);
+    }
+
+    //! vectorValueDatabase.cpp:31-37: appends value and data (data must hold vectorSize entries)
+    void writeState(double val, std::vector<double>& data)
+    {
+        if (mode_ == fileMode::readonly) throw std::runtime_error("valueVectorDatabase: opened read-only");
+        if (data.size() < maximumVectorSize)
+            throw std::runtime_error("valueVectorDatabase: vector shorter than the record");
+        FILE* f = std::fopen(filename.c_str(), "ab");
+        if (!f) throw std::runtime_error("valueVectorDatabase: cannot append to " + filename);
+        std::fwrite(&val, 8, 1, f);
+        std::fwrite(data.data(), 8, maximumVectorSize, f);
+        std::fclose(f);
+    }
+
+    //! vectorValueDatabase.cpp:39-43: fills valueVector[0] and dataVector from record `record`
+    void readState(int record)
+    {
+        if (record < 0 || (unsigned long)record >= currentNumberOfRecords())
+            throw std::runtime_error("valueVectorDatabase: no record " + std::to_string(record));
+        FILE* f = std::fopen(filename.c_str(), "rb");
+        if (!f) throw std::runtime_error("valueVectorDatabase: cannot open " + filename);
+        std::fseek(f, (long)(24 + 8 * (1 + maximumVectorSize) * (size_t)record), SEEK_SET);
+        bool ok = std::fread(valueVector.data(), 8, 1, f) == 1 &&
+                  std::fread(dataVector.data(), 8, maximumVectorSize, f) == maximumVectorSize;
+        std::fclose(f);
+        if (!ok) throw std::runtime_error("valueVectorDatabase: truncated record");
+    }
+
+    std::string filename;
+    unsigned long maximumVectorSize;
+    std::vector<double> valueVector, dataVector;
+
+private:
+    void write_header()
+    {
+        FILE* f = std::fopen(filename.c_str(), "wb");
+        if (!f) throw std::runtime_error("valueVectorDatabase: cannot create " + filename);
+        int64_t size = (int64_t)maximumVectorSize, reserved = 0;
+        std::fwrite("CSSGVV01", 1, 8, f);
+        std::fwrite(&size, 8, 1, f);
+        std::fwrite(&reserved, 8, 1, f);
+        std::fclose(f);
+    }
+    fileMode::Enum mode_;
 };
 
 }  // namespace cssg

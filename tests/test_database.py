@@ -70,3 +70,42 @@ int main(int argc, char** argv) {
     assert float(out[3]) == b.reshape(-1)[7] and float(out[4]) == v.reshape(-1)[10]
     db2 = dbm.SimpleModelDatabase(n, fn, dbm.READONLY)
     assert db2.current_number_of_records() == 2 and db2.read_state(1)["time"] == 3.5
+
+
+def test_value_vector_database_python_and_cpp(tmp_path):
+    """valueVectorDatabase: records written in Python read back in Python and by the C++ header, and records
+    appended by the C++ header read back in Python."""
+    fn = str(tmp_path / "energies.cssgvv")
+    db = dbm.ValueVectorDatabase(fn, 5, dbm.REPLACE)
+    rng = np.random.default_rng(3)
+    rows = [(0.25 * k, rng.standard_normal(5)) for k in range(3)]
+    for v, vec in rows:
+        db.write_state(v, vec)
+    db2 = dbm.ValueVectorDatabase(fn, 5, dbm.READONLY)
+    assert db2.current_number_of_records() == 3
+    for k, (v, vec) in enumerate(rows):
+        rv, rvec = db2.read_state(k)
+        assert rv == v and np.array_equal(rvec, vec)
+    with pytest.raises(ValueError):
+        dbm.ValueVectorDatabase(fn, 6, dbm.READONLY)
+    if subprocess.run(["which", "g++"], capture_output=True).returncode != 0:
+        pytest.skip("no g++")
+    src = tmp_path / "vv.cpp"
+    src.write_text(r'''
+#include <cstdio>
+#include "curvedSpaceSimDatabase.hpp"
+int main(int argc, char** argv) {
+    cssg::valueVectorDatabase db(argv[1], 5, cssg::fileMode::readwrite);
+    db.readState(2);
+    std::printf("%lu %.17g %.17g\n", db.currentNumberOfRecords(), db.valueVector[0], db.dataVector[4]);
+    std::vector<double> v{1, 2, 3, 4, 5};
+    db.writeState(9.5, v);
+    return 0;
+}
+''')
+    exe = str(tmp_path / "vv")
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe], check=True)
+    out = subprocess.run([exe, fn], capture_output=True, text=True, check=True).stdout.split()
+    assert int(out[0]) == 3 and float(out[1]) == rows[2][0] and float(out[2]) == rows[2][1][4]
+    rv, rvec = dbm.ValueVectorDatabase(fn, 5, dbm.READONLY).read_state(3)
+    assert rv == 9.5 and np.array_equal(rvec, [1, 2, 3, 4, 5])
