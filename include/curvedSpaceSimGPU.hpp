@@ -7,7 +7,8 @@
 //   closedMeshSpace / triangulatedMeshSpace     cssg::closedMeshSpace
 //     distance (triangulatedMeshSpace.cpp:212-238, distanceWithSubmeshing :155-205)
 //     transportParticleAndVectors (:448-564), displaceParticle (:428-432), getArea (:153),
-//     useSubmeshingRoutines (triangulatedMeshSpace.h:60-66), randomVectorAtPosition (:118-138)
+//     useSubmeshingRoutines (triangulatedMeshSpace.h:60-66), randomPosition (:108-116),
+//     randomVectorAtPosition (:118-138)
 //   simpleModel (src/models/simpleModel.h:25-111) + force + updater + simulation
 //                                               cssg::gpuSimulation: positions/velocities/forces vectors,
 //                                               moveParticles, computeForces, performTimestep on the device
@@ -23,6 +24,7 @@
 
 #include <cmath>
 #include <fstream>
+#include <random>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -89,6 +91,51 @@ struct devbuf {
         if (n) cudaMemcpyAsync(h, p, sizeof(T) * n, cudaMemcpyDeviceToHost, s);
     }
 };
+
+//! triangulatedMeshSpace::randomPosition (triangulatedMeshSpace.cpp:108-116): a face drawn uniformly by index and
+//! weights (u, v, 1 - u - v) with u ~ U(0, 1), v ~ U(0, 1 - u) - not area-uniform, as in the reference.  Host-side
+//! initialisation; `nFaces` is the mesh's face count.
+template <class Engine>
+inline void randomPosition(int nFaces, meshPosition& p, Engine& rng)
+{
+    std::uniform_real_distribution<double> unit(0.0, 1.0);
+    const double x = unit(rng);
+    const double y = std::uniform_real_distribution<double>(0.0, 1.0 - x)(rng);
+    p.x = point3(x, y, 1.0 - x - y);
+    p.faceIndex = std::uniform_int_distribution<int>(0, nFaces - 1)(rng);
+}
+
+//! triangulatedMeshSpace::randomVectorAtPosition (triangulatedMeshSpace.cpp:118-138): a Gaussian combination of two
+//! orthonormal tangent vectors of the face (the face normal's fixed orthogonaliser and normal x orthogonaliser).
+//! V: 3 doubles per vertex; F: 3 vertex indices per face.
+template <class Engine>
+inline void randomVectorAtPosition(const std::vector<double>& V, const std::vector<int>& F, const meshPosition& p,
+                                   vector3& v, Engine& rng)
+{
+    const double* a = &V[3 * (size_t)F[3 * (size_t)p.faceIndex]];
+    const double* b = &V[3 * (size_t)F[3 * (size_t)p.faceIndex + 1]];
+    const double* c = &V[3 * (size_t)F[3 * (size_t)p.faceIndex + 2]];
+    const double e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+    double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    const double nl = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (double& x : n) x /= nl;
+    double o[3];
+    if (n[0] == 0 && n[1] == 0) {
+        o[0] = n[1] - n[2];
+        o[1] = n[2] - n[0];
+        o[2] = n[0] - n[1];
+    } else {
+        o[0] = n[1];
+        o[1] = -n[0];
+        o[2] = 0;
+    }
+    const double ol = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
+    for (double& x : o) x /= ol;
+    const double t2[3] = {n[1] * o[2] - n[2] * o[1], n[2] * o[0] - n[0] * o[2], n[0] * o[1] - n[1] * o[0]};
+    std::normal_distribution<double> gauss(0.0, 1.0);
+    const double g1 = gauss(rng), g2 = gauss(rng);
+    v = vector3(g1 * o[0] + g2 * t2[0], g1 * o[1] + g2 * t2[1], g1 * o[2] + g2 * t2[2]);
+}
 
 //! closedMeshSpace: a closed triangulated surface whose geodesic work runs on the GPU.
 class closedMeshSpace {
@@ -274,6 +321,18 @@ public:
                 out[3 * i + c] = (p[i].x[0] * V_[3 * (size_t)f[0] + c] + p[i].x[1] * V_[3 * (size_t)f[1] + c] +
                                   p[i].x[2] * V_[3 * (size_t)f[2] + c]) / s;
         }
+    }
+
+    //! triangulatedMeshSpace::randomPosition / randomVectorAtPosition on this mesh (host-side initialisation)
+    template <class Engine>
+    void randomPosition(meshPosition& p, Engine& rng) const
+    {
+        cssg::randomPosition((int)(F_.size() / 3), p, rng);
+    }
+    template <class Engine>
+    void randomVectorAtPosition(meshPosition& p, vector3& v, Engine& rng) const
+    {
+        cssg::randomVectorAtPosition(V_, F_, p, v, rng);
     }
 
     cssg_ctx* context() const { return ctx_; }

@@ -70,3 +70,55 @@ def test_host_classes_match_oracle(tmp_path, oracle_mod):
     # public vectors in one call
     assert res["face2"] == res["face"]
     np.testing.assert_allclose(res["bary2"], res["bary"], atol=1e-13)
+
+
+def test_random_position_and_tangent_without_gpu(tmp_path):
+    """cssg::randomPosition / randomVectorAtPosition (triangulatedMeshSpace.cpp:108-138), host-side: weights in the
+    simplex, faces in range, vectors in the face's tangent plane with unit-variance Gaussian components."""
+    if subprocess.run(["which", "g++"], capture_output=True).returncode != 0:
+        pytest.skip("no g++")
+    V, F = ms.icosphere(2)
+    src = tmp_path / "rnd.cpp"
+    vals = ", ".join(repr(float(x)) for x in V.reshape(-1))
+    fids = ", ".join(str(int(x)) for x in F.reshape(-1))
+    src.write_text(r'''
+#include <cstdio>
+#include "curvedSpaceSimGPU.hpp"
+int main() {
+    std::vector<double> V{''' + vals + r'''};
+    std::vector<int> F{''' + fids + r'''};
+    std::mt19937 rng(5);
+    const int nF = (int)(F.size() / 3);
+    double worstDot = 0, sum2 = 0, minW = 1, worstSum = 0;
+    int badFace = 0;
+    const int n = 20000;
+    for (int i = 0; i < n; ++i) {
+        cssg::meshPosition p;
+        cssg::randomPosition(nF, p, rng);
+        if (p.faceIndex < 0 || p.faceIndex >= nF) ++badFace;
+        for (int c = 0; c < 3; ++c) minW = std::min(minW, p.x[c]);
+        worstSum = std::max(worstSum, std::fabs(p.x[0] + p.x[1] + p.x[2] - 1.0));
+        cssg::vector3 v;
+        cssg::randomVectorAtPosition(V, F, p, v, rng);
+        const double* a = &V[3 * F[3 * p.faceIndex]];
+        const double* b = &V[3 * F[3 * p.faceIndex + 1]];
+        const double* c = &V[3 * F[3 * p.faceIndex + 2]];
+        double e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+        double nn[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        double nl = std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        worstDot = std::max(worstDot, std::fabs(v[0] * nn[0] + v[1] * nn[1] + v[2] * nn[2]) / nl);
+        sum2 += v.squared_length();
+    }
+    std::printf("%d %.17g %.17g %.17g %.17g\n", badFace, minW, worstSum, worstDot, sum2 / n);
+    return 0;
+}
+''')
+    exe = str(tmp_path / "rnd")
+    cuda = "/usr/local/cuda"
+    subprocess.run(["g++", "-O2", "-std=c++17", str(src), "-I", os.path.join(ROOT, "include"), "-I", f"{cuda}/include",
+                    "-o", exe], check=True, capture_output=True, text=True)
+    bad, min_w, worst_sum, worst_dot, mean_sq = subprocess.run([exe], capture_output=True, text=True,
+                                                                check=True).stdout.split()
+    assert int(bad) == 0 and float(min_w) >= 0.0 and float(worst_sum) < 1e-15
+    assert float(worst_dot) < 1e-12
+    assert abs(float(mean_sq) - 2.0) < 0.1  # two unit-variance components
