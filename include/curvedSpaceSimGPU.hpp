@@ -395,6 +395,28 @@ public:
     double k, sigma, maximumInteractionRange;
 };
 
+//! simpleModel's neighbour lists (simpleModel.h:55-60, filled by findNeighbors, simpleModel.cpp:68-112) from the
+//! pair records of cssg_system_pairs (grouped by source): per particle the candidate indices, the unit start tangents
+//! (neighborVectors) and the geodesic distances.  Distances beyond the force cutoff are +inf (the device does not
+//! resolve them further); pairs the learned screen skipped (j < 0, index -j - 1) carry their index and +inf.
+inline void pairsToNeighborLists(int N, int count, const int* i, const int* j, const double* d, const double* t,
+                                 std::vector<std::vector<int>>& neighbors,
+                                 std::vector<std::vector<vector3>>& neighborVectors,
+                                 std::vector<std::vector<double>>& neighborDistances)
+{
+    neighbors.assign(N, {});
+    neighborVectors.assign(N, {});
+    neighborDistances.assign(N, {});
+    for (int k = 0; k < count; ++k) {
+        const int a = i[k];
+        if (a < 0 || a >= N) continue;
+        const bool screened = j[k] < 0;
+        neighbors[a].push_back(screened ? -j[k] - 1 : j[k]);
+        neighborVectors[a].push_back(vector3(t[3 * (size_t)k], t[3 * (size_t)k + 1], t[3 * (size_t)k + 2]));
+        neighborDistances[a].push_back(screened ? HUGE_VAL : d[k]);
+    }
+}
+
 //! simpleModel + harmonicRepulsion + (velocityVerletNVE | noseHooverNVT) + simulation, resident on the GPU.
 //! performTimestep() advances one step without leaving the device; positions/velocities/forces are mirrored into
 //! the public vectors by pull() and pushed by push(), like the reference model's public members.
@@ -534,15 +556,38 @@ public:
     //! the library's autotuner (band width, CTA size, medium-pass slots, warp cap, source order) on this state
     void autotune(int reps = 2) { throwIf(cssg_system_autotune(sys_, reps, nullptr), "cssg_system_autotune"); }
 
+    //! simpleModel::findNeighbors (simpleModel.cpp:68-112) for host-side analysis: evaluates the forces at the current
+    //! device state (candidates, patches, geodesics) and fills neighbors / neighborVectors / neighborDistances from
+    //! the pair records (see pairsToNeighborLists).  The first call switches pair recording on for this system.
+    void findNeighbors()
+    {
+        int count = 0;
+        if (!pairsEnabled_) {
+            throwIf(cssg_system_pairs(sys_, 0, nullptr, nullptr, nullptr, nullptr, &count), "cssg_system_pairs");
+            pairsEnabled_ = true;
+        }
+        computeForces();
+        throwIf(cssg_system_pairs(sys_, 0, nullptr, nullptr, nullptr, nullptr, &count), "cssg_system_pairs");
+        std::vector<int> i(count), j(count);
+        std::vector<double> d(count), t(3 * (size_t)count);
+        throwIf(cssg_system_pairs(sys_, count, i.data(), j.data(), d.data(), t.data(), &count), "cssg_system_pairs");
+        pairsToNeighborLists(N, count, i.data(), j.data(), d.data(), t.data(), neighbors, neighborVectors,
+                             neighborDistances);
+    }
+
     double forceMax = 0;
     closedMeshSpace& space_;
     int N;
     std::vector<meshPosition> positions;
     std::vector<vector3> velocities;
     std::vector<vector3> forces;
+    std::vector<std::vector<int>> neighbors;
+    std::vector<std::vector<vector3>> neighborVectors;
+    std::vector<std::vector<double>> neighborDistances;
 
 private:
     cssg_system* sys_ = nullptr;
+    bool pairsEnabled_ = false;
 };
 
 //! simpleModelDatabase::writeState for a device-resident simulation: pulls the state and appends a record

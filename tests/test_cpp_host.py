@@ -122,3 +122,36 @@ int main() {
     assert int(bad) == 0 and float(min_w) >= 0.0 and float(worst_sum) < 1e-15
     assert float(worst_dot) < 1e-12
     assert abs(float(mean_sq) - 2.0) < 0.1  # two unit-variance components
+
+
+def test_pairs_to_neighbor_lists_without_gpu(tmp_path):
+    """cssg::pairsToNeighborLists: pair records grouped into simpleModel's neighbour lists (screened pairs decoded,
+    their distance +inf)."""
+    if subprocess.run(["which", "g++"], capture_output=True).returncode != 0:
+        pytest.skip("no g++")
+    src = tmp_path / "nl.cpp"
+    src.write_text(r'''
+#include <cstdio>
+#include "curvedSpaceSimGPU.hpp"
+int main() {
+    int i[] = {0, 0, 2, 2, 2};
+    int j[] = {1, 2, 0, -2, 3};
+    double d[] = {0.1, 0.2, 0.2, 0.9, INFINITY};
+    double t[15];
+    for (int k = 0; k < 15; ++k) t[k] = k;
+    std::vector<std::vector<int>> nb;
+    std::vector<std::vector<cssg::vector3>> nv;
+    std::vector<std::vector<double>> nd;
+    cssg::pairsToNeighborLists(4, 5, i, j, d, t, nb, nv, nd);
+    std::printf("%zu %zu %zu %zu %d %d %d %g %g %g %g\n", nb.size(), nb[0].size(), nb[1].size(), nb[2].size(), nb[2][0],
+                nb[2][1], nb[2][2], nd[0][1], nd[2][1], nv[2][1][0], nv[0][1][2]);
+    return 0;
+}
+''')
+    exe = str(tmp_path / "nl")
+    cuda = "/usr/local/cuda"
+    subprocess.run(["g++", "-O2", "-std=c++17", str(src), "-I", os.path.join(ROOT, "include"), "-I", f"{cuda}/include",
+                    "-o", exe], check=True, capture_output=True, text=True)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    assert out[:7] == ["4", "2", "0", "3", "0", "1", "3"]
+    assert float(out[7]) == 0.2 and out[8] == "inf" and float(out[9]) == 9.0 and float(out[10]) == 5.0
