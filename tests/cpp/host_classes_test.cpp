@@ -51,6 +51,12 @@ int main(int argc, char** argv)
     sim2.positions = pos;
     sim2.velocities = vel;
     sim2.performTimestepFromHost(10);
+    // simpleModel::findNeighbors at the initial positions: neighbour lists from the device's pair records
+    cssg::gpuSimulation sim3(space, n, force, cssg::gpuSimulation::NVE, 0.005, 0.0, 1.0, 2, false);
+    sim3.positions = pos;
+    sim3.velocities = vel;
+    sim3.push();
+    sim3.findNeighbors();
     printf("{\"area\": %.17g, \"d\": [", space.getArea());
     for (size_t i = 0; i < d.size(); ++i) printf("%s%.17g", i ? ", " : "", d[i]);
     printf("], \"ts\": [");
@@ -68,6 +74,13 @@ int main(int argc, char** argv)
     for (int i = 0; i < n; ++i)
         printf("%s%.17g, %.17g, %.17g", i ? ", " : "", sim2.positions[i].x[0], sim2.positions[i].x[1],
                sim2.positions[i].x[2]);
+    printf("], \"nb0\": [");
+    for (size_t k = 0; k < sim3.neighbors[0].size(); ++k) printf("%s%d", k ? ", " : "", sim3.neighbors[0][k]);
+    printf("], \"nd0\": [");  // -1 for +inf (beyond the cutoff)
+    for (size_t k = 0; k < sim3.neighborDistances[0].size(); ++k) {
+        const double x = sim3.neighborDistances[0][k];
+        printf("%s%.17g", k ? ", " : "", std::isinf(x) ? -1.0 : x);
+    }
     printf("]}\n");
     return 0;
 }

@@ -70,6 +70,13 @@ def test_host_classes_match_oracle(tmp_path, oracle_mod):
     # public vectors in one call
     assert res["face2"] == res["face"]
     np.testing.assert_allclose(res["bary2"], res["bary"], atol=1e-13)
+    # gpuSimulation::findNeighbors (all-to-all): particle 0's candidates are all others in index order, with the
+    # oracle's distances inside the 0.3 cutoff and +inf (printed -1) beyond it
+    assert res["nb0"] == list(range(1, n))
+    nd0 = np.array(res["nd0"])
+    inside = d < 0.3
+    np.testing.assert_allclose(nd0[inside], d[inside], rtol=1e-12)
+    assert np.all(nd0[~inside] == -1)
 
 
 def test_random_position_and_tangent_without_gpu(tmp_path):
