@@ -29,6 +29,13 @@
 //   * integrators    - velocityVerletNVE (src/updaters/velocityVerletNVE.cpp:3-29), noseHooverNVT
 //                      (src/updaters/noseHooverNVT.cpp:3-150), simpleModel::moveParticles / findNeighbors
 //                      (src/models/simpleModel.cpp:44-112)
+//   * open meshes    - the walk's border branches of openMeshSpace / tangentialOpenMeshSpace / absorbingOpenMeshSpace
+//                      (src/models/openMeshSpace.cpp:114-238, tangentialOpenMeshSpace.cpp:3-64,
+//                       absorbingOpenMeshSpace.cpp:2-50)
+//   * minimisers     - fireMinimization::minimizeByFire / fireStep (src/updaters/fireMinimization.cpp:3-96); the
+//                      gradient-descent updater (gradientDescent.cpp:6-18) is composed in oracle/__init__.py from the
+//                      forces and the walk
+//   * analysis       - simulation::computeMonodisperseStress (src/simulation/simulation.cpp:104-173)
 //
 // Build: see oracle/build.sh (g++ -O2 -ffp-contract=off -fopenmp, no -ffast-math).
 #include <algorithm>
