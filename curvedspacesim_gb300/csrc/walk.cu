@@ -12,10 +12,14 @@
 // This translation unit is compiled with -fmad=false so an edge-crossing walk performs exactly the IEEE operations
 // of the CPU restatement (no fused multiply-add contraction).
 //
-// Memory: per particle-step it reads face (4 B), bary (24 B), disp (24 B), transported vectors (24 B each) and
-// writes them back; each crossing reads the next face's 3 vertex indices, 3 neighbours, 3 vertex positions and
-// normal.  The face arrays are gathered with ordinary loads: particles address faces at random, so a bulk tensor
-// copy (TMA) of a fixed tile has nothing to stage.
+// Memory: per particle-step it reads face (4 B), bary (24 B), disp (24 B; the force instead in the NVE kick mode),
+// transported vectors (24 B each) and writes them back; each crossing reads the next face's 3 vertex indices,
+// 3 neighbours, 3 vertex positions and normal.  The face arrays are gathered with ordinary loads: particles address
+// faces at random, so a bulk tensor copy (TMA) of a fixed tile has nothing to stage.
+//
+// The kernel also carries two pieces of the step around it, to save launches: the velocity-Verlet first half
+// (kick + drift, velocityVerletNVE.cpp:14-21) when given the forces, and the reduction of its warps' failure codes
+// into the system's status bits.
 #include "cssg_internal.cuh"
 
 namespace {
