@@ -30,6 +30,10 @@
 // written, after a group barrier, by the thread whose proposal survived.  Processing order only affects how much
 // gets pruned, not the result.
 //
+// Where each source's force is written, the kernel can also apply the velocity-Verlet second half kick of that
+// particle (velocityVerletNVE.cpp:23-29) and records final per-source failures in the system's status bits, so an
+// NVE step needs no separate integrator or status launches.
+//
 // Roofline: this kernel is bound by the FP64 pipe and latency (scalar double arithmetic on irregular,
 // data-dependent work); its per-source footprint is a few KB of scratch plus mesh reads, mostly L2-resident.
 #include <math_constants.h>
