@@ -176,6 +176,23 @@ def fp64_peak_gflops(ctx: Context) -> float:
     return out.value
 
 
+def pairs_to_neighbor_lists(n, i, j, d, t):
+    """Group pair records (source i, target j, distance d, start tangent t; grouped by source as cssg_system_pairs
+    returns them) into simpleModel's per-particle lists: (neighbors, neighborVectors, neighborDistances).  Pairs the
+    learned screen skipped (j < 0, index -j - 1) keep their index with distance +inf."""
+    neighbors = [[] for _ in range(n)]
+    vectors = [[] for _ in range(n)]
+    distances = [[] for _ in range(n)]
+    for a, b, dist, tan in zip(np.asarray(i), np.asarray(j), np.asarray(d), np.asarray(t).reshape(-1, 3)):
+        if not 0 <= a < n:
+            continue
+        screened = b < 0
+        neighbors[a].append(int(-b - 1 if screened else b))
+        vectors[a].append(np.array(tan, dtype=np.float64))
+        distances[a].append(math.inf if screened else float(dist))
+    return neighbors, vectors, distances
+
+
 def make_params(integrator="nve", force="harmonic", k=1.0, sigma=1.0, range_=None, submesh=False, max_dist=None,
                 cutoff=None, dt=0.001, temperature=0.0, tau=1.0, chain_length=2):
     p = cssg_params()
@@ -309,6 +326,16 @@ class System:
         check(L.cssg_system_pairs(self.h, m, _np_ptr(i), _np_ptr(j), _np_ptr(d), _np_ptr(t), ctypes.byref(cnt)),
               "pairs")
         return i, j, d, t
+
+    def neighbors(self):
+        """simpleModel::findNeighbors (simpleModel.cpp:68-112) for analysis: forces at the current state, then the
+        neighbour lists (indices, start tangents, distances; +inf beyond the force cutoff) from the pair records."""
+        if not getattr(self, "_pairs_on", False):
+            self.enable_pairs()
+            self._pairs_on = True
+        self.compute_forces()
+        i, j, d, t = self.pairs()
+        return pairs_to_neighbor_lists(self.n, i, j, d, t)
 
     def chain(self):
         cap = (4 * (max(1, self.params.chain_length) + 1) + 2) * self.K

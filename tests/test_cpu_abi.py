@@ -72,3 +72,20 @@ def test_null_handles_are_argument_errors_without_gpu():
         assert name.encode() in L.cssg_last_error(), (name, L.cssg_last_error())
     for name in ("cssg_system_destroy", "cssg_mesh_destroy", "cssg_ctx_destroy"):
         assert getattr(L, name)(N) == 0, name
+
+
+def test_pairs_to_neighbor_lists():
+    """api.pairs_to_neighbor_lists groups pair records into simpleModel's lists (no GPU involved)."""
+    import math
+
+    import numpy as np
+
+    from curvedspacesim_gb300 import api
+    i = np.array([0, 0, 2, 2, 2])
+    j = np.array([1, 2, 0, -2, 3])
+    d = np.array([0.1, 0.2, 0.2, 0.9, math.inf])
+    t = np.arange(15, dtype=np.float64)
+    nb, nv, nd = api.pairs_to_neighbor_lists(4, i, j, d, t)
+    assert nb == [[1, 2], [], [0, 1, 3], []]
+    assert nd[0] == [0.1, 0.2] and nd[2][1] == math.inf and nd[2][2] == math.inf
+    assert np.array_equal(nv[2][1], [9.0, 10.0, 11.0])
