@@ -48,6 +48,7 @@ const char* cssg_version(void);
  * defines the barycentric order of positions on that face).  Builds adjacency, edge frames, vertex rings, angle
  * sums and the bounding box on the host and uploads them. */
 int cssg_mesh_create(const double* vertices_host, int nV, const int* faces_host, int nF, int device, cssg_mesh** out);
+/* Releases the mesh (the reference's triangulatedMeshSpace destructor). */
 int cssg_mesh_destroy(cssg_mesh* mesh);
 /* area (triangulatedMeshSpace::getArea, :153), bbox_host[6] = min xyz, max xyz with the origin included (:6-30). */
 int cssg_mesh_info(const cssg_mesh* mesh, int* nV, int* nF, double* area, double* bbox_host);
@@ -61,7 +62,8 @@ int cssg_mesh_info(const cssg_mesh* mesh, int* nV, int* nF, double* area, double
 int cssg_mesh_set_boundary(cssg_mesh* mesh, int bc);
 
 /* ---- context ----------------------------------------------------------------------------------------------- */
-/* stream: a cudaStream_t, or NULL to create a private non-blocking stream. */
+/* No reference counterpart (the reference is single-threaded host code): a device and a stream for batched calls.
+ * stream: a cudaStream_t, or NULL to create a private non-blocking stream. */
 int cssg_ctx_create(int device, void* stream, cssg_ctx** out);
 int cssg_ctx_destroy(cssg_ctx* ctx);
 int cssg_ctx_synchronize(cssg_ctx* ctx);
@@ -132,6 +134,8 @@ typedef struct cssg_params {
     int chain_length;    /* NVT chain length M (default 2) */
 } cssg_params;
 
+/* simpleModel(n) + setSpace + setNeighborStructure (src/models/simpleModel.h:29-38), a force (baseForce.h) and an
+ * updater (velocityVerletNVE.h / noseHooverNVT.h) bound into one device-resident system; state starts at zero. */
 int cssg_system_create(cssg_ctx* ctx, const cssg_mesh* mesh, int n, const cssg_params* params, cssg_system** out);
 /* K independent systems (own mesh, particle count and force / patch parameters) advanced together: every kernel of
  * a step serves all of them (one persistent geodesic launch per step over all sources).  Integrator, dt, T, tau,
@@ -139,6 +143,7 @@ int cssg_system_create(cssg_ctx* ctx, const cssg_mesh* mesh, int n, const cssg_p
  * system_* calls are the concatenation of the systems' particles in order. */
 int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh* const* meshes, const int* counts,
                                const cssg_params* params, cssg_system** out);
+/* Releases the system (no reference counterpart beyond the objects' destructors). */
 int cssg_system_destroy(cssg_system* sys);
 /* simpleModel::setParticlePositions (simpleModel.cpp:204-212) + velocities/forces; host arrays; nullable fields
  * are left unchanged.  Synchronises. */
@@ -147,9 +152,10 @@ int cssg_system_set_state(cssg_system* sys, const int* face_host, const double* 
 /* noseHooverNVT::setBathVariables (noseHooverNVT.cpp:28-36): chain masses from N, T, tau; chain at rest.  Called by
  * cssg_system_create; call again after replacing the particles of an NVT system. */
 int cssg_system_reset_thermostat(cssg_system* sys);
-/* Copies the state to host arrays (nullable) and synchronises. */
+/* The model's public state vectors positions / velocities / forces (simpleModel.h:67-74) copied to host arrays
+ * (nullable) and synchronises. */
 int cssg_system_get_state(cssg_system* sys, int* face_host, double* bary_host, double* vel_host, double* force_host);
-/* Device pointers of the state arrays (face[n], bary[3n], vel[3n], force[3n]). */
+/* Device pointers of the state arrays (face[n], bary[3n], vel[3n], force[3n]); no reference counterpart. */
 int cssg_system_device_state(cssg_system* sys, int** face, double** bary, double** vel, double** force);
 /* simulation::performTimestep x steps (simulation.cpp:84-95); asynchronous on the context stream.  use_graph=1
  * replays one captured CUDA graph per step. */
@@ -213,34 +219,38 @@ int cssg_system_set_tuning(cssg_system* sys, double delta_scale, int warps_per_b
  * warps_per_sm, lpt_order, ms per force evaluation, warps_per_source, wide_registers}.  Synchronises the context's
  * stream. */
 int cssg_system_autotune(cssg_system* sys, int reps, double* result_host);
-/* Error summary since the last call (synchronises): OR of (1 << CSSG_ST_*) over walks and sources, and counters
- * out_host[4] = {walk crossings, windows processed, vertex launches, in-range pairs} (nullable). */
+/* The reference throws at the first failing walk or geodesic (ERRORERROR, inc/debuggingHelp.h:19-31); here failures
+ * are collected. Error summary since the last call (synchronises): OR of (1 << CSSG_ST_*) over walks and sources,
+ * and counters out_host[4] = {walk crossings, windows processed, vertex launches, in-range pairs} (nullable). */
 int cssg_system_check(cssg_system* sys, int* status_bits, unsigned long long* counters_host);
-/* Pair data of the last force evaluation, host arrays with capacity cap: source i, target j, distance, start
- * tangent (3).  Returns the number of candidate pairs in *count (which may exceed cap). */
+/* simpleModel's neighbors / neighborDistances / neighborVectors (simpleModel.h:55-60, filled by findNeighbors,
+ * simpleModel.cpp:68-112): pair data of the last force evaluation, host arrays with capacity cap: source i, target j,
+ * distance, start tangent (3).  Returns the number of candidate pairs in *count (which may exceed cap).  The first
+ * call switches pair recording on (later force evaluations record) and returns 0 pairs. */
 int cssg_system_pairs(cssg_system* sys, int cap, int* i_host, int* j_host, double* d_host, double* t_host, int* count);
-/* Nose-Hoover chain state, per system: (M+1) x 4 bath variables + {kinetic energy, scale factor}, host array of
- * K * (4 (M+1) + 2) doubles. */
+/* noseHooverNVT's bathVariables (noseHooverNVT.h:39-40) plus its KE and scale: Nose-Hoover chain state, per
+ * system: (M+1) x 4 bath variables + {kinetic energy, scale factor}, host array of K * (4 (M+1) + 2) doubles. */
 int cssg_system_chain(cssg_system* sys, double* chain_host, int capacity);
-/* Timing of the last step() call: milliseconds of the dominant kernel (geodesic+force) and of the walk, from
- * CUDA events on the system stream (filled when timing is enabled with cssg_system_timing(sys, 1)). */
+/* No reference counterpart (profiling). Timing of the last step() call: milliseconds of the dominant kernel
+ * (geodesic+force) and of the walk, from CUDA events on the system stream (filled when timing is enabled with
+ * cssg_system_timing(sys, 1)). */
 int cssg_system_timing(cssg_system* sys, int enable);
 int cssg_system_last_times(cssg_system* sys, double* ms_host, int capacity);
-/* Learned screen for the system's force pass (cell-list systems): enable = 1 uploads params_host
- * (cssg_mlp_param_count() FP32 values) and skips candidate pairs whose predicted distance |chord| + sigma * yhat
- * exceeds sigma * (1 + margin); their faces still complete the reference patch, so the patch and every computed
- * distance stay exact.  enable = 0 returns to the plain exact path. */
+/* No reference counterpart. Learned screen for the system's force pass (cell-list systems): enable = 1 uploads
+ * params_host (cssg_mlp_param_count() FP32 values) and skips candidate pairs whose predicted distance |chord| +
+ * sigma * yhat exceeds sigma * (1 + margin); their faces still complete the reference patch, so the patch and every
+ * computed distance stay exact. enable = 0 returns to the plain exact path. */
 int cssg_system_set_screen(cssg_system* sys, const float* params_host, double margin, int enable);
-/* Screen counters since the last call: out_host[3] = {candidate pairs, screened-out pairs, tensor-core wait
- * failures}.  Synchronises and resets. */
+/* No reference counterpart. Screen counters since the last call: out_host[3] = {candidate pairs, screened-out pairs,
+ * tensor-core wait failures}. Synchronises and resets. */
 int cssg_system_screen_counters(cssg_system* sys, unsigned long long* out_host);
-/* Number of kernels one step() launches (the integrator's fixed sequence). */
+/* No reference counterpart.  Number of kernels one step() launches (the integrator's fixed sequence). */
 int cssg_system_kernels_per_step(cssg_system* sys, int* count);
 
 /* ---- diagnostics ------------------------------------------------------------------------------------------------
- * Measured FP64 fused-multiply-add issue rate of the device (GFLOP/s, 2 flops per FMA), from a register-resident
- * dependent-chain kernel timed with CUDA events on the context stream; the denominator of the FP64 roofline of the
- * geodesic kernel.  Synchronises. */
+ * No reference counterpart.  Measured FP64 fused-multiply-add issue rate of the device (GFLOP/s, 2 flops per FMA),
+ * from a register-resident dependent-chain kernel timed with CUDA events on the context stream; the denominator of
+ * the FP64 roofline of the geodesic kernel.  Synchronises. */
 int cssg_diag_fp64_peak(cssg_ctx* ctx, double* gflops_host);
 /* The reciprocal the propagation uses for geometric denominators (Newton-Raphson from a float seed), on n device
  * doubles: out[i] = 1/x[i] within a few ulps.  For accuracy tests. */
