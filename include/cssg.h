@@ -134,7 +134,7 @@ typedef struct cssg_params {
     int chain_length;    /* NVT chain length M (default 2) */
 } cssg_params;
 
-/* simpleModel(n) + setSpace + setNeighborStructure (src/models/simpleModel.h:29-38), a force (baseForce.h) and an
+/* simpleModel(n) + setSpace + setNeighborStructure (src/models/simpleModel.h:29-39), a force (baseForce.h) and an
  * updater (velocityVerletNVE.h / noseHooverNVT.h) bound into one device-resident system; state starts at zero. */
 int cssg_system_create(cssg_ctx* ctx, const cssg_mesh* mesh, int n, const cssg_params* params, cssg_system** out);
 /* K independent systems (own mesh, particle count and force / patch parameters) advanced together: every kernel of
@@ -152,7 +152,7 @@ int cssg_system_set_state(cssg_system* sys, const int* face_host, const double* 
 /* noseHooverNVT::setBathVariables (noseHooverNVT.cpp:28-36): chain masses from N, T, tau; chain at rest.  Called by
  * cssg_system_create; call again after replacing the particles of an NVT system. */
 int cssg_system_reset_thermostat(cssg_system* sys);
-/* The model's public state vectors positions / velocities / forces (simpleModel.h:67-74) copied to host arrays
+/* The model's public state vectors positions / velocities / forces (simpleModel.h:68-72) copied to host arrays
  * (nullable) and synchronises. */
 int cssg_system_get_state(cssg_system* sys, int* face_host, double* bary_host, double* vel_host, double* force_host);
 /* Device pointers of the state arrays (face[n], bary[3n], vel[3n], force[3n]); no reference counterpart. */
@@ -223,7 +223,7 @@ int cssg_system_autotune(cssg_system* sys, int reps, double* result_host);
  * are collected. Error summary since the last call (synchronises): OR of (1 << CSSG_ST_*) over walks and sources,
  * and counters out_host[4] = {walk crossings, windows processed, vertex launches, in-range pairs} (nullable). */
 int cssg_system_check(cssg_system* sys, int* status_bits, unsigned long long* counters_host);
-/* simpleModel's neighbors / neighborDistances / neighborVectors (simpleModel.h:55-60, filled by findNeighbors,
+/* simpleModel's neighbors / neighborDistances / neighborVectors (simpleModel.h:75-79, filled by findNeighbors,
  * simpleModel.cpp:68-112): pair data of the last force evaluation, host arrays with capacity cap: source i, target j,
  * distance, start tangent (3).  Returns the number of candidate pairs in *count (which may exceed cap).  The first
  * call switches pair recording on (later force evaluations record) and returns 0 pairs. */

@@ -395,7 +395,7 @@ public:
     double k, sigma, maximumInteractionRange;
 };
 
-//! simpleModel's neighbour lists (simpleModel.h:55-60, filled by findNeighbors, simpleModel.cpp:68-112) from the
+//! simpleModel's neighbour lists (simpleModel.h:75-79, filled by findNeighbors, simpleModel.cpp:68-112) from the
 //! pair records of cssg_system_pairs (grouped by source): per particle the candidate indices, the unit start tangents
 //! (neighborVectors) and the geodesic distances.  Distances beyond the force cutoff are +inf (the device does not
 //! resolve them further); pairs the learned screen skipped (j < 0, index -j - 1) carry their index and +inf.
