@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <atomic>
 #include <string>
 
 #include "../../include/cssg.h"
@@ -58,6 +60,38 @@ __device__ __forceinline__ double rcp_nr(double d)
     r = fma(r, e, r);
     e = fma(-d, r, 1.0);
     return fma(r, e, r);
+}
+
+// Makes `device` current for the lifetime of the object and restores the caller's device afterwards, so an entry
+// point that receives a context works on the context's device whatever device the calling thread had selected.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceScope(int device)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != device) err = cudaSetDevice(device);
+    }
+    ~DeviceScope()
+    {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
+// Raises a kernel's dynamic shared-memory limit to `bytes` once on each device: the limit is a per-device attribute
+// of the function, so a process that uses several devices must set it on each.  Bit d of `mask` records device d
+// (devices past 63 set it on every call).
+template <class Kernel>
+inline cudaError_t cssg_raise_smem_once(std::atomic<unsigned long long>& mask, Kernel* kernel, int bytes, int device)
+{
+    const unsigned long long bit = device >= 0 && device < 64 ? 1ull << device : 0ull;
+    if (bit && (mask.load() & bit)) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) mask.fetch_or(bit);
+    return e;
 }
 
 // error plumbing
@@ -175,7 +209,19 @@ struct GeoLaunch {
     int wideRegs;                // 1: the kernel build with up to 255 registers per thread (fewer warps per SM)
     int* srcCost;                // nullable: work of each source (windows + launches + rounds), for the next order
     int smemTables;              // set by cssg_launch_geodesic: hash tables in shared memory
+    int device;                  // the CUDA device the launch runs on (SM count, occupancy, attributes)
 };
+
+// Table capacities and the per-source work cap of a batched distance call (cssg_distance_batch and
+// cssg_distance_batch_noalloc share this rule, so both run the same kernels with the same tables): targets = the
+// largest candidate list, the rest from the number of faces within reach of a source (patch radius or cutoff), or the
+// whole mesh.  est receives that face estimate.
+struct GeoSizing {
+    GeoCaps caps;
+    long long est;
+    int maxWindows;
+};
+GeoSizing cssg_geo_sizing(const cssg_mesh* mesh, int maxTargets, int submesh, double max_dist, double cutoff);
 
 size_t cssg_geo_slot_bytes(const GeoCaps& c);
 // shared memory one warp's hash tables need (tables go to global scratch when this exceeds the block budget)

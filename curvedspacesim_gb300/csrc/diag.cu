@@ -28,6 +28,8 @@ __global__ void __launch_bounds__(256) fp64_fma_chain(double* out, int iters, do
 extern "C" int cssg_diag_fp64_peak(cssg_ctx* ctx, double* gflops)
 {
     if (!ctx || !gflops) return cssg_bad_args("cssg_diag_fp64_peak");
+    DeviceScope scope(ctx->device);
+    CSSG_CUDA(scope.err);
     int sms = 0;
     CSSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     double* out = nullptr;
@@ -66,6 +68,8 @@ extern "C" int cssg_diag_reciprocal(cssg_ctx* ctx, int n, const double* x, doubl
         cssg_set_error("cssg_diag_reciprocal: bad arguments");
         return CSSG_ERR_ARG;
     }
+    DeviceScope scope(ctx->device);
+    CSSG_CUDA(scope.err);
     if (n) reciprocal_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, x, out);
     CSSG_CUDA(cudaGetLastError());
     return CSSG_OK;

@@ -1649,21 +1649,18 @@ void launch_groups(GeoLaunch L, cudaStream_t s)
     const int wmax = (L.wpbMax > 0 && L.wpbMax < 8) ? L.wpbMax : 8;
     int gpb = std::max(1, wmax / G);
     size_t smem = 0;
+    const int dev = L.device;
     L.smemTables = per <= budget ? 1 : 0;
     if (L.smemTables) {
         gpb = (int)std::max<size_t>(1, std::min<size_t>(gpb, budget / per));
         smem = per * gpb;
-        static size_t configured = 48 * 1024;
-        if (smem > configured) {
-            cudaFuncSetAttribute(geodesic_kernel<G, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
-            configured = budget;
-        }
+        static std::atomic<unsigned long long> configured{0};
+        if (smem > 48 * 1024) cssg_raise_smem_once(configured, geodesic_kernel<G, MINB>, (int)budget, dev);
     }
     // spread the groups evenly over the SMs: sources are FP64-pipe bound per SM, so an SM holding two blocks while
     // another holds one would take twice as long.  Full occupancy = sms * bps blocks; fewer slots than that get
     // fewer groups per block, not fewer blocks.
-    int dev = 0, sms = 1, bps = 1;
-    cudaGetDevice(&dev);
+    int sms = 1, bps = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (L.warpsPerSM > 0) L.nSlots = (int)std::min<long long>(L.nSlots, std::max<long long>(1, (long long)sms * L.warpsPerSM / G));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, geodesic_kernel<G, MINB>, 32 * G * gpb, smem);
@@ -1695,6 +1692,33 @@ void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
     }
 }
 
+GeoSizing cssg_geo_sizing(const cssg_mesh* mesh, int maxTargets, int submesh, double max_dist, double cutoff)
+{
+    GeoSizing z;
+    long long est;
+    double reach = cutoff;
+    if (submesh && max_dist < reach) reach = max_dist;
+    if (reach < 1e30) {
+        double r = reach + mesh->meanEdge;
+        est = (long long)(1.3 * 3.14159265 * r * r / mesh->meanFaceArea) + 32;
+    } else {
+        est = mesh->d.nF;
+    }
+    if (est > mesh->d.nF) est = mesh->d.nF;
+    long long estV = std::min<long long>(mesh->d.nV, est / 2 + 4 * (long long)std::sqrt((double)est) + 16);
+    GeoCaps& caps = z.caps;
+    caps.CT = std::max(32, maxTargets);
+    // whole mesh: the face table holds only target faces; patch: the patch plus the goal faces
+    caps.CF = submesh ? next_pow2(2 * (est + caps.CT) + 64) : next_pow2(2 * caps.CT + 64);
+    caps.CV = next_pow2(2 * estV + 64);
+    caps.CW = (int)std::min<long long>(1 << 22, 16 * est + 1024);
+    caps.CL = (int)std::min<long long>(1 << 20, 2 * estV + 256);
+    caps.CLOG = (int)std::min<long long>(1 << 22, 32 * (long long)caps.CT + 16 * est + 1024);
+    z.est = est;
+    z.maxWindows = (int)std::min<long long>(1 << 30, 400 * est + 100000);
+    return z;
+}
+
 // --------------------------------------------------------------------------------------------------------------------
 // C ABI: batched distance queries (per-source API of triangulatedMeshSpace::distance)
 // --------------------------------------------------------------------------------------------------------------------
@@ -1709,6 +1733,8 @@ extern "C" int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSr
         return CSSG_ERR_ARG;
     }
     if (nSrc == 0) return CSSG_OK;
+    DeviceScope scope(ctx->device);
+    CSSG_CUDA(scope.err);
     cudaStream_t s = ctx->stream;
     // size the per-warp tables: targets = the largest candidate list, the rest from the domain size
     int* dmax = nullptr;
@@ -1718,32 +1744,13 @@ extern "C" int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSr
     CSSG_CUDA(cudaMemcpyAsync(&hmax, dmax, sizeof(int), cudaMemcpyDeviceToHost, s));
     CSSG_CUDA(cudaStreamSynchronize(s));
     CSSG_CUDA(cudaFreeAsync(dmax, s));
-    // domain estimate: faces within reach of the source (patch radius or cutoff), or the whole mesh
-    long long est;
-    double reach = cutoff;
-    if (submesh && max_dist < reach) reach = max_dist;
-    if (reach < 1e30) {
-        double r = reach + mesh->meanEdge;
-        est = (long long)(1.3 * 3.14159265 * r * r / mesh->meanFaceArea) + 32;
-    } else {
-        est = mesh->d.nF;
-    }
-    if (est > mesh->d.nF) est = mesh->d.nF;
-    long long estV = std::min<long long>(mesh->d.nV, est / 2 + 4 * (long long)std::sqrt((double)est) + 16);
-    GeoCaps caps;
-    caps.CT = std::max(32, hmax);
-    // whole mesh: the face table holds only target faces; patch: the patch plus the goal faces
-    caps.CF = submesh ? next_pow2(2 * (est + caps.CT) + 64) : next_pow2(2 * caps.CT + 64);
-    caps.CV = next_pow2(2 * estV + 64);
-    caps.CW = (int)std::min<long long>(1 << 22, 16 * est + 1024);
-    caps.CL = (int)std::min<long long>(1 << 20, 2 * estV + 256);
-    caps.CLOG = (int)std::min<long long>(1 << 22, 32 * (long long)caps.CT + 16 * est + 1024);
-    size_t slotBytes = cssg_geo_slot_bytes(caps);
+    const GeoSizing z = cssg_geo_sizing(mesh, hmax, submesh, max_dist, cutoff);
+    size_t slotBytes = cssg_geo_slot_bytes(z.caps);
     int dev = ctx->device;
     int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    CSSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     size_t freeB = 0, totalB = 0;
-    cudaMemGetInfo(&freeB, &totalB);
+    CSSG_CUDA(cudaMemGetInfo(&freeB, &totalB));
     long long nSlots = std::min<long long>((long long)sms * 16, nSrc);
     long long fit = (long long)(freeB / 4 / slotBytes);
     if (nSlots > fit) nSlots = std::max<long long>(1, fit);
@@ -1752,7 +1759,7 @@ extern "C" int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSr
     CSSG_CUDA(cudaMallocAsync(&scratch, slotBytes * nSlots, s));
     CSSG_CUDA(cudaMallocAsync((void**)&work, sizeof(int), s));
     CSSG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
-    cssg_geo_init_scratch(scratch, slotBytes, (int)nSlots, caps, s);
+    cssg_geo_init_scratch(scratch, slotBytes, (int)nSlots, z.caps, s);
     SysDesc hd;
     memset(&hd, 0, sizeof(hd));
     hd.mesh = mesh->d;
@@ -1781,12 +1788,13 @@ extern "C" int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSr
     L.patchDisconnected = (submesh && !(cutoff < 1e300)) ? 1 : 0;
     L.delta = mesh->meanEdge;
     L.maxRounds = 1 << 16;
-    L.maxWindows = (int)std::min<long long>(1 << 30, 400 * est + 100000);
-    L.caps = caps;
+    L.maxWindows = z.maxWindows;
+    L.caps = z.caps;
     L.scratch = scratch;
     L.slotBytes = slotBytes;
     L.nSlots = (int)nSlots;
     L.workCounter = work;
+    L.device = dev;
     cssg_launch_geodesic(L, s);
     CSSG_CUDA(cudaGetLastError());
     CSSG_CUDA(cudaFreeAsync(dsys, s));

@@ -448,6 +448,9 @@ __global__ void screen_decide(int n, const int* __restrict__ nDev, const float* 
 
 size_t infer_smem() { return sizeof(InferSmem) + 128; }
 
+// devices on which mlp_infer_tc's dynamic shared-memory limit has been raised
+std::atomic<unsigned long long> g_inferSmemSet{0};
+
 }  // namespace
 
 void cssg_launch_screen(const SysDesc* sys, const int* sysOf, int maxPairs, const int* nPairsDev, const int* pi,
@@ -455,11 +458,9 @@ void cssg_launch_screen(const SysDesc* sys, const int* sysOf, int maxPairs, cons
                         float* yhat, unsigned char* skip, double margin, int* errFlag, int sms, cudaStream_t s)
 {
     if (maxPairs <= 0) return;
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem());
-        configured = true;
-    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cssg_raise_smem_once(g_inferSmemSet, mlp_infer_tc, (int)infer_smem(), dev);
     screen_features<<<(maxPairs + 127) / 128, 128, 0, s>>>(sys, sysOf, maxPairs, nPairsDev, pi, pj, face, pos,
                                                             (__nv_bfloat16*)X, chord);
     int tiles = (maxPairs + TILE_M - 1) / TILE_M;
@@ -482,6 +483,8 @@ extern "C" int cssg_screen_features(cssg_ctx* ctx, const cssg_mesh* mesh, double
         return CSSG_ERR_ARG;
     }
     if (nPairs == 0) return CSSG_OK;
+    DeviceScope scope(ctx->device);
+    CSSG_CUDA(scope.err);
     SysDesc hd;
     memset(&hd, 0, sizeof(hd));
     hd.mesh = mesh->d;
@@ -503,12 +506,10 @@ extern "C" int cssg_mlp_infer(cssg_ctx* ctx, const void* X_bf16, int n, const fl
         return CSSG_ERR_ARG;
     }
     if (n == 0) return CSSG_OK;
-    static bool configured = false;
+    DeviceScope scope(ctx->device);
+    CSSG_CUDA(scope.err);
     size_t smem = infer_smem();
-    if (!configured) {
-        CSSG_CUDA(cudaFuncSetAttribute(mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
+    CSSG_CUDA(cssg_raise_smem_once(g_inferSmemSet, mlp_infer_tc, (int)smem, ctx->device));
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     int tiles = (n + TILE_M - 1) / TILE_M;
@@ -527,12 +528,11 @@ extern "C" int cssg_mlp_grad(cssg_ctx* ctx, const void* X_bf16, const float* y, 
         cssg_set_error("cssg_mlp_grad: bad arguments");
         return CSSG_ERR_ARG;
     }
-    static bool configured = false;
+    DeviceScope scope(ctx->device);
+    CSSG_CUDA(scope.err);
     size_t smem = train_smem();
-    if (!configured) {
-        CSSG_CUDA(cudaFuncSetAttribute(mlp_train_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    CSSG_CUDA(cssg_raise_smem_once(configured, mlp_train_fwd_bwd, (int)smem, ctx->device));
     CSSG_CUDA(cudaMemsetAsync(grad, 0, sizeof(float) * NPARAM, ctx->stream));
     if (loss) CSSG_CUDA(cudaMemsetAsync(loss, 0, sizeof(float), ctx->stream));
     mlp_train_fwd_bwd<<<(n + TB - 1) / TB, TB, smem, ctx->stream>>>((const __nv_bfloat16*)X_bf16, y, n, params, grad,
@@ -549,6 +549,8 @@ extern "C" int cssg_mlp_adam(cssg_ctx* ctx, float* params, const float* grad, fl
         cssg_set_error("cssg_mlp_adam: bad arguments");
         return CSSG_ERR_ARG;
     }
+    DeviceScope scope(ctx->device);
+    CSSG_CUDA(scope.err);
     mlp_adam<<<(NPARAM + 255) / 256, 256, 0, ctx->stream>>>(params, grad, m, v, NPARAM, lr, 0.9f, 0.999f, 1e-8f,
                                                             1.0f / batch, step);
     CSSG_CUDA(cudaGetLastError());

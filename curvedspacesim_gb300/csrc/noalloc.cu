@@ -80,13 +80,6 @@ __global__ void max_targets_kernel(int n, const int* __restrict__ off, int* __re
     }
 }
 
-int pow2_at_least(long long x)
-{
-    long long p = 1;
-    while (p < x) p <<= 1;
-    return (int)p;
-}
-
 }  // namespace
 
 extern "C" int cssg_distance_batch_noalloc(cssg_ctx* ctx, const cssg_mesh* mesh, int nSrc, const int* src_face,
@@ -100,6 +93,10 @@ extern "C" int cssg_distance_batch_noalloc(cssg_ctx* ctx, const cssg_mesh* mesh,
         return CSSG_ERR_ARG;
     }
     if (nSrc == 0) return CSSG_OK;
+    // everything below (the symbol lookup included) runs on the context's device, whatever device the calling
+    // thread had selected; the caller's device is restored on return
+    DeviceScope scope(ctx->device);
+    CSSG_CUDA(scope.err);
     Symbols sym;
     if (int rc = symbols_for(ctx->device, sym)) return rc;
     cudaStream_t s = ctx->stream;
@@ -109,25 +106,9 @@ extern "C" int cssg_distance_batch_noalloc(cssg_ctx* ctx, const cssg_mesh* mesh,
     CSSG_CUDA(cudaMemcpyAsync(&hmax, sym.maxTargets, sizeof(int), cudaMemcpyDeviceToHost, s));
     CSSG_CUDA(cudaStreamSynchronize(s));
 
-    // table capacities: the same sizing rule as cssg_distance_batch
-    long long est;
-    double reach = cutoff;
-    if (submesh && max_dist < reach) reach = max_dist;
-    if (reach < 1e30) {
-        double r = reach + mesh->meanEdge;
-        est = (long long)(1.3 * 3.14159265 * r * r / mesh->meanFaceArea) + 32;
-    } else {
-        est = mesh->d.nF;
-    }
-    if (est > mesh->d.nF) est = mesh->d.nF;
-    long long estV = std::min<long long>(mesh->d.nV, est / 2 + 4 * (long long)std::sqrt((double)est) + 16);
-    GeoCaps caps;
-    caps.CT = std::max(32, hmax);
-    caps.CF = submesh ? pow2_at_least(2 * (est + caps.CT) + 64) : pow2_at_least(2 * caps.CT + 64);
-    caps.CV = pow2_at_least(2 * estV + 64);
-    caps.CW = (int)std::min<long long>(1 << 22, 16 * est + 1024);
-    caps.CL = (int)std::min<long long>(1 << 20, 2 * estV + 256);
-    caps.CLOG = (int)std::min<long long>(1 << 22, 32 * (long long)caps.CT + 16 * est + 1024);
+    // table capacities: the sizing rule of cssg_distance_batch (one shared helper)
+    const GeoSizing z = cssg_geo_sizing(mesh, hmax, submesh, max_dist, cutoff);
+    const GeoCaps caps = z.caps;
     const size_t slotBytes = cssg_geo_slot_bytes(caps);
     if (slotBytes > (size_t)CSSG_NOALLOC_SCRATCH_BYTES) {
         cssg_set_error("cssg_distance_batch_noalloc: one propagation slot needs " + std::to_string(slotBytes) +
@@ -171,12 +152,13 @@ extern "C" int cssg_distance_batch_noalloc(cssg_ctx* ctx, const cssg_mesh* mesh,
     L.patchDisconnected = (submesh && !(cutoff < 1e300)) ? 1 : 0;
     L.delta = mesh->meanEdge;
     L.maxRounds = 1 << 16;
-    L.maxWindows = (int)std::min<long long>(1 << 30, 400 * est + 100000);
+    L.maxWindows = z.maxWindows;
     L.caps = caps;
     L.scratch = sym.scratch;
     L.slotBytes = slotBytes;
     L.nSlots = (int)nSlots;
     L.workCounter = sym.work;
+    L.device = ctx->device;
     cssg_launch_geodesic(L, s);
     CSSG_CUDA(cudaGetLastError());
     return CSSG_OK;

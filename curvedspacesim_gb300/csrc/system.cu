@@ -504,6 +504,7 @@ void launch_forces(cssg_system* s, bool kick = false)
     L.groupWarps = s->tuneGroup;
     L.wideRegs = s->tuneWide;
     L.srcCost = s->srcCost;
+    L.device = s->ctx->device;
     if (s->tuneLpt) {
         if (n <= kLptSmallMax) {
             lpt_small<<<1, 1024, 0, st>>>(n, L.order, s->srcCost, s->lptOrder);
@@ -892,6 +893,8 @@ extern "C" int cssg_system_set_state(cssg_system* s, const int* face, const doub
                                      const double* force)
 {
     if (!s) return cssg_bad_args("cssg_system_set_state");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
     if (face) {
@@ -914,6 +917,8 @@ extern "C" int cssg_system_set_state(cssg_system* s, const int* face, const doub
 extern "C" int cssg_system_reset_thermostat(cssg_system* s)
 {
     if (!s) return cssg_bad_args("cssg_system_reset_thermostat");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     return reset_chain(s);
 }
 
@@ -932,6 +937,8 @@ extern "C" int cssg_system_kernels_per_step(cssg_system* s, int* count)
 extern "C" int cssg_system_get_state(cssg_system* s, int* face, double* bary, double* vel, double* force)
 {
     if (!s) return cssg_bad_args("cssg_system_get_state");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
     if (face) CSSG_CUDA(cudaMemcpyAsync(face, s->face, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
@@ -955,6 +962,8 @@ extern "C" int cssg_system_device_state(cssg_system* s, int** face, double** bar
 extern "C" int cssg_system_step(cssg_system* s, int steps, int use_graph)
 {
     if (!s || steps < 0) return cssg_bad_args("cssg_system_step");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
     s->eventsUsed = 0;
     if (use_graph && !s->timing) {
@@ -992,6 +1001,8 @@ extern "C" int cssg_system_step_host(cssg_system* s, int steps, const int* face_
                                      double* vel_out, double* force_out)
 {
     if (!s || steps < 0) return cssg_bad_args("cssg_system_step_host");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
     if (face_in) {
@@ -1020,6 +1031,8 @@ extern "C" int cssg_system_step_host(cssg_system* s, int steps, const int* face_
 extern "C" int cssg_system_compute_forces(cssg_system* s)
 {
     if (!s) return cssg_bad_args("cssg_system_compute_forces");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     s->eventsUsed = 0;
     launch_forces(s);
     CSSG_CUDA(cudaGetLastError());
@@ -1062,6 +1075,8 @@ extern "C" int cssg_system_set_tuning(cssg_system* s, double delta_scale, int wa
 extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_host)
 {
     if (!s) return cssg_bad_args("cssg_system_autotune");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     if (reps < 1) reps = 1;
     cudaStream_t st = s->ctx->stream;
     int sms = 0;
@@ -1158,6 +1173,8 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
 extern "C" int cssg_system_check(cssg_system* s, int* bits, unsigned long long* counters)
 {
     if (!s) return cssg_bad_args("cssg_system_check");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
     int hb = 0;
     unsigned long long hc[8];
@@ -1175,6 +1192,8 @@ extern "C" int cssg_system_check(cssg_system* s, int* bits, unsigned long long* 
 extern "C" int cssg_system_pairs(cssg_system* s, int cap, int* ih, int* jh, double* dh, double* th, int* count)
 {
     if (!s) return cssg_bad_args("cssg_system_pairs");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
     if (!s->pairD) {
         // enable pair output for subsequent force evaluations
@@ -1237,6 +1256,8 @@ extern "C" int cssg_system_chain(cssg_system* s, double* chain, int capacity)
 extern "C" int cssg_system_set_screen(cssg_system* s, const float* params_host, double margin, int enable)
 {
     if (!s) return cssg_bad_args("cssg_system_set_screen");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
     if (enable) {
         if (!s->useCells || !params_host) {
@@ -1287,6 +1308,8 @@ extern "C" int cssg_system_set_screen(cssg_system* s, const float* params_host, 
 extern "C" int cssg_system_screen_counters(cssg_system* s, unsigned long long* out_host)
 {
     if (!s || !out_host) return cssg_bad_args("cssg_system_screen_counters");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     out_host[0] = out_host[1] = out_host[2] = 0;
     if (!s->screenCounters) return CSSG_OK;
     cudaStream_t st = s->ctx->stream;
@@ -1581,6 +1604,8 @@ extern "C" int cssg_system_fire(cssg_system* s, const cssg_fire_params* fp, int 
         cssg_set_error("cssg_system_fire: bad arguments (one system per call object; maximum_iterations >= 0)");
         return CSSG_ERR_ARG;
     }
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
     const int nBlocks = (n + kFireBlock - 1) / kFireBlock;
@@ -1664,6 +1689,8 @@ __global__ void gd_displacement(int n3, const double* __restrict__ f, double* __
 extern "C" int cssg_system_gradient_descent(cssg_system* s, int steps, double delta_t, int transport_velocity)
 {
     if (!s || steps < 0 || !(delta_t >= 0)) return cssg_bad_args("cssg_system_gradient_descent");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
     s->eventsUsed = 0;
@@ -1684,6 +1711,8 @@ extern "C" int cssg_system_stress(cssg_system* s, double* stress_host)
         cssg_set_error("cssg_system_stress: bad arguments (one system per call object)");
         return CSSG_ERR_ARG;
     }
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
     const int nBlocks = (n + 255) / 256;

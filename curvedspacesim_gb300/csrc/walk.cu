@@ -337,9 +337,20 @@ __device__ int transport_one(const DevMesh& M, int& face, double* bary, double* 
     int lastA = -1, lastB = -1;
     double tb[3];
     int iter = 0, cross = 0;
+    // qf: the face whose triangle the target's weights are computed against.  The reference keeps its vertex
+    // positions in vertexPositions, which updateForEdgeIntersection refreshes (by reference) but
+    // updateForVertexIntersection and getBoundaryVertexHeading receive by value: after a vertex crossing the target
+    // is weighed against the triangle of the face before the vertex, and the weights are read in the new face.
+    int qf = f;
     while (true) {
         if (++iter > maxIter) return CSSG_ST_ITER;
-        bary_of(P, target, tb);
+        if (qf == f) {
+            bary_of(P, target, tb);
+        } else {
+            FacePts Q;
+            load_face(M, qf, Q);
+            bary_of(Q, target, tb);
+        }
         near_zero_clamp(tb);
         construct_pt(P, tb, target);
         below_zero_clamp(sb);
@@ -389,9 +400,8 @@ __device__ int transport_one(const DevMesh& M, int& face, double* bary, double* 
                 load_face(M, f, P);
                 bary_of(P, &M.V[3 * v], sb);
                 if (ntv > 0) project_for_boundary_vertex(M, heading, v, w, ns, f, tv, ntv);
-                // the reference hands vertexPositions and sourceNormal to getBoundaryVertexHeading by value, so its
-                // caller keeps the previous face's; here they follow the new face
-                ld3(&M.N[3 * f], ns);
+                // getBoundaryVertexHeading receives vertexPositions and sourceNormal by value, so the caller keeps the
+                // previous face's: qf and ns are not updated here
                 lastA = lastB = -1;
                 if (M.bc == BC_ABSORBING) {
                     for (int c = 0; c < 3; ++c) tb[c] = sb[c];
@@ -450,7 +460,11 @@ __device__ int transport_one(const DevMesh& M, int& face, double* bary, double* 
                 if (M.F[3 * f + k] != inv0 && M.F[3 * f + k] != inv1) inner = M.F[3 * f + k];
             double edge[3], orth[3], inward[3], here[3];
             for (int c = 0; c < 3; ++c) edge[c] = M.V[3 * inv1 + c] - M.V[3 * inv0 + c];
-            cross3(ns, edge, orth);
+            // the absorbing rule recomputes the face normal, the tangential rule uses the loop's sourceNormal
+            double nf[3];
+            if (M.bc == BC_ABSORBING) ld3(&M.N[3 * f], nf);
+            else ld3(ns, nf);
+            cross3(nf, edge, orth);
             normalize3(orth);
             construct_pt(P, sb, here);
             for (int c = 0; c < 3; ++c) inward[c] = M.V[3 * inner + c] - here[c];
@@ -504,6 +518,7 @@ __device__ int transport_one(const DevMesh& M, int& face, double* bary, double* 
         lastA = inv0;
         lastB = inv1;
         f = g;
+        qf = g;
         load_face(M, f, P);
         bary_of(P, sp, sb);
         for (int c = 0; c < 3; ++c) ns[c] = nt[c];
@@ -622,6 +637,8 @@ extern "C" int cssg_transport_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int n,
         cssg_set_error("cssg_transport_batch: bad arguments (at most 4 transported vectors)");
         return CSSG_ERR_ARG;
     }
+    DeviceScope scope(ctx->device);
+    CSSG_CUDA(scope.err);
     cssg_launch_transport(mesh->dself, nullptr, n, face, bary, disp, transport, nTransport, status, crossings, nullptr,
                           ctx->stream);
     CSSG_CUDA(cudaGetLastError());

@@ -518,9 +518,19 @@ int transport_one(const Mesh& M, int& face, double* bary, double* disp, double* 
     double tb[3];
     int iter = 0;
     int cross = 0;
+    // qf: the face whose vertex positions the target's weights are computed against.  The reference keeps them in
+    // vertexPositions, which updateForEdgeIntersection refreshes (by reference, :614-658) but
+    // updateForVertexIntersection (:566-611) and getBoundaryVertexHeading (openMeshSpace.cpp:3-66) receive by value:
+    // after a vertex crossing the next passes weigh the target against the triangle of the face before the vertex
+    // (the weights are then read in the new face by clampAndUpdatePosition, meshUtilities.cpp:170-182).
+    int qf = f;
     while (true) {
         if (++iter > maxIter) return ST_ITER;
-        bary_of(p[0], p[1], p[2], target, tb);
+        {
+            const double* q[3];
+            face_pts(M, qf, q);
+            bary_of(q[0], q[1], q[2], target, tb);
+        }
         near_zero_clamp(tb);
         construct_pt(p[0], p[1], p[2], tb, target);
         below_zero_clamp(sb);
@@ -572,9 +582,8 @@ int transport_one(const Mesh& M, int& face, double* bary, double* disp, double* 
                 face_pts(M, f, p);
                 bary_of(p[0], p[1], p[2], vp(M, v), sb);
                 if (ntv > 0) project_for_boundary_vertex(M, heading, v, w, ns, f, tv, ntv);
-                // the reference hands vertexPositions and sourceNormal to getBoundaryVertexHeading by value, so its
-                // caller keeps the previous face's; here they follow the new face
-                for (int c = 0; c < 3; ++c) ns[c] = M.N[3 * f + c];
+                // getBoundaryVertexHeading receives vertexPositions and sourceNormal by value, so the caller keeps the
+                // previous face's: qf and ns are not updated here
                 lastA = lastB = -1;
                 if (bc == BC_ABSORBING) {
                     for (int c = 0; c < 3; ++c) tb[c] = sb[c];
@@ -634,7 +643,9 @@ int transport_one(const Mesh& M, int& face, double* bary, double* disp, double* 
                 if (M.F[3 * f + k] != inv0 && M.F[3 * f + k] != inv1) inner = M.F[3 * f + k];
             double edge[3], orth[3], inward[3], here[3];
             sub3(vp(M, inv1), vp(M, inv0), edge);
-            cross3(ns, edge, orth);
+            // the absorbing rule recomputes the face normal (absorbingOpenMeshSpace.cpp:14), the tangential rule uses
+            // the loop's sourceNormal (tangentialOpenMeshSpace.cpp:22)
+            cross3(bc == BC_ABSORBING ? &M.N[3 * f] : ns, edge, orth);
             normalize3(orth);
             construct_pt(p[0], p[1], p[2], sb, here);
             sub3(vp(M, inner), here, inward);
@@ -685,6 +696,7 @@ int transport_one(const Mesh& M, int& face, double* bary, double* disp, double* 
         lastA = inv0;
         lastB = inv1;
         f = g;
+        qf = g;
         face_pts(M, f, p);
         bary_of(p[0], p[1], p[2], sp, sb);
         for (int c = 0; c < 3; ++c) ns[c] = nt[c];

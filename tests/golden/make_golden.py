@@ -9,7 +9,7 @@ finds that it crosses two edges and no vertex.
 
 Run where the reference tree is present (it is read here only; the tests use the .npz files):
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py REFERENCE_ROOT
 
 Each tests/golden/<mesh>.npz holds the mesh as read from the .off file (vertex and face order kept, so face indices
 are the reference's) and, per case, the inputs and the oracle's outputs.
@@ -106,7 +106,9 @@ def make(name, path, opts, seed):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_golden.py REFERENCE_ROOT  (the curvedSpaceSim source tree)")
+    ref = sys.argv[1]
     oracle.build()
     for k, (name, opts) in enumerate(MESHES.items()):
         out = make(name, os.path.join(ref, "exampleMeshes", name + ".off"), opts, seed=100 + k)
