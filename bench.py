@@ -52,7 +52,8 @@ def workload_config(name):
     if name == "bumpy_screen":
         return dict(workload="bumpy_sphere7_N20000_nve_patch_screen", mesh=("bumpy", 7, 0), n=20000, sigma=0.02,
                     integrator="nve", submesh=True, range_=0.02, dt=0.002, T=0.1, seed=4, screen=True,
-                    train_seeds=list(range(1, 9)), configs_per_seed=6, holdout_seeds=[9, 10], train_steps=3000)
+                    train_seeds=list(range(1, 9)), configs_per_seed=8, holdout_seeds=[9, 10], train_steps=3000,
+                    audit_every=50)
     if name == "noisy_torus_nvt":
         return dict(workload="noisy_torus1000x500_N100000_nvt_patch", mesh=("noisy_torus", 1000, 500), n=100000,
                     phi=0.5, sigma=None, integrator="nvt", submesh=True, range_=None, dt=0.001, T=0.05, seed=5,
@@ -483,13 +484,67 @@ def _timed_steps(ctx, S, steps, flush, stream, graph=True):
     return [a.elapsed_time(e) for a, e in zip(starts, ends)]
 
 
+def oracle_audit(V, F, sigma, state, gpu_pairs, gpu_force, threads):
+    """The FP64 oracle's neighbour distances and forces on one state, against a GPU pass on the same state:
+    in-range pair sets (d <= sigma), the largest relative distance error over the common pairs, and the largest
+    force difference."""
+    import oracle
+    oracle.build()
+    face, bary = state[0], state[1]
+    OM = oracle.OracleMesh(V, F)
+    off, idx, mc = OM.candidates(face, bary, sigma)
+    d_o, _, _ = OM.neighbor_distances(face, bary, off, idx, mc, 1, sigma, sigma, threads=threads)
+    src = np.repeat(np.arange(len(face)), np.diff(off))
+    ref = {(int(a), int(b)): float(x) for a, b, x in zip(src, idx, d_o) if x <= sigma}
+    gi, gj, gd = gpu_pairs[:3]
+    got = {(int(a), int(b)): float(x) for a, b, x in zip(gi, gj, gd) if b >= 0 and x <= sigma}
+    common = set(ref) & set(got)
+    rel = max([abs(got[k] - ref[k]) / ref[k] for k in common if ref[k] > 0] or [0.0])
+    prm = OM.params(0, k=1.0 / sigma ** 2, sigma=sigma, rng=sigma, submesh=1, max_dist=sigma, cutoff=sigma)
+    f_o, _, _ = OM.forces(face, bary, prm, threads=threads)
+    return {"in_range_pairs": len(ref), "missing_in_range_pairs": len(set(ref) - set(got)),
+            "extra_in_range_pairs": len(set(got) - set(ref)), "pair_sets_identical": set(ref) == set(got),
+            "max_rel_distance_error": rel, "max_abs_force_error": float(np.max(np.abs(gpu_force - f_o))),
+            "tolerance_rel_distance": 1e-6}
+
+
+def screen_bound(ctx, M, sigma, state, pairs):
+    """Upper bound of any screen's saving: the exact solver's windows for every candidate pair against the windows
+    when only the in-range candidates (d <= sigma, known here from the exact pass) are queried, with the same patch
+    radius per source (the reference patch does not depend on the screen)."""
+    from curvedspacesim_gb300 import api
+    face, bary = state[0], state[1]
+    n = len(face)
+    i, j, d = pairs[:3]
+    pos = ms.bary_to_r3(M.V, M.F, face, bary)
+    chord = np.linalg.norm(pos[i] - pos[j], axis=1)
+    thr = np.zeros(n)
+    np.maximum.at(thr, i, chord)
+    thr = np.minimum(thr, sigma)
+    out = {}
+    for name, keep in (("all_candidates", np.ones(len(i), dtype=bool)), ("in_range_only", d <= sigma)):
+        off = np.zeros(n + 1, dtype=np.int64)
+        np.add.at(off, i[keep] + 1, 1)
+        off = np.cumsum(off).astype(np.int32)
+        _, _, _, st = api.distance_batch(ctx, M, face, bary, off, face[j[keep]], bary[j[keep]], submesh=True,
+                                         max_dist=sigma, threshold=thr, cutoff=sigma)
+        if np.any(st != 0):
+            raise RuntimeError(f"screen bound: per-source errors {np.unique(st)}")
+        out[name] = int(api.distance_batch.last_stats[:, 0].sum())
+    return {"windows_all_candidates": out["all_candidates"], "windows_in_range_only": out["in_range_only"],
+            "out_of_range_candidate_pairs": int((d > sigma).sum()), "candidate_pairs": int(len(d)),
+            "max_window_saving": 1.0 - out["in_range_only"] / max(out["all_candidates"], 1)}
+
+
 def run_screen(args, cfg):
-    """Learned distance screen against the plain exact path on the same surface and particles.
+    """Learned distance screen against the plain exact path on the same surface and particles (the metric's
+    workload: bumpy sphere, subdivision 7, N=20,000, sigma 0.02, NVE).
 
     The screen is trained here on exact pairs that the GPU solver produces on other surfaces (train_seeds), with the
     library's own forward/backward/Adam kernels; its skip margin is calibrated on held-out surfaces (holdout_seeds) so
-    that no held-out in-range pair is skipped.  Both paths then step the evaluation surface from the same state; the
-    audit recomputes forces on one common state with both and compares in-range pair sets and distances."""
+    that no held-out in-range pair is skipped.  Both paths then step the evaluation surface from the same state.
+    After the timed steps the screened path's pairs and forces on its final state are audited against the FP64
+    oracle (the CPU restatement of the reference path), and the plain path against the screened one."""
     import torch
     from curvedspacesim_gb300 import api, screen
     world, rank, local, pg = dist_setup()
@@ -511,6 +566,8 @@ def run_screen(args, cfg):
         S = api.System(ctx, M, n, prm)
         S.set_screen(screen.init_params(0), 1e6)
         S.set_state(f, b, vel, np.zeros((n, 3)))
+        if args.tuning:
+            S.set_tuning(*_parse_tuning(args.tuning))
         S.step(max(args.warmup, 1), graph=False)
         torch.cuda.synchronize()
         bits, cnt = S.check()
@@ -535,6 +592,8 @@ def run_screen(args, cfg):
     plain = api.System(ctx, M, n, prm)
     scr = api.System(ctx, M, n, prm)
     scr.set_screen(params, margin)
+    if cfg.get("audit_every"):
+        scr.set_screen_audit(cfg["audit_every"])
     for S in (plain, scr):
         S.set_state(f, b, vel, np.zeros((n, 3)))
     stream = ctx.tstream
@@ -543,14 +602,18 @@ def run_screen(args, cfg):
     tunes = {}
     for name, S in (("plain", plain), ("screened", scr)):
         S.step(max(args.warmup, 1), graph=True)
-        if not args.no_autotune:
+        if args.tuning:
+            S.set_tuning(*_parse_tuning(args.tuning))
+            tunes[name] = {"source": "--tuning", "value": args.tuning}
+        elif not args.no_autotune:
             tunes[name] = S.autotune(reps=3)
-            S.step(1, graph=True)
+        S.step(1, graph=True)
     torch.cuda.synchronize()
     for name, S in (("plain", plain), ("screened", scr)):
         bits, cnt = S.check()
         if bits:
             raise RuntimeError(f"{name}: per-item errors during warm-up: {bits:#x} {cnt}")
+    scr.screen_counters()  # reset: the line reports the timed steps
 
     sampler = ClockSampler(local)
     sampler.start()
@@ -572,33 +635,48 @@ def run_screen(args, cfg):
     value_plain = world * n * args.steps / (t_plain * 1e-3)
     sc = scr.screen_counters()
 
-    # kernel time of the geodesic pass on both paths
-    kt = {}
+    # kernel time of the geodesic passes on both paths (CUDA events on the library's stream, no graph) and the
+    # windows they processed (the kernel's counters)
+    kt, win = {}, {}
     for name, S in (("plain", plain), ("screened", scr)):
+        S.check()
         S.timing(True)
         S.step(args.steps, graph=False)
         torch.cuda.synchronize()
         kt[name] = S.last_times()["geodesic_ms"] / args.steps
         S.timing(False)
+        win[name] = S.check()[1]["windows"] / args.steps
 
-    # audit on one common state: exact vs screened in-range pairs and distances
-    st = plain.get_state()
-    audit_res = {}
-    for S in (plain, scr):
+    # audits on the screened path's final state: screened GPU pass against the FP64 oracle, plain GPU against
+    # screened GPU, and the bound on what any screen could save
+    st = scr.get_state()
+    pairs = {}
+    for name, S in (("plain", plain), ("screened", scr)):
         S.set_state(*st)
         S.enable_pairs()
         S.compute_forces()
-    missing, extra, rel = screen.audit(plain.pairs(), scr.pairs(), sigma)
-    fp = plain.get_state()[3]
-    fs = scr.get_state()[3]
-    audit_res = {"missing_in_range_pairs": len(missing), "extra_in_range_pairs": len(extra),
-                 "max_rel_distance_diff": rel, "max_abs_force_diff": float(np.max(np.abs(fp - fs)))}
+        pairs[name] = S.pairs()
+    f_scr = scr.get_state()[3]
+    f_plain = plain.get_state()[3]
+    threads = os.cpu_count() or 1
+    audit_oracle = oracle_audit(V, F, sigma, st, pairs["screened"], f_scr, threads) if rank == 0 else None
+    missing, extra, rel = screen.audit(pairs["plain"], pairs["screened"], sigma)
+    audit_plain = {"missing_in_range_pairs": len(missing), "extra_in_range_pairs": len(extra),
+                   "max_rel_distance_diff": rel, "max_abs_force_diff": float(np.max(np.abs(f_plain - f_scr)))}
+    bound = screen_bound(ctx, M, sigma, st, pairs["plain"])
+
+    # FP64 roofline of the geodesic kernel (the propagation's bound) on the screened path
+    fp64_peak = api.fp64_peak_gflops(ctx)
+    geo_flops = win["screened"] * FLOPS_PER_WINDOW
+    achieved = geo_flops / (kt["screened"] * 1e-3) / 1e9
+    traffic = TRAFFIC_BYTES.get(cfg["workload"])
 
     # e2e through the C ABI with host state, screened path
     pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
     hf, hb, hv, hfo = pin((n,), torch.int32), pin((n, 3), torch.float64), pin((n, 3), torch.float64), \
         pin((n, 3), torch.float64)
     hf[:], hb[:], hv[:], hfo[:] = scr.get_state()
+    scr.step_host(1, hf, hb, hv, hfo)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     for _ in range(args.steps):
@@ -616,22 +694,41 @@ def run_screen(args, cfg):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": cfg["workload"], "n": n, "integrator": cfg["integrator"], "submesh": True,
                        "graph": True, "l2": "flushed before every timed step (512 MB write)",
-                       "parallelism": f"replicas x{world}", "autotune": tunes or None},
-            "plain": {"value": value_plain, "ms_per_step": t_plain / args.steps, "geodesic_ms": kt["plain"]},
+                       "parallelism": f"replicas x{world}", "autotune": tunes or None,
+                       "screen_audit_every": cfg.get("audit_every")},
+            "plain": {"value": value_plain, "ms_per_step": t_plain / args.steps, "geodesic_ms": kt["plain"],
+                      "windows_per_step": win["plain"]},
             "screened": {"value": value, "ms_per_step": t_scr / args.steps, "geodesic_ms": kt["screened"],
-                         "speedup_vs_plain": value / value_plain, "counters": sc},
+                         "windows_per_step": win["screened"], "speedup_vs_plain": value / value_plain,
+                         "counters": sc},
             "screen": {"training_pairs": n_train, "train_seeds": cfg["train_seeds"],
                        "holdout_seeds": cfg["holdout_seeds"], "margin": margin, "calibration": cal,
                        "holdout_skip_fraction": skip_frac, "holdout_wrongly_skipped": wrong,
-                       "prep_seconds": prep_s},
-            "audit": audit_res,
+                       "prep_seconds": prep_s, "bound": bound},
+            "audit_vs_oracle": audit_oracle,
+            "audit_vs_plain": audit_plain,
             "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": io_bytes,
                     "d2h_bytes_per_step": io_bytes},
             "gpu_launches": scr.kernels_per_step() * args.steps,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "GFLOP/s",
+                         "frac": achieved / fp64_peak, "traffic": int(traffic) if traffic else None,
+                         "kernel": "geodesic (screened path)", "kernel_ms": kt["screened"],
+                         "flops_per_launch": geo_flops, "flops_per_window": FLOPS_PER_WINDOW,
+                         "windows_per_launch": win["screened"],
+                         "peak_source": "measured FP64 FMA chain on this GPU (cssg_diag_fp64_peak); "
+                                        "MEASURED_PEAKS.json has no FP64 entry"},
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
+
+
+def _parse_tuning(text):
+    fields = text.split(",")
+    d, w, m, cap, lpt = fields[:5]
+    g = int(fields[5]) if len(fields) > 5 else 1
+    wide = bool(int(fields[6])) if len(fields) > 6 else False
+    return float(d), int(w), int(m), int(cap), bool(int(lpt)), g, wide
 
 
 def run_mlp(args, cfg):
@@ -752,7 +849,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="torus_nvt")
+    ap.add_argument("--workload", default="bumpy_screen")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (band width 1, 8 warps)")
     ap.add_argument("--tuning", default="",

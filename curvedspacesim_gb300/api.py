@@ -353,6 +353,21 @@ class System:
         check(_lib.load().cssg_system_set_screen(self.h, ptr, float(margin), int(bool(enable))),
               "cssg_system_set_screen")
 
+    def set_work_caps(self, regular: int = 0, medium: int = 0, large: int = 0):
+        """Per-source window caps of the regular, medium and large propagation passes (<= 0 keeps a cap)."""
+        check(_lib.load().cssg_system_set_work_caps(self.h, int(regular), int(medium), int(large)),
+              "cssg_system_set_work_caps")
+
+    def set_screen_audit(self, every: int):
+        """Periodic exact audit of the screen every `every` steps (0: off); a dropped in-range pair switches the
+        screen off on the device (cssg_system_set_screen_audit)."""
+        check(_lib.load().cssg_system_set_screen_audit(self.h, int(every)), "cssg_system_set_screen_audit")
+
+    def screen_audit_status(self):
+        out = np.zeros(3, dtype=np.int64)
+        check(_lib.load().cssg_system_screen_audit_status(self.h, _np_ptr(out)), "cssg_system_screen_audit_status")
+        return {"audits": int(out[0]), "sources_with_dropped_pairs": int(out[1]), "screen_off": bool(out[2])}
+
     def screen_counters(self):
         out = np.zeros(3, dtype=np.uint64)
         check(_lib.load().cssg_system_screen_counters(self.h, _np_ptr(out)), "cssg_system_screen_counters")

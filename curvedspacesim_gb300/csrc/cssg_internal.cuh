@@ -180,6 +180,7 @@ struct GeoLaunch {
     double* teOut;
     int* pairJ;                  // system mode pair output: target particle index (nullable)
     int* pairCount;              // system mode: candidates per source (nullable)
+    int* inRangeOut;             // nullable: per source, pairs with d <= sigma (the screen's audit compares them)
     int pairCap;                 // system mode: pair slots per source
     double* force;               // system mode: force per source (nullable)
     int* status;                 // per source
@@ -238,6 +239,8 @@ void cssg_launch_candidates(const GeoLaunch& L, int n, int cap, int* candJ, int*
 // features + tensor-core MLP + decision for nPairs CSR pairs (pi -> pj): skip[p] = 1 when the predicted distance
 // |chord| + sigma * yhat exceeds sigma * (1 + margin).  X (nPairs x 16 BF16), chord, yhat are caller scratch.
 // maxPairs bounds the launch; the actual count is read from nPairsDev on the device
+// disable (nullable, device int): when set, every pair is kept (the audit's fallback to the exact path)
 void cssg_launch_screen(const SysDesc* sys, const int* sysOf, int maxPairs, const int* nPairsDev, const int* pi,
                         const int* pj, const int* face, const double* pos, void* X, float* chord, const float* params,
-                        float* yhat, unsigned char* skip, double margin, int* errFlag, int sms, cudaStream_t s);
+                        float* yhat, unsigned char* skip, double margin, int* errFlag, int sms, cudaStream_t s,
+                        const int* disable = nullptr);

@@ -846,6 +846,26 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     src.cutoff = D.cutoff;
     double b0[3] = {Lp.srcBary[3 * si], Lp.srcBary[3 * si + 1], Lp.srcBary[3 * si + 2]};
     load_pt(M, src.f0, b0, src.S);
+    if (!isfinite(src.S[0] + src.S[1] + src.S[2])) {
+        // a source whose position is not finite (a NaN barycentric weight): no geodesics, zero force
+        if (t0 == 0) {
+            Lp.status[si] = CSSG_ST_NAN;
+            if (Lp.statusBits) atomicOr(Lp.statusBits, 1 << CSSG_ST_NAN);
+            if (Lp.force) Lp.force[3 * si] = Lp.force[3 * si + 1] = Lp.force[3 * si + 2] = 0;
+            if (Lp.pairCount) Lp.pairCount[si] = 0;
+            if (Lp.inRangeOut) Lp.inRangeOut[si] = 0;
+            if (Lp.srcCost) Lp.srcCost[si] = 1;
+        }
+        if (D.searchMode == 0)
+            for (int o = Lp.candOff[si] + t0; o < Lp.candOff[si + 1]; o += Grp<G>::NT) {
+                Lp.dOut[o] = CUDART_INF;
+                for (int c = 0; c < 3; ++c) {
+                    if (Lp.tsOut) Lp.tsOut[3 * o + c] = 0;
+                    if (Lp.teOut) Lp.teOut[3 * o + c] = 0;
+                }
+            }
+        return;
+    }
     if (t0 == 0) {
         ctl->nA = ctl->nB = ctl->nLA = ctl->nLB = ctl->nLog = ctl->nV = ctl->nF = ctl->nT = ctl->err = 0;
         ctl->nBA = ctl->nBB = ctl->nProc = 0;
@@ -945,6 +965,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     }
     if (nT == 0) {
         if (Lp.srcCost && t0 == 0) Lp.srcCost[si] = 1;
+        if (Lp.inRangeOut && t0 == 0) Lp.inRangeOut[si] = 0;
         if (Lp.force && t0 == 0) {
             Lp.force[3 * si] = Lp.force[3 * si + 1] = Lp.force[3 * si + 2] = 0;  // no kick: zero force
         }
@@ -1416,6 +1437,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
         }
     }
     inRange = gp.sumi(inRange);
+    if (t0 == 0 && Lp.inRangeOut) Lp.inRangeOut[si] = inRange;
     processed = gp.sumi(processed);
     launches = gp.sumi(launches);
     if (t0 == 0 && Lp.srcCost) Lp.srcCost[si] = processed + launches + 8 * round + 1;

@@ -437,13 +437,17 @@ __global__ void mlp_adam(float* __restrict__ params, const float* __restrict__ g
 
 size_t train_smem() { return sizeof(float) * (NPARAM + 3 + 4 * TB * NH + TB * NIN); }
 
+// skip[p] = 1 when the predicted distance |chord| + sigma yhat exceeds sigma (1 + margin); nothing is skipped while
+// *disable is set (the audit found a dropped pair)
 __global__ void screen_decide(int n, const int* __restrict__ nDev, const float* __restrict__ chord,
-                              const float* __restrict__ yhat, double margin, unsigned char* __restrict__ skip)
+                              const float* __restrict__ yhat, double margin, unsigned char* __restrict__ skip,
+                              const int* __restrict__ disable)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (nDev) n = min(n, *nDev);
     if (p >= n) return;
-    skip[p] = ((double)chord[p] + (double)yhat[p] > 1.0 + margin) ? 1 : 0;
+    const bool off = disable && *disable;
+    skip[p] = (!off && (double)chord[p] + (double)yhat[p] > 1.0 + margin) ? 1 : 0;
 }
 
 size_t infer_smem() { return sizeof(InferSmem) + 128; }
@@ -455,7 +459,8 @@ std::atomic<unsigned long long> g_inferSmemSet{0};
 
 void cssg_launch_screen(const SysDesc* sys, const int* sysOf, int maxPairs, const int* nPairsDev, const int* pi,
                         const int* pj, const int* face, const double* pos, void* X, float* chord, const float* params,
-                        float* yhat, unsigned char* skip, double margin, int* errFlag, int sms, cudaStream_t s)
+                        float* yhat, unsigned char* skip, double margin, int* errFlag, int sms, cudaStream_t s,
+                        const int* disable)
 {
     if (maxPairs <= 0) return;
     int dev = 0;
@@ -466,7 +471,7 @@ void cssg_launch_screen(const SysDesc* sys, const int* sysOf, int maxPairs, cons
     int tiles = (maxPairs + TILE_M - 1) / TILE_M;
     mlp_infer_tc<<<std::min(tiles, sms * 4), 128, infer_smem(), s>>>((const __nv_bfloat16*)X, maxPairs, nPairsDev,
                                                                       params, yhat, errFlag);
-    screen_decide<<<(maxPairs + 255) / 256, 256, 0, s>>>(maxPairs, nPairsDev, chord, yhat, margin, skip);
+    screen_decide<<<(maxPairs + 255) / 256, 256, 0, s>>>(maxPairs, nPairsDev, chord, yhat, margin, skip, disable);
 }
 
 // ======================================================================================================================

@@ -332,6 +332,16 @@ struct cssg_system {
     int nCandScanBlocks = 0;
     int* mlpErr = nullptr;
     unsigned long long* screenCounters = nullptr;  // [0] candidate pairs, [1] screened out
+    // periodic exact audit of the screen: every auditEvery-th step runs the screened and the exact force passes on
+    // the same positions (the exact one drives the step) and compares the in-range pair counts per source
+    int auditEvery = 0;
+    long long stepsDone = 0;                       // steps since the audit schedule was set
+    bool auditStep = false;                        // the step being launched or captured is an audit step
+    double* forceAudit = nullptr;                  // n x 3: the screened pass's forces in an audit step
+    int* inRangeScr = nullptr;                     // n: in-range pairs per source, screened pass
+    int* inRangeExact = nullptr;                   // n: the same, exact pass
+    int* screenOff = nullptr;                      // device flag: an audit found a dropped pair; nothing is skipped
+    unsigned long long* auditCounters = nullptr;   // [0] audits run, [1] sources that lost an in-range pair
     // FIRE minimisation (device state, transport buffer, reduction partials) and stress partials
     void* fireState = nullptr;
     double* fireTrans = nullptr;  // n x 2 x 3: force and velocity carried by the walk
@@ -342,6 +352,7 @@ struct cssg_system {
     double* ke = nullptr;
     // graph
     cudaGraphExec_t graphExec = nullptr;
+    cudaGraphExec_t graphAudit = nullptr;  // the audit step's graph (screen with periodic audit)
     double delta = 1e300;  // bucket width of the propagation order (distance-banded rounds)
     // tuning (cssg_system_autotune / cssg_system_set_tuning): band width scale, warps per block, medium-pass slots
     double tuneDelta = 1.0;
@@ -443,14 +454,15 @@ __global__ void __launch_bounds__(1024) lpt_small(int n, const int* __restrict__
     }
 }
 
-// findNeighbors + computeForces into s->force; kick: the velocity-Verlet second half kick of every particle is
-// applied where its force is written (velocityVerletNVE.cpp:23-29)
-void launch_forces(cssg_system* s, bool kick = false)
+// findNeighbors + computeForces into forceOut; kick: the velocity-Verlet second half kick of every particle is
+// applied where its force is written (velocityVerletNVE.cpp:23-29); useScreen: the learned-screen path (else the
+// exact one); inRangeOut (nullable): in-range pairs per source; cells: rebuild the cell list first
+void launch_forces_ex(cssg_system* s, bool kick, bool useScreen, double* forceOut, int* inRangeOut, bool cells)
 {
     cudaStream_t st = s->ctx->stream;
     const int n = s->n;
     const int tb = 256;
-    if (s->useCells) {
+    if (s->useCells && cells) {
         cudaMemsetAsync(s->cellCount, 0, sizeof(int) * (s->totalCells + 1), st);
         cudaMemsetAsync(s->cellCursor, 0, sizeof(int) * s->totalCells, st);
         cell_assign<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->pos, s->dsys, s->sysOf, s->cellOf, s->cellCount);
@@ -464,7 +476,7 @@ void launch_forces(cssg_system* s, bool kick = false)
     cudaMemsetAsync(s->work, 0, 5 * sizeof(int), st);
     GeoLaunch L;
     memset(&L, 0, sizeof(L));
-    L.sys = s->screen ? s->dsysScreen : s->dsys;
+    L.sys = useScreen ? s->dsysScreen : s->dsys;
     L.sysOf = s->sysOf;
     L.nSrc = n;
     L.srcFace = s->face;
@@ -481,7 +493,8 @@ void launch_forces(cssg_system* s, bool kick = false)
     L.pairJ = s->pairJ;
     L.pairCount = s->pairCount;
     L.pairCap = s->pairCap;
-    L.force = s->force;
+    L.force = forceOut;
+    L.inRangeOut = inRangeOut;
     L.status = s->srcStatus;
     L.statusBits = s->statusBits;
     L.kickVel = kick ? s->vel : nullptr;
@@ -516,7 +529,7 @@ void launch_forces(cssg_system* s, bool kick = false)
         }
         L.order = s->lptOrder;
     }
-    if (s->screen) {
+    if (useScreen) {
         // learned screen: candidate rows -> CSR pairs -> features -> tensor-core MLP -> skip flags; the propagation
         // then reads the CSR (screened pairs keep their faces in the patch but are not queried)
         int sms = 0;
@@ -529,7 +542,8 @@ void launch_forces(cssg_system* s, bool kick = false)
         compact_pairs<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->candCap, s->candCount, s->candOff, s->candJPad,
                                                         s->pairI, s->pairJc);
         cssg_launch_screen(s->dsysScreen, s->sysOf, n * s->candCap, s->candOff + n, s->pairI, s->pairJc, s->face,
-                           s->pos, s->X, s->chordS, s->mlpParams, s->yhat, s->skip, s->margin, s->mlpErr, sms, st);
+                           s->pos, s->X, s->chordS, s->mlpParams, s->yhat, s->skip, s->margin, s->mlpErr, sms, st,
+                           s->screenOff);
         count_screened<<<(n * s->candCap + 255) / 256, 256, 0, st>>>(n * s->candCap, s->candOff + n, s->skip,
                                                                     s->screenCounters);
         L.candOff = s->candOff;
@@ -571,6 +585,42 @@ void launch_forces(cssg_system* s, bool kick = false)
     record(s);
 }
 
+void launch_forces(cssg_system* s, bool kick = false)
+{
+    launch_forces_ex(s, kick, s->screen, s->force, nullptr, true);
+}
+
+// Audit of the screen: sources whose screened pass found fewer in-range pairs than the exact pass on the same
+// positions (the screen dropped an in-range pair) are counted, and any such source switches the screen off on the
+// device (screen_decide then keeps every pair).
+__global__ void audit_compare(int n, const int* __restrict__ scr, const int* __restrict__ exact,
+                              unsigned long long* counters, int* off)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool lost = i < n && scr[i] < exact[i];
+    const unsigned m = __ballot_sync(0xffffffffu, lost);
+    if ((threadIdx.x & 31) == 0 && m) {
+        atomicAdd(&counters[1], (unsigned long long)__popc(m));
+        atomicExch(off, 1);
+    }
+    if (i == 0) atomicAdd(&counters[0], 1ull);
+}
+
+// the force evaluation of one step: the plain one, or on an audit step the screened pass (into scratch) and the
+// exact pass (which drives the step), then their comparison
+void launch_step_forces(cssg_system* s, bool kick)
+{
+    if (!(s->screen && s->auditStep)) {
+        launch_forces(s, kick);
+        return;
+    }
+    const int n = s->n;
+    launch_forces_ex(s, false, true, s->forceAudit, s->inRangeScr, true);
+    launch_forces_ex(s, kick, false, s->force, s->inRangeExact, false);
+    audit_compare<<<(n + 255) / 256, 256, 0, s->ctx->stream>>>(n, s->inRangeScr, s->inRangeExact, s->auditCounters,
+                                                               s->screenOff);
+}
+
 // moveParticles with the velocity transported; kick: the velocity-Verlet first half (disp = dt v + dt^2 f / 2,
 // v += dt f / 2, velocityVerletNVE.cpp:14-21) is done by the walk kernel itself
 void launch_walk(cssg_system* s, bool kick = false)
@@ -592,7 +642,7 @@ void launch_step(cssg_system* s)
         // velocityVerletNVE::performUpdate (velocityVerletNVE.cpp:3-29): first half kick + drift inside the walk
         // kernel, second half kick where each force is written
         launch_walk(s, true);
-        launch_forces(s, true);
+        launch_step_forces(s, true);
     } else {
         const int Mc = s->P.chain_length;
         const double T = s->P.temperature;
@@ -600,7 +650,7 @@ void launch_step(cssg_system* s)
         nh_chain<<<(K + 63) / 64, 64, 0, st>>>(s->chains, K, Mc, T, dt);
         nvt_scale<<<(3 * n + tb - 1) / tb, tb, 0, st>>>(n, s->vel, s->chains, Mc, s->sysOf, s->disp, 0.5 * dt);
         launch_walk(s);
-        launch_forces(s);
+        launch_step_forces(s, false);
         nvt_kick<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->vel, s->force, s->disp, dt, 0.5 * dt, s->ke);
         ke_reduce<<<K, KE_BLOCK, 0, st>>>(s->ke, s->dPartBase, s->chains, Mc);
         launch_walk(s);
@@ -874,6 +924,7 @@ extern "C" int cssg_system_destroy(cssg_system* s)
     cudaSetDevice(s->ctx->device);
     cudaStreamSynchronize(s->ctx->stream);
     if (s->graphExec) cudaGraphExecDestroy(s->graphExec);
+    if (s->graphAudit) cudaGraphExecDestroy(s->graphAudit);
     for (cudaEvent_t e : s->events) cudaEventDestroy(e);
     void* ptrs[] = {s->face, s->bary, s->vel, s->force, s->disp, s->pos, s->walkStatus, s->srcStatus,
                     s->statusBits, s->counters, s->cellOf, s->cellCount, s->cellStart, s->cellCursor, s->cellList,
@@ -882,7 +933,8 @@ extern "C" int cssg_system_destroy(cssg_system* s)
                     s->firePartials, s->stressPartials, s->pairD, s->pairT,
                     s->pairJ, s->pairCount, s->chains, s->ke, s->dsys, s->dmeshes, s->sysOf, s->dPartBase,
                     s->mlpParams, s->candJPad, s->candCount, s->maxChord, s->candOff, s->pairI, s->pairJc, s->X,
-                    s->chordS, s->yhat, s->skip, s->candScanBlocks, s->mlpErr, s->screenCounters, s->dsysScreen};
+                    s->chordS, s->yhat, s->skip, s->candScanBlocks, s->mlpErr, s->screenCounters, s->dsysScreen,
+                    s->forceAudit, s->inRangeScr, s->inRangeExact, s->screenOff, s->auditCounters};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -959,6 +1011,28 @@ extern "C" int cssg_system_device_state(cssg_system* s, int** face, double** bar
     return CSSG_OK;
 }
 
+namespace {
+// captures one step (the audit variant when audit is set) into a graph
+int capture_step(cssg_system* s, bool audit, cudaGraphExec_t* out)
+{
+    cudaStream_t st = s->ctx->stream;
+    cudaGraph_t g;
+    s->auditStep = audit;
+    CSSG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    launch_step(s);
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    s->auditStep = false;
+    if (e != cudaSuccess) return cssg_cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return cssg_cuda_fail(e, "cudaGraphInstantiate");
+    }
+    return CSSG_OK;
+}
+}  // namespace
+
 extern "C" int cssg_system_step(cssg_system* s, int steps, int use_graph)
 {
     if (!s || steps < 0) return cssg_bad_args("cssg_system_step");
@@ -966,31 +1040,30 @@ extern "C" int cssg_system_step(cssg_system* s, int steps, int use_graph)
     CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
     s->eventsUsed = 0;
+    const bool audits = s->screen && s->auditEvery > 0;
     if (use_graph && !s->timing) {
-        if (!s->graphExec) {
-            cudaGraph_t g;
-            CSSG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            launch_step(s);
-            cudaError_t e = cudaStreamEndCapture(st, &g);
-            if (e != cudaSuccess) return cssg_cuda_fail(e, "cudaStreamEndCapture");
-            e = cudaGraphInstantiate(&s->graphExec, g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) {
-                s->graphExec = nullptr;
-                return cssg_cuda_fail(e, "cudaGraphInstantiate");
-            }
+        if (!s->graphExec)
+            if (int rc = capture_step(s, false, &s->graphExec)) return rc;
+        if (audits && !s->graphAudit)
+            if (int rc = capture_step(s, true, &s->graphAudit)) return rc;
+        for (int k = 0; k < steps; ++k) {
+            const bool audit = audits && (++s->stepsDone % s->auditEvery) == 0;
+            CSSG_CUDA(cudaGraphLaunch(audit ? s->graphAudit : s->graphExec, st));
         }
-        for (int k = 0; k < steps; ++k) CSSG_CUDA(cudaGraphLaunch(s->graphExec, st));
     } else {
         if (s->timing) {
-            size_t need = (size_t)steps * 6 + 8;
+            size_t need = (size_t)steps * 12 + 8;
             while (s->events.size() < need) {
                 cudaEvent_t e;
                 CSSG_CUDA(cudaEventCreate(&e));
                 s->events.push_back(e);
             }
         }
-        for (int k = 0; k < steps; ++k) launch_step(s);
+        for (int k = 0; k < steps; ++k) {
+            s->auditStep = audits && (++s->stepsDone % s->auditEvery) == 0;
+            launch_step(s);
+            s->auditStep = false;
+        }
     }
     CSSG_CUDA(cudaGetLastError());
     return CSSG_OK;
@@ -1045,6 +1118,10 @@ void drop_graph(cssg_system* s)
     if (s->graphExec) {
         cudaGraphExecDestroy(s->graphExec);
         s->graphExec = nullptr;
+    }
+    if (s->graphAudit) {
+        cudaGraphExecDestroy(s->graphAudit);
+        s->graphAudit = nullptr;
     }
 }
 }  // namespace
@@ -1203,10 +1280,7 @@ extern "C" int cssg_system_pairs(cssg_system* s, int cap, int* ih, int* jh, doub
         if ((rc = alloc((void**)&s->pairD, sizeof(double) * slots)) || (rc = alloc((void**)&s->pairT, sizeof(double) * 3 * slots)) ||
             (rc = alloc((void**)&s->pairJ, sizeof(int) * slots)) || (rc = alloc((void**)&s->pairCount, sizeof(int) * s->n)))
             return rc;
-        if (s->graphExec) {
-            cudaGraphExecDestroy(s->graphExec);
-            s->graphExec = nullptr;
-        }
+        drop_graph(s);
         CSSG_CUDA(cudaMemsetAsync(s->pairCount, 0, sizeof(int) * s->n, st));
         if (count) *count = 0;
         CSSG_CUDA(cudaStreamSynchronize(st));
@@ -1283,8 +1357,14 @@ extern "C" int cssg_system_set_screen(cssg_system* s, const float* params_host, 
                 (rc = alloc((void**)&s->candScanBlocks, sizeof(int) * (s->nCandScanBlocks + 1))) ||
                 (rc = alloc((void**)&s->mlpErr, sizeof(int))) ||
                 (rc = alloc((void**)&s->screenCounters, sizeof(unsigned long long) * 2)) ||
-                (rc = alloc((void**)&s->dsysScreen, sizeof(SysDesc) * s->K)))
+                (rc = alloc((void**)&s->dsysScreen, sizeof(SysDesc) * s->K)) ||
+                (rc = alloc((void**)&s->forceAudit, sizeof(double) * 3 * n)) ||
+                (rc = alloc((void**)&s->inRangeScr, sizeof(int) * n)) ||
+                (rc = alloc((void**)&s->inRangeExact, sizeof(int) * n)) ||
+                (rc = alloc((void**)&s->screenOff, sizeof(int))) ||
+                (rc = alloc((void**)&s->auditCounters, sizeof(unsigned long long) * 2)))
                 return rc;
+            CSSG_CUDA(cudaMemset(s->auditCounters, 0, sizeof(unsigned long long) * 2));
             std::vector<SysDesc> h = s->hsys;
             for (auto& d : h) d.searchMode = 3;
             CSSG_CUDA(cudaMemcpy(s->dsysScreen, h.data(), sizeof(SysDesc) * s->K, cudaMemcpyHostToDevice));
@@ -1293,14 +1373,12 @@ extern "C" int cssg_system_set_screen(cssg_system* s, const float* params_host, 
         }
         CSSG_CUDA(cudaMemcpyAsync(s->mlpParams, params_host, sizeof(float) * cssg_mlp_param_count(),
                                   cudaMemcpyHostToDevice, st));
+        CSSG_CUDA(cudaMemsetAsync(s->screenOff, 0, sizeof(int), st));  // (re-)enabling clears an audit's fallback
         CSSG_CUDA(cudaStreamSynchronize(st));
         s->margin = margin;
     }
     s->screen = enable != 0;
-    if (s->graphExec) {
-        cudaGraphExecDestroy(s->graphExec);
-        s->graphExec = nullptr;
-    }
+    drop_graph(s);
     return CSSG_OK;
 }
 
@@ -1323,6 +1401,44 @@ extern "C" int cssg_system_screen_counters(cssg_system* s, unsigned long long* o
     out_host[0] = h[0];
     out_host[1] = h[1];
     out_host[2] = (unsigned long long)e;
+    return CSSG_OK;
+}
+
+extern "C" int cssg_system_set_work_caps(cssg_system* s, int regular, int medium, int large)
+{
+    if (!s) return cssg_bad_args("cssg_system_set_work_caps");
+    if (regular > 0) s->maxWindows = regular;
+    if (medium > 0) s->midMaxWindows = medium;
+    if (large > 0) s->bigMaxWindows = large;
+    drop_graph(s);
+    return CSSG_OK;
+}
+
+extern "C" int cssg_system_set_screen_audit(cssg_system* s, int every)
+{
+    if (!s || every < 0) return cssg_bad_args("cssg_system_set_screen_audit");
+    s->auditEvery = every;
+    s->stepsDone = 0;
+    drop_graph(s);
+    return CSSG_OK;
+}
+
+extern "C" int cssg_system_screen_audit_status(cssg_system* s, long long* out_host)
+{
+    if (!s || !out_host) return cssg_bad_args("cssg_system_screen_audit_status");
+    out_host[0] = out_host[1] = out_host[2] = 0;
+    if (!s->auditCounters) return CSSG_OK;
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
+    cudaStream_t st = s->ctx->stream;
+    unsigned long long h[2];
+    int off = 0;
+    CSSG_CUDA(cudaMemcpyAsync(h, s->auditCounters, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CSSG_CUDA(cudaMemcpyAsync(&off, s->screenOff, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CSSG_CUDA(cudaStreamSynchronize(st));
+    out_host[0] = (long long)h[0];
+    out_host[1] = (long long)h[1];
+    out_host[2] = off;
     return CSSG_OK;
 }
 

@@ -244,7 +244,25 @@ int cssg_system_set_screen(cssg_system* sys, const float* params_host, double ma
 /* No reference counterpart. Screen counters since the last call: out_host[3] = {candidate pairs, screened-out pairs,
  * tensor-core wait failures}. Synchronises and resets. */
 int cssg_system_screen_counters(cssg_system* sys, unsigned long long* out_host);
-/* No reference counterpart.  Number of kernels one step() launches (the integrator's fixed sequence). */
+/* No reference counterpart (the reference's propagation and walk loops are unbounded, and a failing walk throws:
+ * triangulatedMeshSpace.cpp:474, :534-541).  Per-source work caps of the three propagation passes, in windows
+ * processed: a source that exceeds the regular pass's cap (or its tables) is redone by the medium pass, then by the
+ * large pass; past the large pass's cap it reports CSSG_ST_CAPACITY (cssg_system_check).  Values <= 0 keep the
+ * current cap (set at creation from the expected patch size).  Drops the captured step graph. */
+int cssg_system_set_work_caps(cssg_system* sys, int regular, int medium, int large);
+/* No reference counterpart. Periodic exact audit of the learned screen: with every > 0, every every-th step of
+ * cssg_system_step runs the screened force pass and the plain exact pass on the same positions.  The exact pass
+ * drives that step (its forces, kicks and pair records), so an audited step is always exact; a source whose screened
+ * pass found fewer in-range pairs (d <= sigma) than the exact one means the screen dropped an in-range pair, and then
+ * the screen switches itself off on the device: later force passes keep every candidate pair (the plain exact
+ * results) until cssg_system_set_screen(..., enable = 1) is called again.  every = 0 turns the audit off.  Steps
+ * between audits are not checked.  Drops the captured step graphs. */
+int cssg_system_set_screen_audit(cssg_system* sys, int every);
+/* No reference counterpart. out_host[3] = {audits run, sources that lost an in-range pair to the screen in an audit,
+ * 1 if an audit has switched the screen off}, cumulative since the screen was enabled.  Synchronises. */
+int cssg_system_screen_audit_status(cssg_system* sys, long long* out_host);
+/* No reference counterpart.  Number of kernels one step() launches (the integrator's fixed sequence).  A step that
+ * audits the screen launches the longest-first ordering kernels (0, 1 or 3) + 4 more. */
 int cssg_system_kernels_per_step(cssg_system* sys, int* count);
 
 /* ---- diagnostics ------------------------------------------------------------------------------------------------

@@ -92,6 +92,70 @@ def test_screen_gain_on_thin_torus():
     print(f"thin torus: holdout skip fraction {frac:.3f}, evaluation skipped {sc['screened']} of {sc['pairs']} "
           f"candidate pairs, windows {w_plain} -> {w_scr}")
     assert sc["screened"] > 0
-    # the gain is the propagation the skipped targets no longer hold open; it is small here because the patch and
-    # the remaining targets still need most of the same windows (the count varies slightly run to run)
-    assert w_scr <= w_plain * 1.001
+    # the gain is the propagation the skipped targets no longer hold open: the early exit comes as soon as the kept
+    # targets are settled.  Window counts vary by a few tenths of a percent between runs (the order in which the
+    # threads of a source group take windows), far less than this gain.
+    assert w_scr < 0.97 * w_plain, (w_plain, w_scr)
+
+
+def test_screen_audit_switches_off_a_screen_that_drops_pairs():
+    """Periodic exact audit with automatic fallback (cssg_system_set_screen_audit): a screen with a negative margin
+    skips every candidate pair, in range or not.  The steps before the first audit run with it; the audit step runs
+    the exact pass too, drives the step with it, finds the dropped in-range pairs and switches the screen off on the
+    device, after which the screened system's force passes equal the plain exact path's."""
+    from curvedspacesim_gb300 import api, screen
+    ctx = api.Context(0)
+    sub, n, sigma = 5, 3000, 0.06
+    V, F = ms.bumpy_sphere(sub, amplitude=0.05, seed=0)
+    rng = np.random.default_rng(3)
+    f, b = ms.area_weighted_positions(V, F, n, rng)
+    vel = ms.tangent_velocities(V, F, f, 0.1, rng)
+    M = api.Mesh(V, F)
+    p = api.make_params("nve", "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=sigma, submesh=True,
+                        max_dist=sigma, cutoff=sigma, dt=1e-3)
+
+    def exact_at(state):
+        P = api.System(ctx, M, n, p)
+        P.set_state(*state)
+        P.enable_pairs()
+        P.compute_forces()
+        assert P.check()[0] == 0
+        return P
+
+    # a screen that skips nothing passes its audits and stays on
+    good = api.System(ctx, M, n, p)
+    good.set_state(f, b, vel, np.zeros((n, 3)))
+    good.set_screen(screen.init_params(0), 1e6)
+    good.set_screen_audit(2)
+    good.step(4, graph=True)
+    st = good.screen_audit_status()
+    assert st == {"audits": 2, "sources_with_dropped_pairs": 0, "screen_off": False}, st
+
+    bad = api.System(ctx, M, n, p)
+    bad.set_state(f, b, vel, np.zeros((n, 3)))
+    bad.set_screen(screen.init_params(0), -10.0)
+    bad.set_screen_audit(3)
+    bad.step(2, graph=True)
+    st = bad.screen_audit_status()
+    assert st["audits"] == 0 and not st["screen_off"]
+    assert np.all(bad.get_state()[3] == 0)  # every pair skipped: zero forces
+    bad.step(1, graph=True)  # the audit step
+    st = bad.screen_audit_status()
+    assert st["audits"] == 1 and st["screen_off"] and st["sources_with_dropped_pairs"] > 0, st
+    assert bad.check()[0] == 0
+    # the audited step's forces are the exact ones at its positions
+    state = bad.get_state()
+    np.testing.assert_allclose(state[3], exact_at(state).get_state()[3], atol=1e-12)
+    # after the fallback the screened system computes the exact pairs and forces
+    bad.step(2, graph=True)
+    state = bad.get_state()
+    ref = exact_at(state)
+    bad.set_state(*state)
+    bad.enable_pairs()
+    bad.compute_forces()
+    missing, extra, err = screen.audit(ref.pairs(), bad.pairs(), sigma)
+    assert not missing and not extra and err <= 1e-12
+    np.testing.assert_allclose(bad.get_state()[3], ref.get_state()[3], atol=1e-12)
+    # enabling the screen again clears the fallback
+    bad.set_screen(screen.init_params(0), 1e6)
+    assert not bad.screen_audit_status()["screen_off"]
