@@ -168,6 +168,12 @@ struct GeoLaunch {
     const double* threshold;     // nullable (CSR modes): per-source patch radius
     const int* candJ;            // mode 3: candidate particle index per CSR entry
     const unsigned char* candSkip;  // mode 3: 1 = screened out (its face still completes the patch, not queried)
+    // padded candidate rows of the cell-list search (one-source-per-lane kernel, mode 1): row si holds rowCount[si]
+    // particle indices at rowJ[si * rowCap], rowChord[si] = the largest candidate chord
+    const int* rowJ;
+    const int* rowCount;
+    const double* rowChord;
+    int rowCap;
     // ... or neighbour search (system mode): all particles + the shared cell arrays
     const int* partFace;
     const double* partBary;
@@ -230,6 +236,16 @@ size_t cssg_geo_smem_per_warp(const GeoCaps& c);
 // Fills slots with their initial (empty) state; call once after allocating the scratch.
 void cssg_geo_init_scratch(void* scratch, size_t slotBytes, int nSlots, const GeoCaps& c, cudaStream_t s);
 void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s);
+// ---- one source per lane (lanes.cu) ----------------------------------------------------------------------------------
+// Per-lane table capacities: targets, face table and vertex table (powers of two), window slab.
+struct LaneCaps {
+    int CT, CF, CV, CW;
+};
+size_t cssg_lane_warp_bytes(const LaneCaps& c);
+// The regular propagation pass with one source per lane: L.nSlots warps, each with cssg_lane_warp_bytes(C) of
+// scratch at L.scratch; a warp takes `lanes` (16 or 32) sources at a time.  Sources that overflow go to L.failList.
+void cssg_launch_lanes(const GeoLaunch& L, const LaneCaps& C, int lanes, cudaStream_t s);
+
 // candidate lists for the learned-screen path: per source (warp) the cell-list candidates in reference order,
 // padded rows of `cap` entries; count[i] (> cap: overflow) and the largest candidate chord maxChord[i]
 void cssg_launch_candidates(const GeoLaunch& L, int n, int cap, int* candJ, int* count, double* maxChord,

@@ -332,6 +332,12 @@ struct cssg_system {
     int nCandScanBlocks = 0;
     int* mlpErr = nullptr;
     unsigned long long* screenCounters = nullptr;  // [0] candidate pairs, [1] screened out
+    // regular pass with one source per lane (lanes.cu): lanes per warp (0: the source-group kernel), per-lane
+    // capacities, scratch of nLaneWarps warps
+    int laneLanes = 0;
+    LaneCaps laneCaps{};
+    void* laneScratch = nullptr;
+    int nLaneWarps = 0;
     // periodic exact audit of the screen: every auditEvery-th step runs the screened and the exact force passes on
     // the same positions (the exact one drives the step) and compares the in-range pair counts per source
     int auditEvery = 0;
@@ -454,6 +460,46 @@ __global__ void __launch_bounds__(1024) lpt_small(int n, const int* __restrict__
     }
 }
 
+// the padded candidate rows of the cell-list search (learned screen and one-source-per-lane pass)
+int ensure_candidate_rows(cssg_system* s)
+{
+    if (s->candJPad) return CSSG_OK;
+    const int n = s->n;
+    s->candCap = std::max(32, 2 * s->caps.CT);
+    int rc;
+    if ((rc = alloc((void**)&s->candJPad, sizeof(int) * (size_t)n * s->candCap)) ||
+        (rc = alloc((void**)&s->candCount, sizeof(int) * (n + 1))) || (rc = alloc((void**)&s->maxChord, sizeof(double) * n)))
+        return rc;
+    return CSSG_OK;
+}
+
+// switches the regular pass to one source per lane (16 or 32 lanes per warp) or back to source groups (0); the
+// lane scratch is allocated on first use
+int set_lanes(cssg_system* s, int lanes)
+{
+    if (lanes > 0 && !s->useCells) {
+        cssg_set_error("cssg_system_set_lanes: the one-source-per-lane pass needs the cell-list neighbour structure");
+        return CSSG_ERR_ARG;
+    }
+    if (lanes > 0 && !s->laneScratch) {
+        if (int rc = ensure_candidate_rows(s)) return rc;
+        // per-lane tables from the regular pass's estimates: targets up to the candidate row, faces and vertices of
+        // the expected patch with the regular tables' margins, live windows up to twice the face table
+        LaneCaps& c = s->laneCaps;
+        c.CT = std::min(s->candCap, std::max(16, s->caps.CT));
+        c.CF = s->caps.CF;
+        c.CV = s->caps.CV;
+        c.CW = std::max(64, std::min(s->caps.CW, 2 * s->caps.CF));
+        int sms = 0;
+        CSSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->ctx->device));
+        const long long batches = (s->n + 15) / 16;
+        s->nLaneWarps = (int)std::max<long long>(1, std::min<long long>(batches, (long long)sms * 16));
+        if (int rc = alloc(&s->laneScratch, cssg_lane_warp_bytes(c) * (size_t)s->nLaneWarps)) return rc;
+    }
+    s->laneLanes = lanes;
+    return CSSG_OK;
+}
+
 // findNeighbors + computeForces into forceOut; kick: the velocity-Verlet second half kick of every particle is
 // applied where its force is written (velocityVerletNVE.cpp:23-29); useScreen: the learned-screen path (else the
 // exact one); inRangeOut (nullable): in-range pairs per source; cells: rebuild the cell list first
@@ -552,7 +598,22 @@ void launch_forces_ex(cssg_system* s, bool kick, bool useScreen, double* forceOu
         L.threshold = s->maxChord;
     }
     record(s);
-    cssg_launch_geodesic(L, st);
+    if (s->laneLanes > 0) {
+        // regular pass with one source per lane; without the screen it reads the cell-list candidates as padded rows
+        if (!useScreen) {
+            cssg_launch_candidates(L, n, s->candCap, s->candJPad, s->candCount, s->maxChord, st);
+            L.rowJ = s->candJPad;
+            L.rowCount = s->candCount;
+            L.rowChord = s->maxChord;
+            L.rowCap = s->candCap;
+        }
+        GeoLaunch LL = L;
+        LL.scratch = s->laneScratch;
+        LL.nSlots = s->nLaneWarps;
+        cssg_launch_lanes(LL, s->laneCaps, s->laneLanes, st);
+    } else {
+        cssg_launch_geodesic(L, st);
+    }
     // medium pass: sources of large-patch systems and regular-pass overflows (exits at once when there are none)
     GeoLaunch R = L;
     R.caps = s->midCaps;
@@ -934,7 +995,7 @@ extern "C" int cssg_system_destroy(cssg_system* s)
                     s->pairJ, s->pairCount, s->chains, s->ke, s->dsys, s->dmeshes, s->sysOf, s->dPartBase,
                     s->mlpParams, s->candJPad, s->candCount, s->maxChord, s->candOff, s->pairI, s->pairJc, s->X,
                     s->chordS, s->yhat, s->skip, s->candScanBlocks, s->mlpErr, s->screenCounters, s->dsysScreen,
-                    s->forceAudit, s->inRangeScr, s->inRangeExact, s->screenOff, s->auditCounters};
+                    s->forceAudit, s->inRangeScr, s->inRangeExact, s->screenOff, s->auditCounters, s->laneScratch};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -981,7 +1042,7 @@ extern "C" int cssg_system_kernels_per_step(cssg_system* s, int* count)
     // inference, decisions, counts] + [longest-first order: 1 or 3] + three geodesic passes; NVE: walk (with both
     // kicks folded in) + forces; NVT: chain, scale, walk, forces, kick, KE, walk, chain, scale
     const int lpt = s->tuneLpt ? (s->n <= kLptSmallMax ? 1 : 3) : 0;
-    const int forces = (s->useCells ? 6 : 0) + (s->screen ? 10 : 0) + lpt + 3;
+    const int forces = (s->useCells ? 6 : 0) + (s->screen ? 10 : (s->laneLanes > 0 ? 1 : 0)) + lpt + 3;
     *count = s->P.integrator == 0 ? 1 + forces : 8 + forces;
     return CSSG_OK;
 }
@@ -1213,6 +1274,44 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
                     bm = m;
                 }
             }
+    // the one-source-per-lane pass (16 or 32 sources per warp, cell or longest-first order); the group tuning found
+    // above still serves the sources it hands to the medium and large passes
+    int bLanes = 0;
+    if (s->useCells) {
+        s->tuneDelta = bd;
+        s->tuneWpb = bw;
+        s->tuneWarpsPerSM = bc;
+        s->tuneGroup = bg;
+        s->tuneWide = bx;
+        s->nMidSlots = bm;
+        for (int lanes : {16, 32})
+            for (int lpt = 0; lpt < 2; ++lpt) {
+                if (set_lanes(s, lanes) != CSSG_OK) break;
+                s->tuneLpt = lpt != 0;
+                launch_forces(s);
+                launch_forces(s);  // warm-up (and the longest-first order from a lane-pass evaluation)
+                cudaEventRecord(e0, st);
+                for (int r = 0; r < reps; ++r) launch_forces(s);
+                cudaEventRecord(e1, st);
+                cudaError_t err = cudaEventSynchronize(e1);
+                if (err != cudaSuccess) {
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    return cssg_cuda_fail(err, "cssg_system_autotune");
+                }
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                int bits = 0;
+                cudaMemcpy(&bits, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost);
+                cudaMemset(s->statusBits, 0, sizeof(int));
+                if (bits == 0 && ms < best) {
+                    best = ms;
+                    bLanes = lanes;
+                    bl = lpt != 0;
+                }
+            }
+        set_lanes(s, bLanes);
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     s->timing = timing;
@@ -1340,14 +1439,11 @@ extern "C" int cssg_system_set_screen(cssg_system* s, const float* params_host, 
         }
         const int n = s->n;
         if (!s->mlpParams) {
-            s->candCap = std::max(32, 2 * s->caps.CT);
+            if (int rc = ensure_candidate_rows(s)) return rc;
             size_t slots = (size_t)n * s->candCap;
             int rc;
             s->nCandScanBlocks = (n + SCAN_BLOCK * SCAN_ITEMS - 1) / (SCAN_BLOCK * SCAN_ITEMS);
             if ((rc = alloc((void**)&s->mlpParams, sizeof(float) * cssg_mlp_param_count())) ||
-                (rc = alloc((void**)&s->candJPad, sizeof(int) * slots)) ||
-                (rc = alloc((void**)&s->candCount, sizeof(int) * (n + 1))) ||
-                (rc = alloc((void**)&s->maxChord, sizeof(double) * n)) ||
                 (rc = alloc((void**)&s->candOff, sizeof(int) * (n + 1))) ||
                 (rc = alloc((void**)&s->pairI, sizeof(int) * slots)) ||
                 (rc = alloc((void**)&s->pairJc, sizeof(int) * slots)) ||
@@ -1401,6 +1497,24 @@ extern "C" int cssg_system_screen_counters(cssg_system* s, unsigned long long* o
     out_host[0] = h[0];
     out_host[1] = h[1];
     out_host[2] = (unsigned long long)e;
+    return CSSG_OK;
+}
+
+extern "C" int cssg_system_set_lanes(cssg_system* s, int lanes_per_warp)
+{
+    if (!s || (lanes_per_warp != 0 && lanes_per_warp != 16 && lanes_per_warp != 32))
+        return cssg_bad_args("cssg_system_set_lanes");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
+    if (int rc = set_lanes(s, lanes_per_warp)) return rc;
+    drop_graph(s);
+    return CSSG_OK;
+}
+
+extern "C" int cssg_system_lanes(cssg_system* s, int* lanes_per_warp)
+{
+    if (!s || !lanes_per_warp) return cssg_bad_args("cssg_system_lanes");
+    *lanes_per_warp = s->laneLanes;
     return CSSG_OK;
 }
 

@@ -244,6 +244,14 @@ int cssg_system_set_screen(cssg_system* sys, const float* params_host, double ma
 /* No reference counterpart. Screen counters since the last call: out_host[3] = {candidate pairs, screened-out pairs,
  * tensor-core wait failures}. Synchronises and resets. */
 int cssg_system_screen_counters(cssg_system* sys, unsigned long long* out_host);
+/* No reference counterpart.  Regular propagation pass with one source per lane: lanes_per_warp = 16 or 32 sources
+ * share a warp, each lane solving its own source (every FP64 instruction then serves up to 32 sources; the pass for
+ * many small patches), 0 = source groups of cssg_system_set_tuning's warps_per_source.  Results are the same either
+ * way; sources whose tables overflow are redone by the medium and large source-group passes.  Needs the cell-list
+ * neighbour structure (range > 0).  cssg_system_autotune also tries both lane widths and keeps the fastest choice;
+ * cssg_system_lanes reports the current one.  Drops the captured step graph. */
+int cssg_system_set_lanes(cssg_system* sys, int lanes_per_warp);
+int cssg_system_lanes(cssg_system* sys, int* lanes_per_warp);
 /* No reference counterpart (the reference's propagation and walk loops are unbounded, and a failing walk throws:
  * triangulatedMeshSpace.cpp:474, :534-541).  Per-source work caps of the three propagation passes, in windows
  * processed: a source that exceeds the regular pass's cap (or its tables) is redone by the medium pass, then by the

@@ -76,7 +76,8 @@ def test_nan_position_reaches_system_check(gpu):
 
 
 @pytest.mark.gpu
-def test_propagation_caps_escalate_then_report_capacity(gpu, oracle_mod):
+@pytest.mark.parametrize("lanes", [0, 32])
+def test_propagation_caps_escalate_then_report_capacity(gpu, oracle_mod, lanes):
     """Host-forced tiny work caps: sources that exceed the regular pass's cap are redone by the medium (then large)
     pass with the same results; when every pass's cap is exceeded they report CSSG_ST_CAPACITY."""
     api, ctx = gpu
@@ -88,6 +89,7 @@ def test_propagation_caps_escalate_then_report_capacity(gpu, oracle_mod):
     p = api.make_params("nve", "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=sigma, submesh=True,
                         max_dist=sigma, cutoff=sigma, dt=1e-3)
     S = api.System(ctx, M, n, p)
+    S.set_lanes(lanes)
     S.set_state(f, b, np.zeros((n, 3)), np.zeros((n, 3)))
     S.compute_forces()
     assert S.check()[0] == 0

@@ -43,7 +43,8 @@ def _compare_pairs(i, j, d, src, idx, do, sigma, sources=None):
     return rel
 
 
-def test_bumpy_sphere7_exact_and_screened_match_oracle(gpu, oracle_mod):
+@pytest.mark.parametrize("lanes", [0, 32])
+def test_bumpy_sphere7_exact_and_screened_match_oracle(gpu, oracle_mod, lanes):
     api, ctx = gpu
     from curvedspacesim_gb300 import screen
     bench = _bench()
@@ -70,6 +71,7 @@ def test_bumpy_sphere7_exact_and_screened_match_oracle(gpu, oracle_mod):
 
     for screened in (False, True):
         S = api.System(ctx, M, n, p)
+        S.set_lanes(lanes)
         S.set_state(f, b, vel, np.zeros((n, 3)))
         if screened:
             S.set_screen(params, margin)
@@ -80,11 +82,12 @@ def test_bumpy_sphere7_exact_and_screened_match_oracle(gpu, oracle_mod):
         i, j, d, _ = S.pairs()
         rel = _compare_pairs(i, j, d, src, idx, do, sigma)
         np.testing.assert_allclose(S.get_state()[3], fo, atol=1e-9)
-        print(f"bumpy sphere 7, {'screened' if screened else 'exact'}: {cnt['in_range_pairs']} in-range pairs, "
+        print(f"bumpy sphere 7, lanes {lanes}, {'screened' if screened else 'exact'}: {cnt['in_range_pairs']} pairs, "
               f"max relative distance error {rel:.2e}")
 
 
-def test_batch64_three_steps_match_oracle(gpu, oracle_mod):
+@pytest.mark.parametrize("lanes", [0, 32])
+def test_batch64_three_steps_match_oracle(gpu, oracle_mod, lanes):
     api, ctx = gpu
     bench = _bench()
     cfg = bench.workload_config("batch64")
@@ -95,6 +98,7 @@ def test_batch64_three_steps_match_oracle(gpu, oracle_mod):
     counts = [sy["n"] for sy in systems]
     assert len(systems) == 64 and sum(counts) == 53606
     S = api.System(ctx, meshes, counts, params)
+    S.set_lanes(lanes)
     S.set_state(np.concatenate([sy["f"] for sy in systems]), np.concatenate([sy["b"] for sy in systems]),
                 np.concatenate([sy["vel"] for sy in systems]), np.zeros((sum(counts), 3)))
     S.step(3, graph=True)
@@ -119,7 +123,8 @@ def test_batch64_three_steps_match_oracle(gpu, oracle_mod):
     print(f"64 systems, 3 NVE steps: largest position difference {worst:.2e}")
 
 
-def test_noisy_torus_sampled_sources_match_oracle(gpu, oracle_mod):
+@pytest.mark.parametrize("lanes", [0, 32])
+def test_noisy_torus_sampled_sources_match_oracle(gpu, oracle_mod, lanes):
     api, ctx = gpu
     bench = _bench()
     cfg = bench.workload_config("noisy_torus_nvt")
@@ -129,6 +134,7 @@ def test_noisy_torus_sampled_sources_match_oracle(gpu, oracle_mod):
     p = api.make_params("nvt", "harmonic", k=1.0 / sigma ** 2, sigma=sigma, range_=sigma, submesh=True,
                         max_dist=sigma, cutoff=sigma, dt=cfg["dt"], temperature=cfg["T"])
     S = api.System(ctx, M, n, p)
+    S.set_lanes(lanes)
     S.set_state(f, b, sy["vel"], np.zeros((n, 3)))
     S.enable_pairs()
     S.compute_forces()

@@ -133,12 +133,14 @@ def test_nve_all_to_all_matches_oracle(gpu, oracle_mod, group):
     np.testing.assert_allclose(vg, vo, atol=1e-5)
 
 
-def test_nvt_patch_matches_oracle(gpu, oracle_mod):
+@pytest.mark.parametrize("lanes", [0, 32])
+def test_nvt_patch_matches_oracle(gpu, oracle_mod, lanes):
     """Torus 200x100, N=2000, sigma=cutoff=0.3, patches, Nose-Hoover T=0.05 dt=0.002: 20 steps."""
     api, ctx = gpu
     V, F = ms.torus(200, 100)
     n, sigma, dt, T = 2000, 0.3, 0.002, 0.05
     S, f, b, vel = _system(api, ctx, V, F, n, 2, "nvt", sigma, True, sigma, dt, T)
+    S.set_lanes(lanes)
     S.step(20, graph=True)
     bits, cnt = S.check()
     assert bits == 0, cnt
@@ -154,11 +156,15 @@ def test_nvt_patch_matches_oracle(gpu, oracle_mod):
     np.testing.assert_allclose(S.chain(), ch, rtol=1e-9, atol=1e-12)
 
 
-def test_pair_sets_identical(gpu, oracle_mod):
+@pytest.mark.parametrize("lanes", [0, 16, 32])
+def test_pair_sets_identical(gpu, oracle_mod, lanes):
+    """Torus 200x100, N=2000: in-range pair sets, distances and forces of one force pass against the oracle, with the
+    source-group pass (lanes = 0) and the one-source-per-lane pass (16 or 32 sources per warp)."""
     api, ctx = gpu
     V, F = ms.torus(200, 100)
     n, sigma = 2000, 0.3
     S, f, b, vel = _system(api, ctx, V, F, n, 3, "nvt", sigma, True, sigma, 0.002, 0.05)
+    S.set_lanes(lanes)
     S.enable_pairs()
     S.compute_forces()
     i, j, d, t = S.pairs()
@@ -180,8 +186,8 @@ def test_pair_sets_identical(gpu, oracle_mod):
     np.testing.assert_allclose(fg, fo, atol=1e-11)
 
 
-@pytest.mark.parametrize("group", [1, 4])
-def test_batched_systems_match_oracle(gpu, oracle_mod, group):
+@pytest.mark.parametrize("group,lanes", [(1, 0), (4, 0), (1, 32)])
+def test_batched_systems_match_oracle(gpu, oracle_mod, group, lanes):
     """Three independent systems (different meshes, counts and ranges) in one system object: each must evolve
     exactly as it does alone (velocity Verlet, cell lists, patches, 20 steps; one and four warps per source)."""
     api, ctx = gpu
@@ -201,6 +207,7 @@ def test_batched_systems_match_oracle(gpu, oracle_mod, group):
     S.set_state(np.concatenate([s[2] for s in states]), np.concatenate([s[3] for s in states]),
                 np.concatenate([s[4] for s in states]), np.zeros((sum(counts), 3)))
     S.set_tuning(2.0, 8, 0, 0, True, group)
+    S.set_lanes(lanes)
     S.step(20, graph=True)
     bits, cnt = S.check()
     assert bits == 0, cnt

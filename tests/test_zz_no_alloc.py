@@ -1,5 +1,6 @@
 """cssg_distance_batch_noalloc (fixed file-scope scratch, no allocation) against cssg_distance_batch, both called
-through the C ABI on the same inputs, two calls in a row (the second reuses the scratch the first left behind)."""
+through the C ABI on the same inputs, two calls in a row (the second reuses the scratch the first left behind), and
+against the FP64 oracle on a sample of the sources."""
 import ctypes
 
 import numpy as np
@@ -30,8 +31,11 @@ def _call(L, name, ctx, mesh, args, ns, m, dev, torch):
     return d.cpu().numpy()[:m], ts.cpu().numpy()[:m], te.cpu().numpy()[:m], st.cpu().numpy()
 
 
-@pytest.mark.parametrize("submesh", [0, 1])
-def test_noalloc_matches_distance_batch(submesh):
+@pytest.mark.parametrize("submesh,r", [(0, None), (1, 0.5), (1, 1.5)])
+def test_noalloc_matches_distance_batch(submesh, r, oracle_mod):
+    """Two calls in a row against cssg_distance_batch and against the FP64 oracle.  With r = 1.5 one propagation slot
+    needs a few MiB, so the fixed scratch holds fewer slots than the 16 per SM the allocating call uses: the path
+    that runs with fewer slots is exercised."""
     import torch
     from curvedspacesim_gb300 import _lib, api
     L = _lib.load()
@@ -43,12 +47,11 @@ def test_noalloc_matches_distance_batch(submesh):
     n = 600
     f, b = ms.area_weighted_positions(V, F, n, rng)
     pos = ms.bary_to_r3(V, F, f, b)
-    # candidates: chord < 0.5 (every other particle for the whole-mesh case on a few sources)
+    # candidates: chord < r (every other particle for the whole-mesh case on a few sources)
     if submesh:
-        ns = n
-        r = 0.5
+        ns = n if r < 1 else 200
         lists = [np.nonzero((np.sum((pos - pos[i]) ** 2, axis=1) < r * r) & (np.arange(n) != i))[0]
-                 for i in range(n)]
+                 for i in range(ns)]
         max_dist, cutoff = r, r
     else:
         ns = 8
@@ -64,6 +67,12 @@ def test_noalloc_matches_distance_batch(submesh):
             torch.tensor(f[idx], dtype=torch.int32, device=dev),
             torch.tensor(b[idx], dtype=torch.float64, device=dev),
             submesh, max_dist, cutoff)
+    if submesh:
+        # the scratch must hold fewer slots than the allocating call's min(16 x SMs, sources) in the large case
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        if r > 1:
+            caps_slot = _slot_bytes_estimate(mesh, max(len(x) for x in lists), max_dist)
+            assert (64 << 20) // caps_slot < min(16 * sms, ns), caps_slot
     with ctx.use():
         ref = _call(L, "cssg_distance_batch", ctx, mesh, args, ns, m, dev, torch)
         for _ in range(2):
@@ -74,6 +83,31 @@ def test_noalloc_matches_distance_batch(submesh):
             np.testing.assert_allclose(got[0][fin], ref[0][fin], rtol=RTOL, atol=0)
             np.testing.assert_allclose(got[1][fin], ref[1][fin], rtol=0, atol=1e-12)
             np.testing.assert_allclose(got[2][fin], ref[2][fin], rtol=0, atol=1e-12)
+    # against the FP64 oracle (the CPU restatement of triangulatedMeshSpace::distance / distanceWithSubmeshing)
+    OM = oracle_mod.OracleMesh(V, F)
+    for q in range(0, ns, max(1, ns // 40)):
+        a, e = off[q], off[q + 1]
+        do, tso, teo, _ = OM.distance(f[q], b[q], f[idx[a:e]], b[idx[a:e]], submesh=bool(submesh),
+                                      max_dist=max_dist, cutoff=cutoff)
+        fin = np.isfinite(do)
+        assert np.array_equal(fin, np.isfinite(got[0][a:e]))
+        np.testing.assert_allclose(got[0][a:e][fin], do[fin], rtol=1e-12, atol=1e-13)
+        np.testing.assert_allclose(got[1][a:e][fin], tso[fin], atol=1e-9)
+
+
+def _slot_bytes_estimate(mesh, max_targets, reach):
+    """Bytes of one propagation slot by the distance calls' sizing rule (the table capacities and record sizes of
+    geodesic.cu), for the assertion that the fixed scratch caps the slot count."""
+    import math
+    est = min(mesh.nF, int(1.3 * math.pi * (reach + mesh_mean_edge(mesh)) ** 2 / (mesh.area / mesh.nF)) + 32)
+    CW = min(1 << 22, 16 * est + 1024)
+    CLOG = min(1 << 22, 32 * max(32, max_targets) + 16 * est + 1024)
+    return 64 * (2 * CW + CLOG)  # the window frontiers and the log alone
+
+
+def mesh_mean_edge(mesh):
+    E = np.concatenate([mesh.V[mesh.F[:, k]] - mesh.V[mesh.F[:, (k + 1) % 3]] for k in range(3)])
+    return float(np.linalg.norm(E, axis=1).mean())
 
 
 def test_noalloc_rejects_oversize_slot():
