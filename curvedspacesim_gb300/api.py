@@ -6,8 +6,10 @@ torch's current stream so ordering with torch copies is implicit.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
 import math
+import weakref
 
 import numpy as np
 
@@ -15,6 +17,24 @@ from . import _lib
 from ._lib import check, cssg_params
 
 _P = ctypes.c_void_p
+
+# Library objects still alive at interpreter exit are released in dependency order (systems, then meshes, then
+# contexts) by an exit hook registered after torch's own, so none is released after the CUDA context it uses.
+_live = {"system": weakref.WeakSet(), "mesh": weakref.WeakSet(), "context": weakref.WeakSet()}
+_exit_hook = []
+
+
+def _register(kind, obj):
+    _live[kind].add(obj)
+    if not _exit_hook:
+        atexit.register(_release_all)
+        _exit_hook.append(True)
+
+
+def _release_all():
+    for kind in ("system", "mesh", "context"):
+        for obj in list(_live[kind]):
+            obj.close()
 
 
 def _np_ptr(a):
@@ -49,6 +69,7 @@ class Context:
         check(L.cssg_ctx_create(device, ctypes.c_void_p(self.tstream.cuda_stream), ctypes.byref(h)),
               "cssg_ctx_create")
         self.h = h
+        _register("context", self)
 
     def use(self):
         """Context manager: make the library's stream torch's current stream."""
@@ -61,10 +82,13 @@ class Context:
     def synchronize(self):
         check(_lib.load().cssg_ctx_synchronize(self.h), "cssg_ctx_synchronize")
 
-    def __del__(self):
+    def close(self):
         if getattr(self, "h", None) is not None and _lib._lib is not None:
             _lib._lib.cssg_ctx_destroy(self.h)
-            self.h = None
+        self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 class Mesh:
@@ -90,6 +114,7 @@ class Mesh:
         self.nV, self.nF, self.area = nv.value, nf.value, area.value
         self.bbox = (bbox[:3].copy(), bbox[3:].copy())
         self.boundary = "closed"
+        _register("mesh", self)
         if boundary != "closed":
             self.set_boundary(boundary)
 
@@ -98,10 +123,13 @@ class Mesh:
         check(_lib.load().cssg_mesh_set_boundary(self.h, bc), "cssg_mesh_set_boundary")
         self.boundary = boundary
 
-    def __del__(self):
+    def close(self):
         if getattr(self, "h", None) is not None and _lib._lib is not None:
             _lib._lib.cssg_mesh_destroy(self.h)
-            self.h = None
+        self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def transport_batch(ctx: Context, mesh: Mesh, face, bary, disp, transport=None):
@@ -239,11 +267,15 @@ class System:
             check(L.cssg_system_create_batched(ctx.h, self.K, mh, cn, pa, ctypes.byref(h)),
                   "cssg_system_create_batched")
         self.h = h
+        _register("system", self)
 
-    def __del__(self):
+    def close(self):
         if getattr(self, "h", None) is not None and _lib._lib is not None:
             _lib._lib.cssg_system_destroy(self.h)
-            self.h = None
+        self.h = None
+
+    def __del__(self):
+        self.close()
 
     def set_state(self, face=None, bary=None, vel=None, force=None):
         def prep(a, dt, shape):

@@ -118,6 +118,10 @@ struct Lane {
     float invBw;        // buckets per unit key
     float bw;           // bucket width
     int processed, launches, pops;
+    long long popCap;
+    double b0[3];       // the source's barycentric weights
+    double rmax;        // patch radius
+    bool handedOff;     // passed to the medium-table source-group pass
 };
 
 struct LaneCtx {
@@ -308,70 +312,104 @@ __device__ void lane_propose_from(const LaneCtx& x, const Win& w, int v, double 
     if (d <= x.st.cutoff && lane_launchable(x, v)) queue_vertex(x, h, d);
 }
 
-// ---- one window ----------------------------------------------------------------------------------------------------
-__device__ void lane_window(const LaneCtx& x, int s)
+// ---- one window, in stages (the kernel reconverges the warp between stages) ------------------------------------------
+// The window's frame on its face.
+struct WinGeo {
+    int g, j;
+    double L, cx, cy, tol;
+};
+
+__device__ __forceinline__ WinGeo win_geo(const DevMesh& M, const Win& w)
+{
+    WinGeo q;
+    q.g = w.he >> 2;
+    q.j = w.he & 3;
+    q.L = M.geom[9 * q.g + 3 * q.j];
+    q.cx = M.geom[9 * q.g + 3 * q.j + 1];
+    q.cy = M.geom[9 * q.g + 3 * q.j + 2];
+    q.tol = 1e-12 * q.L;
+    return q;
+}
+
+// Stage 1: load and trim the window in slot s; a dominated window frees its slot.  Returns true if it survives.
+__device__ bool lane_trim(const LaneCtx& x, int s, Win& w)
+{
+    w = x.S.W[s];
+    if (!trim_window(x.M, w, [&](int v) { return lv_label(x, v); })) {
+        free_slot(x, s);
+        return false;
+    }
+    x.st.processed++;
+    return true;
+}
+
+// Stage 2: targets on the window's face: the path through this window
+__device__ void lane_targets(const LaneCtx& x, const Win& w)
 {
     const DevMesh& M = x.M;
-    Lane& st = x.st;
-    Win w = x.S.W[s];
-    if (!trim_window(M, w, [&](int v) { return lv_label(x, v); })) {
-        free_slot(x, s);
-        return;
-    }
-    st.processed++;
-    const int g = w.he >> 2, j = w.he & 3;
-    const double L = M.geom[9 * g + 3 * j], cx = M.geom[9 * g + 3 * j + 1], cy = M.geom[9 * g + 3 * j + 2];
-    const double tol = 1e-12 * L;
-    // targets on g: the path through this window
-    const int fh = lf_find(x, g);
-    if (fh >= 0) {
-        for (int t = (x.S.F[fh].val & (kInDomain - 1)) - 1; t >= 0; t = x.S.T[t].next) {
-            TRec& tr = x.S.T[t];
-            if (tr.idx < 0) continue;  // screened out: not queried
-            const double b1 = tr.b[(j + 1) % 3], b2 = tr.b[(j + 2) % 3];
-            const double px = b1 * L + b2 * cx, py = b2 * cy;
-            if (!ray_hits(w, px, py, tol)) continue;
-            const double l = len2(px - w.sx, py - w.sy);
-            const double d = w.sigma + l;
-            if (!(d < tr.best)) continue;
-            tr.best = d;
-            double dx, dy;
-            start_dir_l(w, px, py, l, dx, dy);
-            tr.dx = dx;
-            tr.dy = dy;
-            if (st.wantTe) {
-                // direction of arrival in R3: the ray in g's edge frame
-                const double* PA = &M.V[3 * M.F[3 * g + j]];
-                const double* PB = &M.V[3 * M.F[3 * g + (j + 1) % 3]];
-                const double* PC = &M.V[3 * M.F[3 * g + (j + 2) % 3]];
-                const double ux = px - w.sx, uy = py - w.sy;
-                for (int c = 0; c < 3; ++c) {
-                    const double ex = (PB[c] - PA[c]) / L;
-                    const double ey = (PC[c] - PA[c] - cx * ex) / cy;
-                    x.S.te[3 * t + c] = (ux * ex + uy * ey) / l;
-                }
+    const WinGeo q = win_geo(M, w);
+    const int fh = lf_find(x, q.g);
+    if (fh < 0) return;
+    for (int t = (x.S.F[fh].val & (kInDomain - 1)) - 1; t >= 0; t = x.S.T[t].next) {
+        TRec& tr = x.S.T[t];
+        if (tr.idx < 0) continue;  // screened out: not queried
+        const double b1 = tr.b[(q.j + 1) % 3], b2 = tr.b[(q.j + 2) % 3];
+        const double px = b1 * q.L + b2 * q.cx, py = b2 * q.cy;
+        if (!ray_hits(w, px, py, q.tol)) continue;
+        const double l = len2(px - w.sx, py - w.sy);
+        const double d = w.sigma + l;
+        if (!(d < tr.best)) continue;
+        tr.best = d;
+        double dx, dy;
+        start_dir_l(w, px, py, l, dx, dy);
+        tr.dx = dx;
+        tr.dy = dy;
+        if (x.st.wantTe) {
+            // direction of arrival in R3: the ray in g's edge frame
+            const double* PA = &M.V[3 * M.F[3 * q.g + q.j]];
+            const double* PB = &M.V[3 * M.F[3 * q.g + (q.j + 1) % 3]];
+            const double* PC = &M.V[3 * M.F[3 * q.g + (q.j + 2) % 3]];
+            const double ux = px - w.sx, uy = py - w.sy;
+            for (int c = 0; c < 3; ++c) {
+                const double ex = (PB[c] - PA[c]) / q.L;
+                const double ey = (PC[c] - PA[c] - q.cx * ex) / q.cy;
+                x.S.te[3 * t + c] = (ux * ex + uy * ey) / l;
             }
         }
     }
-    // vertex proposals: the opposite vertex C when the window's rays reach it, the edge's ends when it covers them
-    const CrossC xc(w, cx, cy);
-    if (xc.rel(w.b0 - tol) <= 0 && xc.rel(w.b1 + tol) >= 0) lane_propose_from(x, w, M.F[3 * g + (j + 2) % 3], cx, cy);
-    if (w.b0 <= tol) lane_propose_from(x, w, M.F[3 * g + j], 0.0, 0.0);
-    if (w.b1 >= L - tol) lane_propose_from(x, w, M.F[3 * g + (j + 1) % 3], L, 0.0);
-    // children through the two other edges; the first reuses this window's slot
+}
+
+// Stage 3: vertex proposals: the opposite vertex C when the window's rays reach it, the edge's ends when it covers
+// them.  k selects one of the three (the kernel runs them as three sub-stages).
+__device__ void lane_proposal(const LaneCtx& x, const Win& w, int k)
+{
+    const DevMesh& M = x.M;
+    const WinGeo q = win_geo(M, w);
+    if (k == 0) {
+        const CrossC xc(w, q.cx, q.cy);
+        if (xc.rel(w.b0 - q.tol) <= 0 && xc.rel(w.b1 + q.tol) >= 0)
+            lane_propose_from(x, w, M.F[3 * q.g + (q.j + 2) % 3], q.cx, q.cy);
+    } else if (k == 1) {
+        if (w.b0 <= q.tol) lane_propose_from(x, w, M.F[3 * q.g + q.j], 0.0, 0.0);
+    } else {
+        if (w.b1 >= q.L - q.tol) lane_propose_from(x, w, M.F[3 * q.g + (q.j + 1) % 3], q.L, 0.0);
+    }
+}
+
+// Stage 4: the child through exit edge C->A (exitBC = false) or B->C (true); *reuse is the processed window's slot
+// while it is free to hold a child (-1 once used).  After the last child the caller frees an unused slot.
+__device__ void lane_child(const LaneCtx& x, const Win& w, bool exitBC, int* reuse)
+{
+    const DevMesh& M = x.M;
+    const WinGeo q = win_geo(M, w);
+    const CrossC xc(w, q.cx, q.cy);
     const double r0 = xc.rel(w.b0), r1 = xc.rel(w.b1);
-    int reuse = s;
-    if (r0 < 0 && M.twin[3 * g + (j + 2) % 3] >= 0) {
-        Win c;
-        make_child(M, w, false, r1 >= 0, c);
-        if (lane_push(x, c, reuse)) reuse = -1;
-    }
-    if (r1 > 0 && M.twin[3 * g + (j + 1) % 3] >= 0) {
-        Win c;
-        make_child(M, w, true, r0 <= 0, c);
-        if (lane_push(x, c, reuse)) reuse = -1;
-    }
-    if (reuse >= 0) free_slot(x, reuse);
+    const bool want = exitBC ? (r1 > 0 && M.twin[3 * q.g + (q.j + 1) % 3] >= 0)
+                             : (r0 < 0 && M.twin[3 * q.g + (q.j + 2) % 3] >= 0);
+    if (!want) return;
+    Win c;
+    make_child(M, w, exitBC, exitBC ? r0 <= 0 : r1 >= 0, c);
+    if (lane_push(x, c, *reuse)) *reuse = -1;
 }
 
 // ---- one pseudo-source launch ----------------------------------------------------------------------------------------
@@ -454,8 +492,9 @@ __device__ int lane_pop(const LaneCtx& x)
     return -1;
 }
 
-// ---- the per-source solve ------------------------------------------------------------------------------------------
-__device__ void lane_solve(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, Lane& st, unsigned long long* cnt)
+// ---- the per-source solve: set-up, propagation steps, results ----------------------------------------------------
+// Targets, patch, source frame and the initial windows.  Returns true when the source has propagation to do.
+__device__ bool lane_setup(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, Lane& st)
 {
     const int si = st.si;
     const SysDesc& D = Lp.sys[Lp.sysOf ? Lp.sysOf[si] : 0];
@@ -465,19 +504,19 @@ __device__ void lane_solve(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, 
     st.processed = st.launches = st.pops = 0;
     st.freeTop = st.wTop = 0;
     st.cur = 0;
+    st.nT = 0;
+    st.handedOff = false;
     st.f0 = Lp.srcFace[si];
     st.cutoff = D.cutoff;
     st.full = !D.submesh;
     st.wantTe = D.searchMode == 0 && Lp.teOut != nullptr;
-    auto to_medium = [&]() {
-        Lp.status[si] = 0;
-        Lp.failList[atomicAdd(Lp.failCount, 1)] = si;
-    };
+    st.popCap = 4LL * Lp.maxWindows + 1024;
     if (D.bigBin && Lp.routeBig && Lp.failList) {
-        to_medium();
-        return;
+        st.handedOff = true;
+        return false;
     }
-    double b0[3] = {Lp.srcBary[3 * si], Lp.srcBary[3 * si + 1], Lp.srcBary[3 * si + 2]};
+    double* b0 = st.b0;
+    for (int c = 0; c < 3; ++c) b0[c] = Lp.srcBary[3 * si + c];
     load_pt(M, st.f0, b0, st.S);
     // empty tables
     for (int k = 0; k < C.CF; ++k) S.F[k].key = -1;
@@ -531,145 +570,160 @@ __device__ void lane_solve(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, 
         if (Lp.pairCount) Lp.pairCount[si] = nT;
     }
     st.nT = nT;
+    st.rmax = rmax;
     if (st.err == CSSG_ST_CAPACITY && Lp.failList) {
-        to_medium();
-        return;
+        st.handedOff = true;
+        return false;
     }
     if (!isfinite(st.S[0] + st.S[1] + st.S[2])) st.err = CSSG_ST_NAN;
-    if (nT > 0 && !st.err) {
-        for (int t = 0; t < nT; ++t) {
-            TRec& tr = S.T[t];
-            load_pt(M, tr.face, tr.b, tr.P);
-            tr.best = CUDART_INF;
-            tr.next = -1;
+    if (nT == 0 || st.err) return false;
+    for (int t = 0; t < nT; ++t) {
+        TRec& tr = S.T[t];
+        load_pt(M, tr.face, tr.b, tr.P);
+        tr.best = CUDART_INF;
+        tr.next = -1;
+    }
+    // ---- domain: the reference patch (faces with a vertex within rmax of the source, from the source face's
+    // neighbours outward; target faces complete it) or the whole mesh ------------------------------------------------
+    bool fresh;
+    if (D.submesh) {
+        const int h0 = lf_insert(x, st.f0, &fresh);
+        if (h0 >= 0) S.F[h0].val |= kInDomain;
+        bool notInF0 = false, notInSeeds = false;
+        int nb[3];
+        for (int k = 0; k < 3; ++k) {
+            const int t = M.twin[3 * st.f0 + k];
+            nb[k] = t < 0 ? -1 : t / 3;
         }
-        // ---- domain: the reference patch (faces with a vertex within rmax of the source, from the source face's
-        // neighbours outward; target faces complete it) or the whole mesh --------------------------------------------
-        bool fresh;
-        if (D.submesh) {
-            const int h0 = lf_insert(x, st.f0, &fresh);
-            if (h0 >= 0) S.F[h0].val |= kInDomain;
-            bool notInF0 = false, notInSeeds = false;
-            int nb[3];
+        for (int t = 0; t < nT; ++t) {
+            const int f = S.T[t].face;
+            if (f != st.f0) {
+                notInF0 = true;
+                if (f != nb[0] && f != nb[1] && f != nb[2]) notInSeeds = true;
+            }
+        }
+        if (notInF0) {
+            int nq = 0;
             for (int k = 0; k < 3; ++k) {
-                const int t = M.twin[3 * st.f0 + k];
-                nb[k] = t < 0 ? -1 : t / 3;
+                if (nb[k] < 0) continue;
+                const int h = lf_insert(x, nb[k], &fresh);
+                if (h < 0) break;
+                S.F[h].val |= kInDomain;
+                if (fresh && notInSeeds) S.bfs[nq++] = nb[k];
             }
-            for (int t = 0; t < nT; ++t) {
-                const int f = S.T[t].face;
-                if (f != st.f0) {
-                    notInF0 = true;
-                    if (f != nb[0] && f != nb[1] && f != nb[2]) notInSeeds = true;
-                }
-            }
-            if (notInF0) {
-                int nq = 0;
-                for (int k = 0; k < 3; ++k) {
-                    if (nb[k] < 0) continue;
-                    const int h = lf_insert(x, nb[k], &fresh);
-                    if (h < 0) break;
-                    S.F[h].val |= kInDomain;
-                    if (fresh && notInSeeds) S.bfs[nq++] = nb[k];
-                }
-                if (notInSeeds) {
-                    const double r2 = rmax * rmax;
-                    for (int q = 0; q < nq && !st.err; ++q) {
-                        const int f = S.bfs[q];
-                        for (int k = 0; k < 3; ++k) {
-                            const int tw = M.twin[3 * f + k];
-                            if (tw < 0) continue;
-                            const int g = tw / 3;
-                            if (lf_find(x, g) >= 0) continue;
-                            bool near = false;
-                            for (int c = 0; c < 3; ++c) {
-                                const double* pv = &M.V[3 * M.F[3 * g + c]];
-                                const double dx = st.S[0] - pv[0], dy = st.S[1] - pv[1], dz = st.S[2] - pv[2];
-                                if (!(dx * dx + dy * dy + dz * dz > r2)) near = true;
-                            }
-                            if (!near) continue;
-                            const int h = lf_insert(x, g, &fresh);
-                            if (h < 0) break;
-                            S.F[h].val |= kInDomain;
-                            if (nq < C.CF) S.bfs[nq++] = g;
-                            else st.err = CSSG_ST_CAPACITY;
+            if (notInSeeds) {
+                const double r2 = rmax * rmax;
+                for (int q = 0; q < nq && !st.err; ++q) {
+                    const int f = S.bfs[q];
+                    for (int k = 0; k < 3; ++k) {
+                        const int tw = M.twin[3 * f + k];
+                        if (tw < 0) continue;
+                        const int g = tw / 3;
+                        if (lf_find(x, g) >= 0) continue;
+                        bool near = false;
+                        for (int c = 0; c < 3; ++c) {
+                            const double* pv = &M.V[3 * M.F[3 * g + c]];
+                            const double dx = st.S[0] - pv[0], dy = st.S[1] - pv[1], dz = st.S[2] - pv[2];
+                            if (!(dx * dx + dy * dy + dz * dz > r2)) near = true;
                         }
+                        if (!near) continue;
+                        const int h = lf_insert(x, g, &fresh);
+                        if (h < 0) break;
+                        S.F[h].val |= kInDomain;
+                        if (nq < C.CF) S.bfs[nq++] = g;
+                        else st.err = CSSG_ST_CAPACITY;
                     }
                 }
             }
         }
-        // target lists per face (in patch mode the target faces complete the patch)
-        for (int t = nT - 1; t >= 0 && !st.err; --t) {
-            const int h = lf_insert(x, S.T[t].face, &fresh);
-            if (h < 0) break;
-            if (D.submesh) S.F[h].val |= kInDomain;
-            S.T[t].next = (S.F[h].val & (kInDomain - 1)) - 1;
-            S.F[h].val = (S.F[h].val & kInDomain) | (t + 1);
-        }
-        // ---- source: frame, face-vertex labels, the three initial windows ---------------------------------------------
-        const int f0 = st.f0;
-        const double L0 = M.geom[9 * f0], cx0 = M.geom[9 * f0 + 1], cy0 = M.geom[9 * f0 + 2];
-        {
-            const double* p0 = &M.V[3 * M.F[3 * f0]];
-            const double* p1 = &M.V[3 * M.F[3 * f0 + 1]];
-            const double* p2 = &M.V[3 * M.F[3 * f0 + 2]];
-            for (int c = 0; c < 3; ++c) st.e1[c] = (p1[c] - p0[c]) / L0;
-            for (int c = 0; c < 3; ++c) st.e2[c] = (p2[c] - p0[c] - cx0 * st.e1[c]) / cy0;
-        }
-        // bucket width: the key range is [0, min(cutoff, 2 x patch radius or 4 x the mean edge)]
-        {
-            double reach = st.cutoff;
-            const double cap = D.submesh ? 2.0 * rmax + 2.0 * D.delta : reach;
-            if (!(reach < cap)) reach = cap;
-            if (!(reach > 0) || !(reach < 1e300)) reach = 64.0 * (D.delta > 0 ? D.delta : 1.0);
-            st.bw = (float)(reach / kBuckets);
-            st.invBw = (float)(kBuckets / reach);
-        }
-        const double P2[3][2] = {{0, 0}, {L0, 0}, {cx0, cy0}};
-        const double S2x = b0[1] * L0 + b0[2] * cx0, S2y = b0[2] * cy0;
-        for (int k = 0; k < 3 && !st.err; ++k) {
-            const int v = M.F[3 * f0 + k];
-            const double dx = P2[k][0] - S2x, dy = P2[k][1] - S2y;
-            const double l = len2(dx, dy);
-            const double* pv = &M.V[3 * v];
-            const double u[3] = {pv[0] - st.S[0], pv[1] - st.S[1], pv[2] - st.S[2]};
-            lane_propose(x, v, sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]), dx / l, dy / l);
-        }
-        for (int k = 0; k < 3 && !st.err; ++k) {
-            const int t = M.twin[3 * f0 + k];
-            if (t < 0) continue;
-            const double L = M.geom[9 * f0 + 3 * k];
-            const double skx = b0[(k + 1) % 3] * L + b0[(k + 2) % 3] * M.geom[9 * f0 + 3 * k + 1];
-            const double sky = b0[(k + 2) % 3] * M.geom[9 * f0 + 3 * k + 2];
-            Win w;
-            w.he = (t / 3) * 4 + t % 3;
-            w.sigma = 0;
-            w.sx = L - skx;
-            w.sy = fmin(-sky, -1e-15 * L);
-            w.b0 = 0;
-            w.b1 = L;
-            const double ddx = P2[(k + 1) % 3][0] - P2[k][0], ddy = P2[(k + 1) % 3][1] - P2[k][1];
-            const double dl = len2(ddx, ddy);
-            w.c = -ddx / dl;
-            w.s = -ddy / dl;
-            lane_push(x, w, -1);
-        }
-        // ---- propagation in key order ----------------------------------------------------------------------------------
-        const long long popCap = 4LL * Lp.maxWindows + 1024;
-        while (!st.err) {
-            const int it = lane_pop(x);
-            if (it < 0) break;
-            if (++st.pops > popCap || st.processed > Lp.maxWindows) {
-                st.err = CSSG_ST_CAPACITY;
-                break;
-            }
-            if (it < C.CW) lane_window(x, it);
-            else lane_launch(x, it - C.CW);
-        }
     }
-    if (st.err == CSSG_ST_CAPACITY && Lp.failList) {
-        to_medium();
+    // target lists per face (in patch mode the target faces complete the patch)
+    for (int t = nT - 1; t >= 0 && !st.err; --t) {
+        const int h = lf_insert(x, S.T[t].face, &fresh);
+        if (h < 0) break;
+        if (D.submesh) S.F[h].val |= kInDomain;
+        S.T[t].next = (S.F[h].val & (kInDomain - 1)) - 1;
+        S.F[h].val = (S.F[h].val & kInDomain) | (t + 1);
+    }
+    // ---- source: frame, face-vertex labels, the three initial windows -------------------------------------------------
+    const int f0 = st.f0;
+    const double L0 = M.geom[9 * f0], cx0 = M.geom[9 * f0 + 1], cy0 = M.geom[9 * f0 + 2];
+    {
+        const double* p0 = &M.V[3 * M.F[3 * f0]];
+        const double* p1 = &M.V[3 * M.F[3 * f0 + 1]];
+        const double* p2 = &M.V[3 * M.F[3 * f0 + 2]];
+        for (int c = 0; c < 3; ++c) st.e1[c] = (p1[c] - p0[c]) / L0;
+        for (int c = 0; c < 3; ++c) st.e2[c] = (p2[c] - p0[c] - cx0 * st.e1[c]) / cy0;
+    }
+    // bucket width: the key range is [0, min(cutoff, 2 x patch radius + 2 mean edges)]
+    {
+        double reach = st.cutoff;
+        const double cap = D.submesh ? 2.0 * rmax + 2.0 * D.delta : reach;
+        if (!(reach < cap)) reach = cap;
+        if (!(reach > 0) || !(reach < 1e300)) reach = 64.0 * (D.delta > 0 ? D.delta : 1.0);
+        st.bw = (float)(reach / kBuckets);
+        st.invBw = (float)(kBuckets / reach);
+    }
+    const double P2[3][2] = {{0, 0}, {L0, 0}, {cx0, cy0}};
+    const double S2x = b0[1] * L0 + b0[2] * cx0, S2y = b0[2] * cy0;
+    for (int k = 0; k < 3 && !st.err; ++k) {
+        const int v = M.F[3 * f0 + k];
+        const double dx = P2[k][0] - S2x, dy = P2[k][1] - S2y;
+        const double l = len2(dx, dy);
+        const double* pv = &M.V[3 * v];
+        const double u[3] = {pv[0] - st.S[0], pv[1] - st.S[1], pv[2] - st.S[2]};
+        lane_propose(x, v, sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]), dx / l, dy / l);
+    }
+    for (int k = 0; k < 3 && !st.err; ++k) {
+        const int t = M.twin[3 * f0 + k];
+        if (t < 0) continue;
+        const double L = M.geom[9 * f0 + 3 * k];
+        const double skx = b0[(k + 1) % 3] * L + b0[(k + 2) % 3] * M.geom[9 * f0 + 3 * k + 1];
+        const double sky = b0[(k + 2) % 3] * M.geom[9 * f0 + 3 * k + 2];
+        Win w;
+        w.he = (t / 3) * 4 + t % 3;
+        w.sigma = 0;
+        w.sx = L - skx;
+        w.sy = fmin(-sky, -1e-15 * L);
+        w.b0 = 0;
+        w.b1 = L;
+        const double ddx = P2[(k + 1) % 3][0] - P2[k][0], ddy = P2[(k + 1) % 3][1] - P2[k][1];
+        const double dl = len2(ddx, ddy);
+        w.c = -ddx / dl;
+        w.s = -ddy / dl;
+        lane_push(x, w, -1);
+    }
+    return !st.err;
+}
+
+// The next item of the propagation in key order (-1: the source is done or failed).
+__device__ __forceinline__ int lane_next(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, Lane& st)
+{
+    const SysDesc& D = Lp.sys[Lp.sysOf ? Lp.sysOf[st.si] : 0];
+    LaneCtx x{D.mesh, C, S, st};
+    const int it = lane_pop(x);
+    if (it < 0) return -1;
+    if (++st.pops > st.popCap || st.processed > Lp.maxWindows) {
+        st.err = CSSG_ST_CAPACITY;
+        return -1;
+    }
+    return it;
+}
+
+// Distances, tangents, pair records and the force of the source (or its hand-off to the medium pass).
+__device__ void lane_finish(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, Lane& st, unsigned long long* cnt)
+{
+    const int si = st.si;
+    if (st.err == CSSG_ST_CAPACITY && Lp.failList) st.handedOff = true;
+    if (st.handedOff) {
+        Lp.status[si] = 0;
+        Lp.failList[atomicAdd(Lp.failCount, 1)] = si;
         return;
     }
+    const SysDesc& D = Lp.sys[Lp.sysOf ? Lp.sysOf[si] : 0];
+    const DevMesh& M = D.mesh;
+    LaneCtx x{M, C, S, st};
+    const int nT = st.nT;
     // ---- results ---------------------------------------------------------------------------------------------------
     const int err = st.err;
     double fx = 0, fy = 0, fz = 0;
@@ -774,7 +828,9 @@ __device__ void lane_solve(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, 
     cnt[3] += err ? 1 : 0;
 }
 
-// One warp takes `lanes` consecutive sources (one per lane) at a time from the work counter.
+// One warp takes `lanes` consecutive sources (one per lane) at a time from the work counter.  The propagation loop is
+// warp-synchronous: every lane takes one item per iteration (or idles once its source is done), so the lanes' window
+// steps execute as the same instructions instead of one lane after another.
 __global__ void __launch_bounds__(128) lane_kernel(GeoLaunch L, LaneCaps C, size_t warpBytes, int lanes)
 {
     const int lane = threadIdx.x & 31;
@@ -791,11 +847,45 @@ __global__ void __launch_bounds__(128) lane_kernel(GeoLaunch L, LaneCaps C, size
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= nItems) break;
         const int item = base + lane;
-        if (lane < lanes && item < nItems) {
-            Lane st;
-            st.si = L.order ? L.order[item] : item;
-            lane_solve(L, C, S, st, cnt);
+        const bool active = lane < lanes && item < nItems;
+        Lane st;
+        st.si = active ? (L.order ? L.order[item] : item) : 0;
+        bool live = active && lane_setup(L, C, S, st);
+        __syncwarp();
+        const DevMesh& M = L.sys[active && L.sysOf ? L.sysOf[st.si] : 0].mesh;
+        const LaneCtx x{M, C, S, st};
+        // One item per lane and iteration.  Every stage sits at the top level of the loop body and ends with a
+        // warp-wide reconvergence, so the lanes' window steps issue as shared instructions rather than one lane's
+        // path after another's.
+        while (__any_sync(0xffffffffu, live)) {
+            int it = -1;
+            if (live) {
+                it = lane_next(L, C, S, st);
+                if (it < 0) live = false;
+            }
+            __syncwarp();
+            const bool isWin = live && it < C.CW, isVtx = live && it >= C.CW;
+            Win w;
+            bool on = false;
+            if (isWin) on = lane_trim(x, it, w);
+            __syncwarp();
+            if (on) lane_targets(x, w);
+            __syncwarp();
+            for (int k = 0; k < 3; ++k) {
+                if (on) lane_proposal(x, w, k);
+                __syncwarp();
+            }
+            int reuse = on ? it : -1;
+            if (on) lane_child(x, w, false, &reuse);
+            __syncwarp();
+            if (on) lane_child(x, w, true, &reuse);
+            __syncwarp();
+            if (on && reuse >= 0) free_slot(x, reuse);
+            if (isVtx) lane_launch(x, it - C.CW);
+            __syncwarp();
+            if (live && st.err) live = false;
         }
+        if (active) lane_finish(L, C, S, st, cnt);
         __syncwarp();
     }
     for (int k = 0; k < 4; ++k) {

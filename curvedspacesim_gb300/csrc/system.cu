@@ -483,13 +483,13 @@ int set_lanes(cssg_system* s, int lanes)
     }
     if (lanes > 0 && !s->laneScratch) {
         if (int rc = ensure_candidate_rows(s)) return rc;
-        // per-lane tables from the regular pass's estimates: targets up to the candidate row, faces and vertices of
-        // the expected patch with the regular tables' margins, live windows up to twice the face table
+        // per-lane tables from the regular pass's estimates: targets up to the candidate row, face and vertex tables at
+        // half the regular tables' margins (a lane's tables hold one source), live windows up to twice the face table
         LaneCaps& c = s->laneCaps;
         c.CT = std::min(s->candCap, std::max(16, s->caps.CT));
-        c.CF = s->caps.CF;
-        c.CV = s->caps.CV;
-        c.CW = std::max(64, std::min(s->caps.CW, 2 * s->caps.CF));
+        c.CF = std::max(64, s->caps.CF / 2);
+        c.CV = std::max(64, s->caps.CV / 2);
+        c.CW = std::max(64, std::min(s->caps.CW, c.CF * 2));
         int sms = 0;
         CSSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->ctx->device));
         const long long batches = (s->n + 15) / 16;

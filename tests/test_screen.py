@@ -1,9 +1,13 @@
 """Learned screen on a bumpy sphere: trained on the exact GPU solver's pairs from other seeds, calibrated on held-out
 surfaces; the screened force pass must keep the exact path's in-range pair set and distances."""
+import os
+
 import numpy as np
 import pytest
 
 from curvedspacesim_gb300 import meshes as ms
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 pytestmark = pytest.mark.gpu
 
@@ -52,23 +56,28 @@ def test_screened_path_keeps_pairs_and_distances():
 
 
 def test_screen_gain_on_thin_torus():
-    """What the trained network gains over the exact path alone: on a thin-tubed torus many candidate pairs
-    (chord < sigma) lie across the tube with geodesics longer than sigma.  The screen skips them (no exact
-    propagation toward them), the early exit comes sooner, and the in-range pair set stays identical."""
+    """What the trained network gains over the method without it: on a thin-tubed torus (tube radius 0.3,
+    sigma 0.5) candidate pairs across the tube have chords below sigma and geodesics above it.  Such a pair holds the
+    exact path's early exit open until the propagation reaches the cutoff; the screen skips it, and the source stops
+    once its in-range targets are settled.  At 40 particles a source has few candidates, so this is most of the
+    propagation's reach: the measured bound (every out-of-range pair skipped, from the exact distances) and the
+    trained screen's saving are both real, and the in-range pair set stays identical."""
+    import sys
     from curvedspacesim_gb300 import api, screen
     ctx = api.Context(0)
-    n, sigma = 400, 0.5
+    sigma = 0.5
 
     def mesh(seed):
         return ms.noisy_torus(60, 30, 1.0, 0.3, std=0.01, smoothing_rings=2, seed=seed)
 
-    X, y, c, _ = screen.generate(ctx, mesh, [1, 2, 3], n, sigma, configs_per_seed=2)
+    X, y, c, _ = screen.generate(ctx, mesh, [1, 2, 3], 400, sigma, configs_per_seed=2)
     params, _ = screen.train(ctx, X, y, steps=800, batch=4096, lr=3e-3)
-    Xh, yh, ch, _ = screen.generate(ctx, mesh, [4, 5], n, sigma, configs_per_seed=2)
+    Xh, yh, ch, _ = screen.generate(ctx, mesh, [4, 5], 400, sigma, configs_per_seed=2)
     margin, info = screen.calibrate(ctx, params, Xh, yh, ch)
     frac, wrong = screen.skipped_fraction(ctx, params, margin, Xh, yh, ch)
     assert wrong == 0
     V, F = mesh(0)
+    n = 40
     rng = np.random.default_rng(9)
     f, b = ms.area_weighted_positions(V, F, n, rng)
     M = api.Mesh(V, F)
@@ -89,12 +98,17 @@ def test_screen_gain_on_thin_torus():
     missing, extra, err = screen.audit(runs["plain"][0].pairs(), runs["screened"][0].pairs(), sigma)
     assert not missing and not extra and err <= 1e-12
     w_plain, w_scr = runs["plain"][1]["windows"], runs["screened"][1]["windows"]
-    print(f"thin torus: holdout skip fraction {frac:.3f}, evaluation skipped {sc['screened']} of {sc['pairs']} "
-          f"candidate pairs, windows {w_plain} -> {w_scr}")
+    sys.path.insert(0, ROOT)
+    import bench
+    bound = bench.screen_bound(ctx, M, sigma, runs["plain"][0].get_state(), runs["plain"][0].pairs())
+    print(f"thin torus, N={n}: holdout skip fraction {frac:.3f}, evaluation skipped {sc['screened']} of "
+          f"{sc['pairs']} candidate pairs ({bound['out_of_range_candidate_pairs']} out of range), windows "
+          f"{w_plain} -> {w_scr}; every out-of-range pair skipped: {bound['windows_in_range_only']} "
+          f"(saving {bound['max_window_saving']:.3f})")
     assert sc["screened"] > 0
-    # the gain is the propagation the skipped targets no longer hold open: the early exit comes as soon as the kept
-    # targets are settled.  Window counts vary by a few tenths of a percent between runs (the order in which the
-    # threads of a source group take windows), far less than this gain.
+    assert bound["max_window_saving"] > 0.1  # the configuration has something to gain
+    # window counts vary by a few tenths of a percent between runs (the order in which the threads of a source group
+    # take windows); the screen's saving is several percent
     assert w_scr < 0.97 * w_plain, (w_plain, w_scr)
 
 
