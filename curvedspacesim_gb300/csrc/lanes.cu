@@ -828,9 +828,12 @@ __device__ void lane_finish(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S,
     cnt[3] += err ? 1 : 0;
 }
 
-// One warp takes `lanes` consecutive sources (one per lane) at a time from the work counter.  The propagation loop is
-// warp-synchronous: every lane takes one item per iteration (or idles once its source is done), so the lanes' window
-// steps execute as the same instructions instead of one lane after another.
+// A warp keeps up to `lanes` sources in flight, one per lane.  Lanes whose source is done wait until half of them
+// are idle (or none is live); then the idle lanes write their sources' results and take the next consecutive sources
+// from the work counter together, so set-up and results run on many lanes at once and no lane waits for the slowest
+// source of a fixed batch.  The propagation loop is warp-synchronous: every live lane takes one item per iteration,
+// and every stage sits at the top level of the loop body and ends with a warp-wide reconvergence, so the lanes' window
+// steps issue as shared instructions rather than one lane's path after another's.
 __global__ void __launch_bounds__(128) lane_kernel(GeoLaunch L, LaneCaps C, size_t warpBytes, int lanes)
 {
     const int lane = threadIdx.x & 31;
@@ -841,53 +844,68 @@ __global__ void __launch_bounds__(128) lane_kernel(GeoLaunch L, LaneCaps C, size
     unsigned long long cnt[4] = {0, 0, 0, 0};
     int nItems = L.nSrc;
     if (L.itemCountDev) nItems = min(nItems, *(volatile const int*)L.itemCountDev);
+    const int refillAt = max(1, lanes / 2);
+    Lane st;
+    st.si = 0;
+    bool live = false, pending = false, more = true;
     while (true) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(L.workCounter, lanes);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= nItems) break;
-        const int item = base + lane;
-        const bool active = lane < lanes && item < nItems;
-        Lane st;
-        st.si = active ? (L.order ? L.order[item] : item) : 0;
-        bool live = active && lane_setup(L, C, S, st);
-        __syncwarp();
-        const DevMesh& M = L.sys[active && L.sysOf ? L.sysOf[st.si] : 0].mesh;
-        const LaneCtx x{M, C, S, st};
-        // One item per lane and iteration.  Every stage sits at the top level of the loop body and ends with a
-        // warp-wide reconvergence, so the lanes' window steps issue as shared instructions rather than one lane's
-        // path after another's.
-        while (__any_sync(0xffffffffu, live)) {
-            int it = -1;
-            if (live) {
-                it = lane_next(L, C, S, st);
-                if (it < 0) live = false;
+        const bool idle = lane < lanes && !live;
+        const unsigned idleMask = __ballot_sync(0xffffffffu, idle);
+        const int nLive = __popc(__ballot_sync(0xffffffffu, live));
+        if (!more && nLive == 0) break;
+        if (more && (nLive == 0 || __popc(idleMask) >= refillAt)) {
+            if (idle && pending) {
+                lane_finish(L, C, S, st, cnt);
+                pending = false;
             }
             __syncwarp();
-            const bool isWin = live && it < C.CW, isVtx = live && it >= C.CW;
-            Win w;
-            bool on = false;
-            if (isWin) on = lane_trim(x, it, w);
-            __syncwarp();
-            if (on) lane_targets(x, w);
-            __syncwarp();
-            for (int k = 0; k < 3; ++k) {
-                if (on) lane_proposal(x, w, k);
-                __syncwarp();
+            const int want = __popc(idleMask);
+            int base = 0;
+            if (lane == 0) base = atomicAdd(L.workCounter, want);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base + want >= nItems) more = false;
+            if (idle) {
+                const int item = base + __popc(idleMask & ((1u << lane) - 1));
+                if (item < nItems) {
+                    st.si = L.order ? L.order[item] : item;
+                    live = lane_setup(L, C, S, st);
+                    pending = true;
+                }
             }
-            int reuse = on ? it : -1;
-            if (on) lane_child(x, w, false, &reuse);
             __syncwarp();
-            if (on) lane_child(x, w, true, &reuse);
-            __syncwarp();
-            if (on && reuse >= 0) free_slot(x, reuse);
-            if (isVtx) lane_launch(x, it - C.CW);
-            __syncwarp();
-            if (live && st.err) live = false;
+            continue;
         }
-        if (active) lane_finish(L, C, S, st, cnt);
+        const DevMesh& M = L.sys[L.sysOf ? L.sysOf[st.si] : 0].mesh;
+        const LaneCtx x{M, C, S, st};
+        int it = -1;
+        if (live) {
+            it = lane_next(L, C, S, st);
+            if (it < 0) live = false;
+        }
         __syncwarp();
+        const bool isWin = live && it < C.CW, isVtx = live && it >= C.CW;
+        Win w;
+        bool on = false;
+        if (isWin) on = lane_trim(x, it, w);
+        __syncwarp();
+        if (on) lane_targets(x, w);
+        __syncwarp();
+        for (int k = 0; k < 3; ++k) {
+            if (on) lane_proposal(x, w, k);
+            __syncwarp();
+        }
+        int reuse = on ? it : -1;
+        if (on) lane_child(x, w, false, &reuse);
+        __syncwarp();
+        if (on) lane_child(x, w, true, &reuse);
+        __syncwarp();
+        if (on && reuse >= 0) free_slot(x, reuse);
+        if (isVtx) lane_launch(x, it - C.CW);
+        __syncwarp();
+        if (live && st.err) live = false;
     }
+    if (pending) lane_finish(L, C, S, st, cnt);
+    __syncwarp();
     for (int k = 0; k < 4; ++k) {
         unsigned long long v = cnt[k];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
