@@ -10,14 +10,16 @@
 // ~64 cycles whether 1 or 32 lanes are active.  Small patches (tens of faces, a few dozen windows per source) give a
 // source group only a handful of windows at a time, so most FP64 instructions there run with a few lanes.  Here each
 // lane solves its own source serially, in the order of a bucket queue (Dial's algorithm on the windows' FP32 lower
-// bounds), and every FP64 instruction of the window step serves up to 32 sources at once.  A warp takes a batch of
-// consecutive sources (the longest-first order keeps their costs alike) and moves on when all of them are done.
+// bounds), and every FP64 instruction of the window step serves up to 32 sources at once.  Lanes take new sources in
+// bulk as old ones finish (lane_kernel).  Every data-dependent loop (hash probes, list walks, the bucket scan) has one
+// exit and re-converges the lanes that entered it, so a warp's lanes stay one instruction stream.
 //
 // Memory: each lane has its own tables in global memory (L2- and L1-resident at these sizes), interleaved by lane
 // (element k of lane l at [k * 32 + l]) so that the lanes' accesses to the same element coalesce:
 //   targets (96 B records), face table (patch membership + per-face target lists), vertex table (dense keys; labels,
 //   start directions, launch state and queue links in 40 B records), a window slab with a free list (64 B records),
-//   the bucket heads and a breadth-first queue for the patch.  Tables are cleared at the start of every source (coalesced stores).
+//   the bucket heads and a breadth-first queue for the patch.  Tables are cleared at the start of every source
+//   (coalesced stores).
 // A source whose tables or work cap overflow is handed to the medium-table source-group pass (failList), so
 // results never depend on the capacities chosen here.
 #include <algorithm>
@@ -55,7 +57,7 @@ struct VRec {         // a vertex of the lane's table (its key, the vertex index
     double dx, dy;    // start direction of that path
     double launched;  // label of its last pseudo-source launch (-1: never)
     int qnext;        // next item of its bucket list; kNotQueued: not queued
-    int pad;
+    int pad;          // can it become a pseudo-source: -1 not evaluated yet, 0 no, 1 yes
 };
 
 struct FRec {         // a face of the lane's table
@@ -103,6 +105,13 @@ __host__ __device__ inline size_t lane_carve(const LaneCaps& c, char* base, int 
 
 __device__ __forceinline__ unsigned lhash(int k) { return (unsigned)k * 2654435761u; }
 
+// Lanes that enter a data-dependent loop together (a hash probe, a list walk) leave it at different steps, and nothing
+// makes them converge again on their own: the code after the loop would then be issued once per exit step, and with
+// nested probes the warp ends up running its lanes one after another.  Functions with such loops therefore have one
+// exit and re-converge the lanes that entered them before returning.
+#define LANES_ENTER const unsigned lanesIn = __activemask()
+#define LANES_LEAVE __syncwarp(lanesIn)
+
 // Per-lane solver state (registers).
 struct Lane {
     int si;           // source index
@@ -134,79 +143,100 @@ struct LaneCtx {
 // ---- face table --------------------------------------------------------------------------------------------------
 __device__ int lf_find(const LaneCtx& x, int f)
 {
+    LANES_ENTER;
     const int CF = x.C.CF;
     unsigned h = lhash(f) & (CF - 1);
+    int found = -1;
     for (int p = 0; p < CF; ++p) {
         const int k = x.S.F[h].key;
-        if (k == f) return (int)h;
-        if (k == -1) return -1;
+        if (k == f) found = (int)h;
+        if (k == f || k == -1) break;
         h = (h + 1) & (CF - 1);
     }
-    return -1;
+    LANES_LEAVE;
+    return found;
 }
 
 // returns the entry of f (inserted if absent); *fresh = 1 when inserted here
 __device__ int lf_insert(const LaneCtx& x, int f, bool* fresh)
 {
+    LANES_ENTER;
     const int CF = x.C.CF;
     *fresh = false;
     unsigned h = lhash(f) & (CF - 1);
+    int found = -1;
     for (int p = 0; p < CF; ++p) {
         const int k = x.S.F[h].key;
-        if (k == f) return (int)h;
         if (k == -1) {
             x.S.F[h].key = f;
             x.S.F[h].val = 0;
             *fresh = true;
-            return (int)h;
+        }
+        if (k == f || k == -1) {
+            found = (int)h;
+            break;
         }
         h = (h + 1) & (CF - 1);
     }
-    x.st.err = CSSG_ST_CAPACITY;
-    return -1;
+    if (found < 0) x.st.err = CSSG_ST_CAPACITY;
+    LANES_LEAVE;
+    return found;
 }
 
 __device__ __forceinline__ bool lane_in_domain(const LaneCtx& x, int g)
 {
-    if (g < 0) return false;
-    if (x.st.full) return true;
-    const int h = lf_find(x, g);
-    return h >= 0 && (x.S.F[h].val & kInDomain);
+    LANES_ENTER;
+    bool in = g >= 0 && x.st.full;
+    if (g >= 0 && !x.st.full) {
+        const int h = lf_find(x, g);
+        in = h >= 0 && (x.S.F[h].val & kInDomain);
+    }
+    LANES_LEAVE;
+    return in;
 }
 
 // ---- vertex table ------------------------------------------------------------------------------------------------
 __device__ int lv_find(const LaneCtx& x, int v)
 {
+    LANES_ENTER;
     const int CV = x.C.CV;
     unsigned h = lhash(v) & (CV - 1);
+    int found = -1;
     for (int p = 0; p < CV; ++p) {
         const int k = x.S.vkey[h];
-        if (k == v) return (int)h;
-        if (k == -1) return -1;
+        if (k == v) found = (int)h;
+        if (k == v || k == -1) break;
         h = (h + 1) & (CV - 1);
     }
-    return -1;
+    LANES_LEAVE;
+    return found;
 }
 
 __device__ int lv_insert(const LaneCtx& x, int v)
 {
+    LANES_ENTER;
     const int CV = x.C.CV;
     unsigned h = lhash(v) & (CV - 1);
+    int found = -1;
     for (int p = 0; p < CV; ++p) {
         const int k = x.S.vkey[h];
-        if (k == v) return (int)h;
         if (k == -1) {
             x.S.vkey[h] = v;
             VRec& r = x.S.V[h];
             r.lab = CUDART_INF;
             r.launched = -1.0;
             r.qnext = kNotQueued;
-            return (int)h;
+            r.pad = -1;  // launchable: not evaluated yet
+        }
+        if (k == v || k == -1) {
+            found = (int)h;
+            break;
         }
         h = (h + 1) & (CV - 1);
     }
-    x.st.err = CSSG_ST_CAPACITY;
-    return -1;
+    if (found < 0) x.st.err = CSSG_ST_CAPACITY;
+    LANES_LEAVE;
+    return found;
 }
 
 __device__ __forceinline__ double lv_label(const LaneCtx& x, int v)
@@ -254,62 +284,83 @@ __device__ __forceinline__ void free_slot(const LaneCtx& x, int s) { x.S.wfree[x
 // beyond the cutoff.  reuse >= 0: the slot to write it to (the processed parent's).  Returns true if a slot was used.
 __device__ bool lane_push(const LaneCtx& x, Win& c, int reuse)
 {
+    LANES_ENTER;
     const DevMesh& M = x.M;
     const int g = c.he >> 2, j = c.he & 3;
-    if (g == x.st.f0 || !lane_in_domain(x, g)) return false;
-    const double L = M.geom[9 * g + 3 * j];
-    c.b0 = fmax(0.0, c.b0);
-    c.b1 = fmin(L, c.b1);
-    if (!(c.b1 - c.b0 > 1e-14 * L)) return false;
-    const float key = key_lo(c);
-    if ((double)key > x.st.cutoff) return false;
-    c.key = key;
-    const int s = reuse >= 0 ? reuse : alloc_slot(x);
-    if (s < 0) return false;
-    x.S.W[s] = c;
-    queue_window(x, s, key);
-    return true;
+    bool used = false;
+    if (g != x.st.f0 && lane_in_domain(x, g)) {
+        const double L = M.geom[9 * g + 3 * j];
+        c.b0 = fmax(0.0, c.b0);
+        c.b1 = fmin(L, c.b1);
+        const float key = key_lo(c);
+        if (c.b1 - c.b0 > 1e-14 * L && (double)key <= x.st.cutoff) {
+            c.key = key;
+            const int s = reuse >= 0 ? reuse : alloc_slot(x);
+            if (s >= 0) {
+                x.S.W[s] = c;
+                queue_window(x, s, key);
+                used = true;
+            }
+        }
+    }
+    LANES_LEAVE;
+    return used;
 }
 
-// can v become a pseudo-source: a saddle or border vertex of the mesh, or (patch) a vertex on the patch's border
-__device__ bool lane_launchable(const LaneCtx& x, int v)
+// can vertex v (entry h) become a pseudo-source: a saddle or border vertex of the mesh, or (patch) a vertex on the
+// patch's border; evaluated once per source and kept in the entry (the domain does not change during propagation)
+__device__ bool lane_launchable(const LaneCtx& x, int h, int v)
 {
+    LANES_ENTER;
     const DevMesh& M = x.M;
-    if (M.vflag[v] & (VF_BORDER | VF_SADDLE)) return true;
-    if (x.st.full) return false;
-    for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i)
-        if (!lane_in_domain(x, M.vfList[i])) return true;
-    return false;
+    VRec& r = x.S.V[h];
+    if (r.pad < 0) {
+        bool yes = (M.vflag[v] & (VF_BORDER | VF_SADDLE)) != 0;
+        if (!yes && !x.st.full)
+            for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i)
+                if (!lane_in_domain(x, M.vfList[i])) {
+                    yes = true;
+                    break;
+                }
+        r.pad = yes ? 1 : 0;
+    }
+    const bool yes = r.pad == 1;
+    LANES_LEAVE;
+    return yes;
 }
 
 // a path of length d with start direction (dx, dy) to vertex v
 __device__ void lane_propose(const LaneCtx& x, int v, double d, double dx, double dy)
 {
+    LANES_ENTER;
     const int h = lv_insert(x, v);
-    if (h < 0) return;
-    VRec& r = x.S.V[h];
-    if (!(d < r.lab)) return;
-    r.lab = d;
-    r.dx = dx;
-    r.dy = dy;
-    if (d <= x.st.cutoff && lane_launchable(x, v)) queue_vertex(x, h, d);
+    if (h >= 0 && d < x.S.V[h].lab) {
+        VRec& r = x.S.V[h];
+        r.lab = d;
+        r.dx = dx;
+        r.dy = dy;
+        if (d <= x.st.cutoff && lane_launchable(x, h, v)) queue_vertex(x, h, d);
+    }
+    LANES_LEAVE;
 }
 
 // a window's proposal for its face's vertex at (px, py) of its frame; the start direction only when it wins
 __device__ void lane_propose_from(const LaneCtx& x, const Win& w, int v, double px, double py)
 {
+    LANES_ENTER;
     const int h = lv_insert(x, v);
-    if (h < 0) return;
-    VRec& r = x.S.V[h];
     const double l = len2(px - w.sx, py - w.sy);
     const double d = w.sigma + l;
-    if (!(d < r.lab)) return;
-    r.lab = d;
-    double dx, dy;
-    start_dir_l(w, px, py, l, dx, dy);
-    r.dx = dx;
-    r.dy = dy;
-    if (d <= x.st.cutoff && lane_launchable(x, v)) queue_vertex(x, h, d);
+    if (h >= 0 && d < x.S.V[h].lab) {
+        VRec& r = x.S.V[h];
+        r.lab = d;
+        double dx, dy;
+        start_dir_l(w, px, py, l, dx, dy);
+        r.dx = dx;
+        r.dy = dy;
+        if (d <= x.st.cutoff && lane_launchable(x, h, v)) queue_vertex(x, h, d);
+    }
+    LANES_LEAVE;
 }
 
 // ---- one window, in stages (the kernel reconverges the warp between stages) ------------------------------------------
@@ -334,23 +385,24 @@ __device__ __forceinline__ WinGeo win_geo(const DevMesh& M, const Win& w)
 // Stage 1: load and trim the window in slot s; a dominated window frees its slot.  Returns true if it survives.
 __device__ bool lane_trim(const LaneCtx& x, int s, Win& w)
 {
+    LANES_ENTER;
     w = x.S.W[s];
-    if (!trim_window(x.M, w, [&](int v) { return lv_label(x, v); })) {
-        free_slot(x, s);
-        return false;
-    }
-    x.st.processed++;
-    return true;
+    const bool keep = trim_window(x.M, w, [&](int v) { return lv_label(x, v); });
+    if (keep) x.st.processed++;
+    else free_slot(x, s);
+    LANES_LEAVE;
+    return keep;
 }
 
 // Stage 2: targets on the window's face: the path through this window
 __device__ void lane_targets(const LaneCtx& x, const Win& w)
 {
+    LANES_ENTER;
     const DevMesh& M = x.M;
     const WinGeo q = win_geo(M, w);
     const int fh = lf_find(x, q.g);
-    if (fh < 0) return;
-    for (int t = (x.S.F[fh].val & (kInDomain - 1)) - 1; t >= 0; t = x.S.T[t].next) {
+    const int head = fh >= 0 ? (x.S.F[fh].val & (kInDomain - 1)) - 1 : -1;
+    for (int t = head; t >= 0; t = x.S.T[t].next) {
         TRec& tr = x.S.T[t];
         if (tr.idx < 0) continue;  // screened out: not queried
         const double b1 = tr.b[(q.j + 1) % 3], b2 = tr.b[(q.j + 2) % 3];
@@ -377,12 +429,14 @@ __device__ void lane_targets(const LaneCtx& x, const Win& w)
             }
         }
     }
+    LANES_LEAVE;
 }
 
 // Stage 3: vertex proposals: the opposite vertex C when the window's rays reach it, the edge's ends when it covers
 // them.  k selects one of the three (the kernel runs them as three sub-stages).
 __device__ void lane_proposal(const LaneCtx& x, const Win& w, int k)
 {
+    LANES_ENTER;
     const DevMesh& M = x.M;
     const WinGeo q = win_geo(M, w);
     if (k == 0) {
@@ -394,67 +448,76 @@ __device__ void lane_proposal(const LaneCtx& x, const Win& w, int k)
     } else {
         if (w.b1 >= q.L - q.tol) lane_propose_from(x, w, M.F[3 * q.g + (q.j + 1) % 3], q.L, 0.0);
     }
+    LANES_LEAVE;
 }
 
 // Stage 4: the child through exit edge C->A (exitBC = false) or B->C (true); *reuse is the processed window's slot
 // while it is free to hold a child (-1 once used).  After the last child the caller frees an unused slot.
 __device__ void lane_child(const LaneCtx& x, const Win& w, bool exitBC, int* reuse)
 {
+    LANES_ENTER;
     const DevMesh& M = x.M;
     const WinGeo q = win_geo(M, w);
     const CrossC xc(w, q.cx, q.cy);
     const double r0 = xc.rel(w.b0), r1 = xc.rel(w.b1);
     const bool want = exitBC ? (r1 > 0 && M.twin[3 * q.g + (q.j + 1) % 3] >= 0)
                              : (r0 < 0 && M.twin[3 * q.g + (q.j + 2) % 3] >= 0);
-    if (!want) return;
-    Win c;
-    make_child(M, w, exitBC, exitBC ? r0 <= 0 : r1 >= 0, c);
-    if (lane_push(x, c, *reuse)) *reuse = -1;
+    if (want) {
+        Win c;
+        make_child(M, w, exitBC, exitBC ? r0 <= 0 : r1 >= 0, c);
+        if (lane_push(x, c, *reuse)) *reuse = -1;
+    }
+    LANES_LEAVE;
 }
 
 // ---- one pseudo-source launch ----------------------------------------------------------------------------------------
 __device__ void lane_launch(const LaneCtx& x, int h)
 {
+    LANES_ENTER;
     const DevMesh& M = x.M;
     VRec& r = x.S.V[h];
     r.qnext = kNotQueued;
     const double d = r.lab;
-    if (d == r.launched) return;  // already launched with this label
-    r.launched = d;
-    x.st.launches++;
-    const int v = x.S.vkey[h];
-    const double tx = r.dx, ty = r.dy;
-    for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
-        const int f = M.vfList[i];
-        if (!lane_in_domain(x, f)) continue;
-        int k = 0;
-        while (M.F[3 * f + k] != v) ++k;
-        const int e = (k + 1) % 3;
-        // edge paths to the face's two other vertices, then the window on the opposite edge
-        lane_propose(x, M.F[3 * f + e], d + M.geom[9 * f + 3 * k], tx, ty);
-        lane_propose(x, M.F[3 * f + (k + 2) % 3], d + M.geom[9 * f + 3 * ((k + 2) % 3)], tx, ty);
-        const int t = M.twin[3 * f + e];
-        if (t < 0) continue;
-        Win c;
-        c.he = (t / 3) * 4 + t % 3;
-        c.sigma = d;
-        const double L = M.geom[9 * f + 3 * e];
-        c.sx = L - M.geom[9 * f + 3 * e + 1];
-        c.sy = -M.geom[9 * f + 3 * e + 2];
-        c.b0 = 0;
-        c.b1 = L;
-        c.c = tx;
-        c.s = ty;
-        lane_push(x, c, -1);
+    if (d != r.launched) {  // not yet launched with this label
+        r.launched = d;
+        x.st.launches++;
+        const int v = x.S.vkey[h];
+        const double tx = r.dx, ty = r.dy;
+        for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
+            const int f = M.vfList[i];
+            if (!lane_in_domain(x, f)) continue;
+            int k = 0;
+            while (M.F[3 * f + k] != v) ++k;
+            const int e = (k + 1) % 3;
+            // edge paths to the face's two other vertices, then the window on the opposite edge
+            lane_propose(x, M.F[3 * f + e], d + M.geom[9 * f + 3 * k], tx, ty);
+            lane_propose(x, M.F[3 * f + (k + 2) % 3], d + M.geom[9 * f + 3 * ((k + 2) % 3)], tx, ty);
+            const int t = M.twin[3 * f + e];
+            if (t < 0) continue;
+            Win c;
+            c.he = (t / 3) * 4 + t % 3;
+            c.sigma = d;
+            const double L = M.geom[9 * f + 3 * e];
+            c.sx = L - M.geom[9 * f + 3 * e + 1];
+            c.sy = -M.geom[9 * f + 3 * e + 2];
+            c.b0 = 0;
+            c.b1 = L;
+            c.c = tx;
+            c.s = ty;
+            lane_push(x, c, -1);
+        }
     }
+    LANES_LEAVE;
 }
 
 // Early exit: every queried target's best known path (through a window or a labelled vertex of its face) is no
 // longer than `bound`, a lower bound of every queued item's distances.  The vertex paths are FP32 upper bounds.
 __device__ bool lane_settled(const LaneCtx& x, double bound)
 {
+    LANES_ENTER;
     const DevMesh& M = x.M;
-    for (int t = 0; t < x.st.nT; ++t) {
+    bool done = true;
+    for (int t = 0; t < x.st.nT && done; ++t) {
         const TRec& tr = x.S.T[t];
         if (tr.face == x.st.f0 || tr.idx < 0) continue;  // on the source face, or screened out
         double b = tr.best;
@@ -467,34 +530,36 @@ __device__ bool lane_settled(const LaneCtx& x, double bound)
             const float l = sqrtf(ux * ux + uy * uy + uz * uz) * 1.000001f + 1e-30f;
             b = fmin(b, lab + (double)l);
         }
-        if (!(b <= bound)) return false;
+        if (!(b <= bound)) done = false;
     }
-    return true;
+    LANES_LEAVE;
+    return done;
 }
 
 // next item in key order, or -1 when the source is done
 __device__ int lane_pop(const LaneCtx& x)
 {
+    LANES_ENTER;
     Lane& st = x.st;
+    int item = -1;
     while (st.cur < kBuckets) {
         const int h = x.S.bucket[st.cur];
         if (h >= 0) {
             x.S.bucket[st.cur] = h < x.C.CW ? x.S.wnext[h] : x.S.V[h - x.C.CW].qnext;
-            return h;
+            item = h;
+            break;
         }
         ++st.cur;
-        if (st.cur < kBuckets) {
-            // every queued key is >= cur * bw up to the float rounding of the bucket index
-            const double bound = (double)st.cur * (double)st.bw * (1.0 - 1e-5);
-            if (lane_settled(x, bound)) return -1;
-        }
+        // every queued key is >= cur * bw up to the float rounding of the bucket index
+        if (st.cur < kBuckets && lane_settled(x, (double)st.cur * (double)st.bw * (1.0 - 1e-5))) st.cur = kBuckets;
     }
-    return -1;
+    LANES_LEAVE;
+    return item;
 }
 
 // ---- the per-source solve: set-up, propagation steps, results ----------------------------------------------------
 // Targets, patch, source frame and the initial windows.  Returns true when the source has propagation to do.
-__device__ bool lane_setup(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, Lane& st)
+__device__ bool lane_setup_body(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, Lane& st)
 {
     const int si = st.si;
     const SysDesc& D = Lp.sys[Lp.sysOf ? Lp.sysOf[si] : 0];
@@ -696,6 +761,14 @@ __device__ bool lane_setup(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, 
     return !st.err;
 }
 
+__device__ bool lane_setup(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, Lane& st)
+{
+    LANES_ENTER;
+    const bool live = lane_setup_body(Lp, C, S, st);
+    LANES_LEAVE;
+    return live;
+}
+
 // The next item of the propagation in key order (-1: the source is done or failed).
 __device__ __forceinline__ int lane_next(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, Lane& st)
 {
@@ -711,7 +784,8 @@ __device__ __forceinline__ int lane_next(const GeoLaunch& Lp, const LaneCaps& C,
 }
 
 // Distances, tangents, pair records and the force of the source (or its hand-off to the medium pass).
-__device__ void lane_finish(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, Lane& st, unsigned long long* cnt)
+__device__ void lane_finish_body(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, Lane& st,
+                                 unsigned long long* cnt)
 {
     const int si = st.si;
     if (st.err == CSSG_ST_CAPACITY && Lp.failList) st.handedOff = true;
@@ -826,6 +900,13 @@ __device__ void lane_finish(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S,
     cnt[1] += st.launches;
     cnt[2] += inRange;
     cnt[3] += err ? 1 : 0;
+}
+
+__device__ void lane_finish(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot& S, Lane& st, unsigned long long* cnt)
+{
+    LANES_ENTER;
+    lane_finish_body(Lp, C, S, st, cnt);
+    LANES_LEAVE;
 }
 
 // A warp keeps up to `lanes` sources in flight, one per lane.  Lanes whose source is done wait until half of them
