@@ -35,8 +35,8 @@ sys.path.insert(0, ROOT)
 
 from curvedspacesim_gb300 import meshes as ms  # noqa: E402
 
-# algorithmic work constants of the geodesic+force kernel (roofline accounting of the propagation)
-FLOPS_PER_WINDOW = 250          # FP64 flops of one window step (trim, target/vertex updates, two children)
+# algorithmic work constants of the geodesic+force kernel (roofline accounting of the propagation); the FP64 flops of
+# one processed window come from the library (api.flops_per_window(), counted once in its window geometry code)
 BYTES_PER_SOURCE = 4 + 24 + 24 + 24   # read face, barycentrics, R3 position; write force
 BYTES_PER_CANDIDATE = 4 + 4 + 24 + 24  # read index, face, barycentrics, R3 position
 BYTES_PER_FACE = 12 + 12 + 72         # patch face: vertex ids, neighbours, edge frames
@@ -409,7 +409,7 @@ def run_ours(args, cfg):
     faces = sum(sy["n"] * min(len(sy["F"]), 1.3 * math.pi * (sy["sigma"] + 0.0) ** 2 /
                               (ms.total_area(sy["V"], sy["F"]) / len(sy["F"]))) for sy in systems)
     geo_bytes = n * BYTES_PER_SOURCE + cands * BYTES_PER_CANDIDATE + faces * BYTES_PER_FACE
-    geo_flops = windows * FLOPS_PER_WINDOW
+    geo_flops = windows * api.flops_per_window()
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -667,7 +667,7 @@ def run_screen(args, cfg):
 
     # FP64 roofline of the geodesic kernel (the propagation's bound) on the screened path
     fp64_peak = api.fp64_peak_gflops(ctx)
-    geo_flops = win["screened"] * FLOPS_PER_WINDOW
+    geo_flops = win["screened"] * api.flops_per_window()
     achieved = geo_flops / (kt["screened"] * 1e-3) / 1e9
     traffic = TRAFFIC_BYTES.get(cfg["workload"])
 
@@ -713,7 +713,7 @@ def run_screen(args, cfg):
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "GFLOP/s",
                          "frac": achieved / fp64_peak, "traffic": int(traffic) if traffic else None,
                          "kernel": "geodesic (screened path)", "kernel_ms": kt["screened"],
-                         "flops_per_launch": geo_flops, "flops_per_window": FLOPS_PER_WINDOW,
+                         "flops_per_launch": geo_flops, "flops_per_window": api.flops_per_window(),
                          "windows_per_launch": win["screened"],
                          "peak_source": "measured FP64 FMA chain on this GPU (cssg_diag_fp64_peak); "
                                         "MEASURED_PEAKS.json has no FP64 entry"},

@@ -28,7 +28,7 @@ EXPORTS = [
     "cssg_system_set_tuning", "cssg_system_autotune", "cssg_system_fire", "cssg_system_stress",
     "cssg_mesh_set_boundary", "cssg_diag_reciprocal", "cssg_system_step_host",
     "cssg_system_gradient_descent", "cssg_system_set_screen_audit", "cssg_system_screen_audit_status",
-    "cssg_system_set_work_caps", "cssg_system_set_lanes", "cssg_system_lanes",
+    "cssg_system_set_work_caps", "cssg_system_set_lanes", "cssg_system_lanes", "cssg_diag_flops_per_window",
 ]
 
 
@@ -124,6 +124,7 @@ def load(build_if_missing: bool = True):
     L.cssg_system_kernels_per_step.argtypes = [P, P]
     L.cssg_diag_fp64_peak.argtypes = [P, P]
     L.cssg_diag_reciprocal.argtypes = [P, I, P, P]
+    L.cssg_diag_flops_per_window.argtypes = []
     L.cssg_mlp_param_count.argtypes = []
     L.cssg_system_set_screen.argtypes = [P, P, D, I]
     L.cssg_system_screen_counters.argtypes = [P, P]

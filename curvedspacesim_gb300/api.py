@@ -198,6 +198,11 @@ def _distance_batch(ctx, mesh, src_face, src_bary, cand_off, cand_face, cand_bar
     return d.cpu().numpy()[:m], ts.cpu().numpy()[:m], te.cpu().numpy()[:m], st.cpu().numpy()[:ns]
 
 
+def flops_per_window() -> int:
+    """FP64 flops of one processed window of the propagation (the library's own count, window.cuh)."""
+    return int(_lib.load().cssg_diag_flops_per_window())
+
+
 def fp64_peak_gflops(ctx: Context) -> float:
     out = ctypes.c_double()
     check(_lib.load().cssg_diag_fp64_peak(ctx.h, ctypes.byref(out)), "cssg_diag_fp64_peak")

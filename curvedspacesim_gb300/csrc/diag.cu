@@ -1,6 +1,7 @@
 // Device diagnostics: the measured FP64 FMA issue rate used as the denominator of the geodesic kernel's FP64
 // roofline (the measured peaks cover HBM copy bandwidth and BF16 tensor throughput only).
 #include "cssg_internal.cuh"
+#include "window.cuh"
 
 namespace {
 
@@ -74,3 +75,5 @@ extern "C" int cssg_diag_reciprocal(cssg_ctx* ctx, int n, const double* x, doubl
     CSSG_CUDA(cudaGetLastError());
     return CSSG_OK;
 }
+
+extern "C" int cssg_diag_flops_per_window(void) { return kFlopsPerWindow; }

@@ -111,6 +111,10 @@ __device__ __forceinline__ unsigned lhash(int k) { return (unsigned)k * 26544357
 // exit and re-converge the lanes that entered them before returning.
 #define LANES_ENTER const unsigned lanesIn = __activemask()
 #define LANES_LEAVE __syncwarp(lanesIn)
+// The same for one iteration of a loop whose body branches: the lanes that start an iteration together finish it
+// together (loop bodies have no `continue`, so every lane that starts an iteration reaches its end).
+#define ITER_BEGIN const unsigned iterLanes = __activemask()
+#define ITER_END __syncwarp(iterLanes)
 
 // Per-lane solver state (registers).
 struct Lane {
@@ -386,8 +390,15 @@ __device__ __forceinline__ WinGeo win_geo(const DevMesh& M, const Win& w)
 __device__ bool lane_trim(const LaneCtx& x, int s, Win& w)
 {
     LANES_ENTER;
+    const DevMesh& M = x.M;
     w = x.S.W[s];
-    const bool keep = trim_window(x.M, w, [&](int v) { return lv_label(x, v); });
+    // the three labels first (each probe re-converges), then the trim arithmetic on all lanes together
+    const int g = w.he >> 2, j = w.he & 3;
+    const int A = M.F[3 * g + j], B = M.F[3 * g + (j + 1) % 3];
+    const double dA = lv_label(x, A), dB = lv_label(x, B), dC = lv_label(x, M.F[3 * g + (j + 2) % 3]);
+    __syncwarp(lanesIn);
+    const bool keep = trim_window(M, w, [&](int v) { return v == A ? dA : (v == B ? dB : dC); });
+    __syncwarp(lanesIn);
     if (keep) x.st.processed++;
     else free_slot(x, s);
     LANES_LEAVE;
@@ -403,31 +414,33 @@ __device__ void lane_targets(const LaneCtx& x, const Win& w)
     const int fh = lf_find(x, q.g);
     const int head = fh >= 0 ? (x.S.F[fh].val & (kInDomain - 1)) - 1 : -1;
     for (int t = head; t >= 0; t = x.S.T[t].next) {
+        ITER_BEGIN;
         TRec& tr = x.S.T[t];
-        if (tr.idx < 0) continue;  // screened out: not queried
         const double b1 = tr.b[(q.j + 1) % 3], b2 = tr.b[(q.j + 2) % 3];
         const double px = b1 * q.L + b2 * q.cx, py = b2 * q.cy;
-        if (!ray_hits(w, px, py, q.tol)) continue;
         const double l = len2(px - w.sx, py - w.sy);
         const double d = w.sigma + l;
-        if (!(d < tr.best)) continue;
-        tr.best = d;
-        double dx, dy;
-        start_dir_l(w, px, py, l, dx, dy);
-        tr.dx = dx;
-        tr.dy = dy;
-        if (x.st.wantTe) {
-            // direction of arrival in R3: the ray in g's edge frame
-            const double* PA = &M.V[3 * M.F[3 * q.g + q.j]];
-            const double* PB = &M.V[3 * M.F[3 * q.g + (q.j + 1) % 3]];
-            const double* PC = &M.V[3 * M.F[3 * q.g + (q.j + 2) % 3]];
-            const double ux = px - w.sx, uy = py - w.sy;
-            for (int c = 0; c < 3; ++c) {
-                const double ex = (PB[c] - PA[c]) / q.L;
-                const double ey = (PC[c] - PA[c] - q.cx * ex) / q.cy;
-                x.S.te[3 * t + c] = (ux * ex + uy * ey) / l;
+        // screened-out targets (idx < 0) are not queried
+        if (tr.idx >= 0 && ray_hits(w, px, py, q.tol) && d < tr.best) {
+            tr.best = d;
+            double dx, dy;
+            start_dir_l(w, px, py, l, dx, dy);
+            tr.dx = dx;
+            tr.dy = dy;
+            if (x.st.wantTe) {
+                // direction of arrival in R3: the ray in g's edge frame
+                const double* PA = &M.V[3 * M.F[3 * q.g + q.j]];
+                const double* PB = &M.V[3 * M.F[3 * q.g + (q.j + 1) % 3]];
+                const double* PC = &M.V[3 * M.F[3 * q.g + (q.j + 2) % 3]];
+                const double ux = px - w.sx, uy = py - w.sy;
+                for (int c = 0; c < 3; ++c) {
+                    const double ex = (PB[c] - PA[c]) / q.L;
+                    const double ey = (PC[c] - PA[c] - q.cx * ex) / q.cy;
+                    x.S.te[3 * t + c] = (ux * ex + uy * ey) / l;
+                }
             }
         }
+        ITER_END;
     }
     LANES_LEAVE;
 }
@@ -463,8 +476,10 @@ __device__ void lane_child(const LaneCtx& x, const Win& w, bool exitBC, int* reu
     const bool want = exitBC ? (r1 > 0 && M.twin[3 * q.g + (q.j + 1) % 3] >= 0)
                              : (r0 < 0 && M.twin[3 * q.g + (q.j + 2) % 3] >= 0);
     if (want) {
+        const unsigned lanesWant = __activemask();
         Win c;
         make_child(M, w, exitBC, exitBC ? r0 <= 0 : r1 >= 0, c);
+        __syncwarp(lanesWant);
         if (lane_push(x, c, *reuse)) *reuse = -1;
     }
     LANES_LEAVE;
@@ -484,27 +499,31 @@ __device__ void lane_launch(const LaneCtx& x, int h)
         const int v = x.S.vkey[h];
         const double tx = r.dx, ty = r.dy;
         for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i) {
+            ITER_BEGIN;
             const int f = M.vfList[i];
-            if (!lane_in_domain(x, f)) continue;
-            int k = 0;
-            while (M.F[3 * f + k] != v) ++k;
-            const int e = (k + 1) % 3;
-            // edge paths to the face's two other vertices, then the window on the opposite edge
-            lane_propose(x, M.F[3 * f + e], d + M.geom[9 * f + 3 * k], tx, ty);
-            lane_propose(x, M.F[3 * f + (k + 2) % 3], d + M.geom[9 * f + 3 * ((k + 2) % 3)], tx, ty);
-            const int t = M.twin[3 * f + e];
-            if (t < 0) continue;
-            Win c;
-            c.he = (t / 3) * 4 + t % 3;
-            c.sigma = d;
-            const double L = M.geom[9 * f + 3 * e];
-            c.sx = L - M.geom[9 * f + 3 * e + 1];
-            c.sy = -M.geom[9 * f + 3 * e + 2];
-            c.b0 = 0;
-            c.b1 = L;
-            c.c = tx;
-            c.s = ty;
-            lane_push(x, c, -1);
+            if (lane_in_domain(x, f)) {
+                int k = 0;
+                while (M.F[3 * f + k] != v) ++k;
+                const int e = (k + 1) % 3;
+                // edge paths to the face's two other vertices, then the window on the opposite edge
+                lane_propose(x, M.F[3 * f + e], d + M.geom[9 * f + 3 * k], tx, ty);
+                lane_propose(x, M.F[3 * f + (k + 2) % 3], d + M.geom[9 * f + 3 * ((k + 2) % 3)], tx, ty);
+                const int t = M.twin[3 * f + e];
+                if (t >= 0) {
+                    Win c;
+                    c.he = (t / 3) * 4 + t % 3;
+                    c.sigma = d;
+                    const double L = M.geom[9 * f + 3 * e];
+                    c.sx = L - M.geom[9 * f + 3 * e + 1];
+                    c.sy = -M.geom[9 * f + 3 * e + 2];
+                    c.b0 = 0;
+                    c.b1 = L;
+                    c.c = tx;
+                    c.s = ty;
+                    lane_push(x, c, -1);
+                }
+            }
+            ITER_END;
         }
     }
     LANES_LEAVE;
@@ -518,19 +537,21 @@ __device__ bool lane_settled(const LaneCtx& x, double bound)
     const DevMesh& M = x.M;
     bool done = true;
     for (int t = 0; t < x.st.nT && done; ++t) {
+        ITER_BEGIN;
         const TRec& tr = x.S.T[t];
-        if (tr.face == x.st.f0 || tr.idx < 0) continue;  // on the source face, or screened out
-        double b = tr.best;
-        for (int c = 0; c < 3; ++c) {
-            const int v = M.F[3 * tr.face + c];
-            const double lab = lv_label(x, v);
-            if (!(lab < CUDART_INF)) continue;
-            const double* pv = &M.V[3 * v];
-            const float ux = (float)(tr.P[0] - pv[0]), uy = (float)(tr.P[1] - pv[1]), uz = (float)(tr.P[2] - pv[2]);
-            const float l = sqrtf(ux * ux + uy * uy + uz * uz) * 1.000001f + 1e-30f;
-            b = fmin(b, lab + (double)l);
+        if (tr.face != x.st.f0 && tr.idx >= 0) {  // targets on the source face and screened-out ones do not count
+            double b = tr.best;
+            for (int c = 0; c < 3; ++c) {
+                const int v = M.F[3 * tr.face + c];
+                const double lab = lv_label(x, v);
+                const double* pv = &M.V[3 * v];
+                const float ux = (float)(tr.P[0] - pv[0]), uy = (float)(tr.P[1] - pv[1]), uz = (float)(tr.P[2] - pv[2]);
+                const float l = sqrtf(ux * ux + uy * uy + uz * uz) * 1.000001f + 1e-30f;
+                if (lab < CUDART_INF) b = fmin(b, lab + (double)l);
+            }
+            if (!(b <= bound)) done = false;
         }
-        if (!(b <= bound)) done = false;
+        ITER_END;
     }
     LANES_LEAVE;
     return done;
@@ -679,25 +700,31 @@ __device__ bool lane_setup_body(const GeoLaunch& Lp, const LaneCaps& C, LaneSlot
             if (notInSeeds) {
                 const double r2 = rmax * rmax;
                 for (int q = 0; q < nq && !st.err; ++q) {
+                    ITER_BEGIN;
                     const int f = S.bfs[q];
-                    for (int k = 0; k < 3; ++k) {
+                    for (int k = 0; k < 3 && !st.err; ++k) {
                         const int tw = M.twin[3 * f + k];
-                        if (tw < 0) continue;
-                        const int g = tw / 3;
-                        if (lf_find(x, g) >= 0) continue;
-                        bool near = false;
-                        for (int c = 0; c < 3; ++c) {
-                            const double* pv = &M.V[3 * M.F[3 * g + c]];
-                            const double dx = st.S[0] - pv[0], dy = st.S[1] - pv[1], dz = st.S[2] - pv[2];
-                            if (!(dx * dx + dy * dy + dz * dz > r2)) near = true;
+                        const int g = tw < 0 ? -1 : tw / 3;
+                        bool add = g >= 0 && lf_find(x, g) < 0;
+                        if (add) {
+                            bool near = false;
+                            for (int c = 0; c < 3; ++c) {
+                                const double* pv = &M.V[3 * M.F[3 * g + c]];
+                                const double dx = st.S[0] - pv[0], dy = st.S[1] - pv[1], dz = st.S[2] - pv[2];
+                                if (!(dx * dx + dy * dy + dz * dz > r2)) near = true;
+                            }
+                            add = near;
                         }
-                        if (!near) continue;
-                        const int h = lf_insert(x, g, &fresh);
-                        if (h < 0) break;
-                        S.F[h].val |= kInDomain;
-                        if (nq < C.CF) S.bfs[nq++] = g;
-                        else st.err = CSSG_ST_CAPACITY;
+                        if (add) {
+                            const int h = lf_insert(x, g, &fresh);
+                            if (h >= 0) {
+                                S.F[h].val |= kInDomain;
+                                if (nq < C.CF) S.bfs[nq++] = g;
+                                else st.err = CSSG_ST_CAPACITY;
+                            }
+                        }
                     }
+                    ITER_END;
                 }
             }
         }
@@ -820,8 +847,7 @@ __device__ void lane_finish_body(const GeoLaunch& Lp, const LaneCaps& C, LaneSlo
                 for (int c = 0; c < 3; ++c) {
                     const int v = M.F[3 * tr.face + c];
                     const int h = lv_find(x, v);
-                    if (h < 0) continue;
-                    const double lab = S.V[h].lab;
+                    const double lab = h < 0 ? CUDART_INF : S.V[h].lab;
                     if (!(lab < CUDART_INF)) continue;
                     const double* pv = &M.V[3 * v];
                     const double u[3] = {tr.P[0] - pv[0], tr.P[1] - pv[1], tr.P[2] - pv[2]};

@@ -23,6 +23,15 @@ namespace {
 constexpr unsigned long long INF_BITS = 0x7FF0000000000000ull;
 constexpr unsigned FULL = 0xffffffffu;
 
+// FP64 arithmetic of one processed window on its usual path, counted from the functions below (add, subtract and
+// multiply 1 flop, fused multiply-add 2, square root 1; rcp_nr = its four fused multiply-adds, 8; comparisons, min/max
+// and FP32 work not counted): trim_window 7 (label differences, the trimmed ends, the emptiness test); the opposite
+// vertex's proposal 36 (CrossC 5, two interval tests 6, path length 7, start direction through rcp_nr 18); two
+// children 98 (per child CrossC 9 with its two tests, make_child 37-39, the interval clamp of the push 2).  A
+// window that also proposes an end vertex of its edge adds 7-25 per end.  The propagation roofline counts
+// windows processed (the kernels' counters) times this figure; cssg_diag_flops_per_window exports it.
+constexpr int kFlopsPerWindow = 141;
+
 struct __align__(16) Win {
     double b0, b1, sx, sy, sigma, c, s;
     int he;     // entered face * 4 + local edge

@@ -278,6 +278,10 @@ int cssg_system_kernels_per_step(cssg_system* sys, int* count);
  * from a register-resident dependent-chain kernel timed with CUDA events on the context stream; the denominator of
  * the FP64 roofline of the geodesic kernel.  Synchronises. */
 int cssg_diag_fp64_peak(cssg_ctx* ctx, double* gflops_host);
+/* FP64 flops of one processed window of the exact propagation on its usual path (trim, the opposite vertex's
+ * proposal, two children), counted from the code once (window.cuh); the propagation's FP64 roofline is windows
+ * processed x this figure. */
+int cssg_diag_flops_per_window(void);
 /* The reciprocal the propagation uses for geometric denominators (Newton-Raphson from a float seed), on n device
  * doubles: out[i] = 1/x[i] within a few ulps.  For accuracy tests. */
 int cssg_diag_reciprocal(cssg_ctx* ctx, int n, const double* x, double* out);
