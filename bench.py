@@ -341,13 +341,10 @@ def run_ours(args, cfg):
         raise RuntimeError(f"per-item errors during warm-up: {bits:#x} {cnt}")
     tune = None
     if args.tuning:
-        fields = args.tuning.split(",")
-        d, w, m, cap, lpt = fields[:5]
-        g = int(fields[5]) if len(fields) > 5 else 1
-        wide = bool(int(fields[6])) if len(fields) > 6 else False
-        S.set_tuning(float(d), int(w), int(m), int(cap), bool(int(lpt)), g, wide)
-        tune = {"delta_scale": float(d), "warps_per_block": int(w), "mid_slots": int(m), "warps_per_sm": int(cap),
-                "lpt_order": bool(int(lpt)), "warps_per_source": g, "wide_registers": wide, "source": "--tuning"}
+        _apply_tuning(S, args.tuning)
+        d, w, m, cap, lpt, g, wide = _parse_tuning(args.tuning)
+        tune = {"delta_scale": d, "warps_per_block": w, "mid_slots": m, "warps_per_sm": cap, "lpt_order": lpt,
+                "warps_per_source": g, "wide_registers": wide, "lanes_per_warp": S.lanes(), "source": "--tuning"}
         S.step(1, graph=not args.profile)
         torch.cuda.synchronize()
     elif not args.no_autotune:
@@ -452,14 +449,17 @@ def run_ours(args, cfg):
             "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": io_bytes,
                     "d2h_bytes_per_step": io_bytes},
             "gpu_launches": kps * args.steps,
-            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved_gbs / hbm_peak, "traffic": int(traffic) if traffic else None,
-                         "kernel": "geodesic_kernel", "kernel_ms": geo_ms,
-                         "algorithmic_bytes_per_launch": geo_bytes,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "of fallback 6.8 TB/s",
-                         "fp64": {"achieved_gflops": achieved_fp64, "peak_gflops": fp64_peak,
-                                  "frac": achieved_fp64 / fp64_peak, "flops_per_launch": geo_flops,
-                                  "windows_per_launch": windows, "peak_source": "measured FMA-chain kernel"}},
+            "roofline": {"bound": "fp64", "achieved": achieved_fp64, "peak": fp64_peak, "unit": "GFLOP/s",
+                         "frac": achieved_fp64 / fp64_peak, "traffic": int(traffic) if traffic else None,
+                         "kernel": "geodesic pass", "kernel_ms": geo_ms, "flops_per_launch": geo_flops,
+                         "flops_per_window": api.flops_per_window(), "windows_per_launch": windows,
+                         "lanes_per_warp": tune.get("lanes_per_warp") if tune else None,
+                         "peak_source": "measured FP64 FMA chain on this GPU (cssg_diag_fp64_peak); "
+                                        "MEASURED_PEAKS.json has no FP64 entry",
+                         "hbm": {"achieved_gbs": achieved_gbs, "peak_gbs": hbm_peak, "frac": achieved_gbs / hbm_peak,
+                                 "algorithmic_bytes_per_launch": geo_bytes,
+                                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks
+                                 else "of fallback 6.8 TB/s"}},
             "kernels_ms_per_step": {"geodesic": geo_ms, "walk": walk_ms},
             "counters_per_step": {k: v / args.steps for k, v in cnt2.items()},
             "clocks": clocks,
@@ -567,7 +567,7 @@ def run_screen(args, cfg):
         S.set_screen(screen.init_params(0), 1e6)
         S.set_state(f, b, vel, np.zeros((n, 3)))
         if args.tuning:
-            S.set_tuning(*_parse_tuning(args.tuning))
+            _apply_tuning(S, args.tuning)
         S.step(max(args.warmup, 1), graph=False)
         torch.cuda.synchronize()
         bits, cnt = S.check()
@@ -603,7 +603,7 @@ def run_screen(args, cfg):
     for name, S in (("plain", plain), ("screened", scr)):
         S.step(max(args.warmup, 1), graph=True)
         if args.tuning:
-            S.set_tuning(*_parse_tuning(args.tuning))
+            _apply_tuning(S, args.tuning)
             tunes[name] = {"source": "--tuning", "value": args.tuning}
         elif not args.no_autotune:
             tunes[name] = S.autotune(reps=3)
@@ -724,11 +724,19 @@ def run_screen(args, cfg):
 
 
 def _parse_tuning(text):
+    """delta_scale,warps_per_block,mid_slots,warps_per_sm,lpt[,warps_per_source[,wide_registers[,lanes]]]: the first
+    seven are System.set_tuning's arguments, the eighth System.set_lanes' (0: source groups)."""
     fields = text.split(",")
     d, w, m, cap, lpt = fields[:5]
     g = int(fields[5]) if len(fields) > 5 else 1
     wide = bool(int(fields[6])) if len(fields) > 6 else False
     return float(d), int(w), int(m), int(cap), bool(int(lpt)), g, wide
+
+
+def _apply_tuning(S, text):
+    S.set_tuning(*_parse_tuning(text))
+    fields = text.split(",")
+    S.set_lanes(int(fields[7]) if len(fields) > 7 else 0)
 
 
 def run_mlp(args, cfg):
@@ -854,7 +862,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (band width 1, 8 warps)")
     ap.add_argument("--tuning", default="",
                     help="explicit tuning instead of the autotuner: delta_scale,warps_per_block,mid_slots,"
-                         "warps_per_sm,lpt[,warps_per_source[,wide_registers]] (e.g. 4,8,0,0,1,2,0)")
+                         "warps_per_sm,lpt[,warps_per_source[,wide_registers[,lanes_per_warp]]] (e.g. 4,8,0,0,1,2,0 "
+                         "or 2,8,0,0,0,1,1,32)")
     ap.add_argument("--profile", action="store_true",
                     help="minimal run for ncu: warm-up steps, then one step without graph replay, no other legs")
     args = ap.parse_args()
