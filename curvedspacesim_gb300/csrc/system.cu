@@ -500,6 +500,36 @@ int set_lanes(cssg_system* s, int lanes)
     return CSSG_OK;
 }
 
+// Longest-first within spatial segments (the one-source-per-lane pass): the cell order is cut into segments of 256
+// sources and each segment is sorted by the last evaluation's cost, largest first (bitonic sort in shared memory).
+// Consecutive sources, which a warp takes together, then cost about the same and still lie close on the mesh.
+__global__ void __launch_bounds__(256) lpt_segmented(int n, const int* __restrict__ order, const int* __restrict__ cost,
+                                                     int* __restrict__ out)
+{
+    __shared__ int kc[256], kv[256];
+    const int i = threadIdx.x, g = blockIdx.x * 256 + i;
+    const int si = g < n ? (order ? order[g] : g) : -1;
+    kc[i] = g < n ? cost[si] : -1;  // padding sorts last
+    kv[i] = si;
+    __syncthreads();
+    for (int k = 2; k <= 256; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const int p = i ^ j;
+            if (p > i) {
+                const int a = kc[i], b = kc[p];
+                if ((i & k) == 0 ? a < b : a > b) {
+                    kc[i] = b;
+                    kc[p] = a;
+                    const int t = kv[i];
+                    kv[i] = kv[p];
+                    kv[p] = t;
+                }
+            }
+            __syncthreads();
+        }
+    if (g < n) out[g] = kv[i];
+}
+
 // findNeighbors + computeForces into forceOut; kick: the velocity-Verlet second half kick of every particle is
 // applied where its force is written (velocityVerletNVE.cpp:23-29); useScreen: the learned-screen path (else the
 // exact one); inRangeOut (nullable): in-range pairs per source; cells: rebuild the cell list first
@@ -564,7 +594,10 @@ void launch_forces_ex(cssg_system* s, bool kick, bool useScreen, double* forceOu
     L.wideRegs = s->tuneWide;
     L.srcCost = s->srcCost;
     L.device = s->ctx->device;
-    if (s->tuneLpt) {
+    if (s->tuneLpt && s->laneLanes > 0) {
+        lpt_segmented<<<(n + 255) / 256, 256, 0, st>>>(n, L.order, s->srcCost, s->lptOrder);
+        L.order = s->lptOrder;
+    } else if (s->tuneLpt) {
         if (n <= kLptSmallMax) {
             lpt_small<<<1, 1024, 0, st>>>(n, L.order, s->srcCost, s->lptOrder);
         } else {
@@ -1041,7 +1074,7 @@ extern "C" int cssg_system_kernels_per_step(cssg_system* s, int* count)
     // forces: [cell list: assign, scan x3, scatter, sort] + [screen: candidates, clamp, scan x3, compact, features,
     // inference, decisions, counts] + [longest-first order: 1 or 3] + three geodesic passes; NVE: walk (with both
     // kicks folded in) + forces; NVT: chain, scale, walk, forces, kick, KE, walk, chain, scale
-    const int lpt = s->tuneLpt ? (s->n <= kLptSmallMax ? 1 : 3) : 0;
+    const int lpt = s->tuneLpt ? ((s->laneLanes > 0 || s->n <= kLptSmallMax) ? 1 : 3) : 0;
     const int forces = (s->useCells ? 6 : 0) + (s->screen ? 10 : (s->laneLanes > 0 ? 1 : 0)) + lpt + 3;
     *count = s->P.integrator == 0 ? 1 + forces : 8 + forces;
     return CSSG_OK;

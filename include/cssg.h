@@ -248,7 +248,9 @@ int cssg_system_screen_counters(cssg_system* sys, unsigned long long* out_host);
  * share a warp, each lane solving its own source (every FP64 instruction then serves up to 32 sources; the pass for
  * many small patches), 0 = source groups of cssg_system_set_tuning's warps_per_source.  Results are the same either
  * way; sources whose tables overflow are redone by the medium and large source-group passes.  Needs the cell-list
- * neighbour structure (range > 0).  cssg_system_autotune also tries both lane widths and keeps the fastest choice;
+ * neighbour structure (range > 0).  With this pass, set_tuning's lpt_order = 1 sorts each run of 256 consecutive
+ * sources of the cell order by their last cost, largest first (sources a warp takes together then cost about the
+ * same and stay close on the mesh).  cssg_system_autotune also tries both lane widths and keeps the fastest choice;
  * cssg_system_lanes reports the current one.  Drops the captured step graph. */
 int cssg_system_set_lanes(cssg_system* sys, int lanes_per_warp);
 int cssg_system_lanes(cssg_system* sys, int* lanes_per_warp);
