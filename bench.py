@@ -41,8 +41,12 @@ BYTES_PER_SOURCE = 4 + 24 + 24 + 24   # read face, barycentrics, R3 position; wr
 BYTES_PER_CANDIDATE = 4 + 4 + 24 + 24  # read index, face, barycentrics, R3 position
 BYTES_PER_FACE = 12 + 12 + 72         # patch face: vertex ids, neighbours, edge frames
 # DRAM bytes (read + write) of one launch of the regular propagation pass, from a full ncu capture of that workload
-# (profiles/geodesic_kernel_torus200x100_N2000_nvt.txt); workloads without a capture report null
-TRAFFIC_BYTES = {"torus200x100_N2000_nvt_patch": 47_415_808 + 112_837_888}
+# (profiles/geodesic_kernel_torus200x100_N2000_nvt.txt, geodesic_kernel_bumpy_sphere7_N20000_screen.txt and
+# lane_kernel_noisy_torus1000x500_N100000_nvt.txt, each with the pass the autotuner picks there); workloads without a
+# capture report null
+TRAFFIC_BYTES = {"torus200x100_N2000_nvt_patch": 47_415_808 + 112_837_888,
+                 "bumpy_sphere7_N20000_nve_patch_screen": 98_366_976 + 41_592_576,
+                 "noisy_torus1000x500_N100000_nvt_patch": 7_921_458 + 976_500_992}
 
 
 def workload_config(name):
@@ -56,8 +60,7 @@ def workload_config(name):
                     audit_every=50)
     if name == "noisy_torus_nvt":
         return dict(workload="noisy_torus1000x500_N100000_nvt_patch", mesh=("noisy_torus", 1000, 500), n=100000,
-                    phi=0.5, sigma=None, integrator="nvt", submesh=True, range_=None, dt=0.001, T=0.05, seed=5,
-                    cpu_subset=1000)
+                    phi=0.5, sigma=None, integrator="nvt", submesh=True, range_=None, dt=0.001, T=0.05, seed=5)
     if name == "mlp_infer":
         return dict(workload="mlp14x64x64x64x1_bf16_4M_pairs", pairs=1 << 22, mlp=True)
     if name == "torus_nvt":
@@ -268,7 +271,7 @@ def run_reference(args, cfg):
     world, rank, _, pg = dist_setup()
     if rank != 0:
         return
-    systems, note = _cpu_subset(cfg, systems_of(cfg))
+    systems = systems_of(cfg)
     threads = os.cpu_count() or 1
     oracle_step_rate(cfg, systems, threads, 0.0, max_steps=args.warmup)  # warm-up
     value, steps = oracle_step_rate(cfg, systems, threads, 1e30, max_steps=args.steps)
@@ -280,31 +283,20 @@ def run_reference(args, cfg):
         "config": {"workload": cfg["workload"], "n": sum(sy["n"] for sy in systems), "systems": len(systems),
                    "integrator": cfg["integrator"], "submesh": cfg["submesh"], "l2": "cpu run"},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{steps} full steps of the workload{note} (oracle restatement; CGAL reference "
-                                   f"not buildable)"},
+                         "sample": f"{steps} full steps of the whole workload (oracle restatement; CGAL "
+                                   f"reference not buildable)"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def _cpu_subset(cfg, systems):
-    """The workload's CPU-baseline sample: the first cfg['cpu_subset'] particles of a single system, if named."""
-    k = cfg.get("cpu_subset")
-    if not k or len(systems) != 1 or systems[0]["n"] <= k:
-        return systems, ""
-    sy = dict(systems[0])
-    sy.update(n=k, f=sy["f"][:k], b=sy["b"][:k], vel=sy["vel"][:k])
-    return [sy], f" ({k}-particle subset of the same mesh and sigma)"
-
-
 def cpu_baseline(cfg, systems, seconds_budget=20.0):
     """Bounded sample of the same workload on the host: the oracle on all threads and on one thread."""
-    systems, note = _cpu_subset(cfg, systems)
     threads = os.cpu_count() or 1
     v_all, s_all = oracle_step_rate(cfg, systems, threads, seconds_budget / 2)
     v_one, s_one = oracle_step_rate(cfg, systems, 1, seconds_budget / 2)
     return {"value": v_all, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{s_all} whole steps of the workload{note} on {threads} threads (oracle restatement; the CGAL "
+            "sample": f"{s_all} whole steps of the whole workload on {threads} threads (oracle restatement; the CGAL "
                       f"reference is not buildable); single thread: {v_one:.1f} particle-steps/s over {s_one} steps"}
 
 
@@ -344,7 +336,7 @@ def run_ours(args, cfg):
         _apply_tuning(S, args.tuning)
         d, w, m, cap, lpt, g, wide = _parse_tuning(args.tuning)
         tune = {"delta_scale": d, "warps_per_block": w, "mid_slots": m, "warps_per_sm": cap, "lpt_order": lpt,
-                "warps_per_source": g, "wide_registers": wide, "lanes_per_warp": S.lanes(), "source": "--tuning"}
+                "warps_per_source": g, "wide_registers": wide, "lanes_per_warp": S.lanes(), "lane_split": S.lane_split(), "source": "--tuning"}
         S.step(1, graph=not args.profile)
         torch.cuda.synchronize()
     elif not args.no_autotune:
@@ -729,8 +721,9 @@ def run_screen(args, cfg):
 
 
 def _parse_tuning(text):
-    """delta_scale,warps_per_block,mid_slots,warps_per_sm,lpt[,warps_per_source[,wide_registers[,lanes]]]: the first
-    seven are System.set_tuning's arguments, the eighth System.set_lanes' (0: source groups)."""
+    """delta_scale,warps_per_block,mid_slots,warps_per_sm,lpt[,warps_per_source[,wide_registers[,lanes[,split]]]]: the
+    first seven are System.set_tuning's arguments, the eighth System.set_lanes' (0: source groups), the ninth
+    System.set_lane_split's (the costliest sources that the group pass takes before the lane pass)."""
     fields = text.split(",")
     d, w, m, cap, lpt = fields[:5]
     g = int(fields[5]) if len(fields) > 5 else 1
@@ -742,6 +735,7 @@ def _apply_tuning(S, text):
     S.set_tuning(*_parse_tuning(text))
     fields = text.split(",")
     S.set_lanes(int(fields[7]) if len(fields) > 7 else 0)
+    S.set_lane_split(int(fields[8]) if len(fields) > 8 else 0)
 
 
 def run_mlp(args, cfg):
@@ -867,8 +861,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (band width 1, 8 warps)")
     ap.add_argument("--tuning", default="",
                     help="explicit tuning instead of the autotuner: delta_scale,warps_per_block,mid_slots,"
-                         "warps_per_sm,lpt[,warps_per_source[,wide_registers[,lanes_per_warp]]] (e.g. 4,8,0,0,1,2,0 "
-                         "or 2,8,0,0,0,1,1,32)")
+                         "warps_per_sm,lpt[,warps_per_source[,wide_registers[,lanes_per_warp[,lane_split]]]] "
+                         "(e.g. 4,8,0,0,1,2,0 or 2,8,0,0,0,1,1,32)")
     ap.add_argument("--profile", action="store_true",
                     help="minimal run for ncu: warm-up steps, then one step without graph replay, no other legs")
     args = ap.parse_args()

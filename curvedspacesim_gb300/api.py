@@ -399,6 +399,22 @@ class System:
         check(_lib.load().cssg_system_lanes(self.h, ctypes.byref(out)), "cssg_system_lanes")
         return out.value
 
+    def set_lane_split(self, group_sources: int):
+        """With the lane pass: the `group_sources` costliest sources of the last evaluation go to the source-group
+        pass, the rest to the lane pass (cssg_system_set_lane_split)."""
+        check(_lib.load().cssg_system_set_lane_split(self.h, int(group_sources)), "cssg_system_set_lane_split")
+
+    def lane_split(self):
+        out = ctypes.c_int()
+        check(_lib.load().cssg_system_lane_split(self.h, ctypes.byref(out)), "cssg_system_lane_split")
+        return out.value
+
+    def source_costs(self):
+        """Work of each source in the last force evaluation (cssg_system_source_costs)."""
+        out = np.zeros(self.n, dtype=np.int32)
+        check(_lib.load().cssg_system_source_costs(self.h, int(self.n), _np_ptr(out)), "cssg_system_source_costs")
+        return out
+
     def set_work_caps(self, regular: int = 0, medium: int = 0, large: int = 0):
         """Per-source window caps of the regular, medium and large propagation passes (<= 0 keeps a cap)."""
         check(_lib.load().cssg_system_set_work_caps(self.h, int(regular), int(medium), int(large)),
@@ -435,7 +451,8 @@ class System:
             check(_lib.load().cssg_system_autotune(self.h, int(reps), _np_ptr(out)), "cssg_system_autotune")
         return {"delta_scale": float(out[0]), "warps_per_block": int(out[1]), "mid_slots": int(out[2]),
                 "warps_per_sm": int(out[3]), "lpt_order": bool(out[4]), "ms_per_force_pass": float(out[5]),
-                "warps_per_source": int(out[6]), "wide_registers": bool(out[7]), "lanes_per_warp": self.lanes()}
+                "warps_per_source": int(out[6]), "wide_registers": bool(out[7]), "lanes_per_warp": self.lanes(),
+                "lane_split": self.lane_split()}
 
     def fire(self, maximum_iterations=1000, alpha_start=0.99, dt_max=0.1, dt_min=1e-5, dt_inc=1.1, dt_dec=0.95,
              alpha_dec=0.9, n_min=4, force_cutoff=1e-12, alpha_min=0.0, reset=False):

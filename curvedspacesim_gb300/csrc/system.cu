@@ -335,6 +335,7 @@ struct cssg_system {
     // regular pass with one source per lane (lanes.cu): lanes per warp (0: the source-group kernel), per-lane
     // capacities, scratch of nLaneWarps warps
     int laneLanes = 0;
+    int laneSplit = 0;  // with the lane pass: the costliest sources (by the last evaluation) that the group pass takes
     LaneCaps laneCaps{};
     void* laneScratch = nullptr;
     int nLaneWarps = 0;
@@ -549,7 +550,7 @@ void launch_forces_ex(cssg_system* s, bool kick, bool useScreen, double* forceOu
                                                        s->slotOf);
         cell_sort<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->cellOf, s->cellStart, s->slotOf, s->cellList);
     }
-    cudaMemsetAsync(s->work, 0, 5 * sizeof(int), st);
+    cudaMemsetAsync(s->work, 0, 6 * sizeof(int), st);
     GeoLaunch L;
     memset(&L, 0, sizeof(L));
     L.sys = useScreen ? s->dsysScreen : s->dsys;
@@ -594,10 +595,13 @@ void launch_forces_ex(cssg_system* s, bool kick, bool useScreen, double* forceOu
     L.wideRegs = s->tuneWide;
     L.srcCost = s->srcCost;
     L.device = s->ctx->device;
-    if (s->tuneLpt && s->laneLanes > 0) {
+    // split of the regular pass: the costliest sources go to the source-group pass, the rest to the lane pass (the
+    // global longest-first order picks them)
+    const int split = s->laneLanes > 0 ? std::min(n, s->laneSplit) : 0;
+    if (s->tuneLpt && s->laneLanes > 0 && split == 0) {
         lpt_segmented<<<(n + 255) / 256, 256, 0, st>>>(n, L.order, s->srcCost, s->lptOrder);
         L.order = s->lptOrder;
-    } else if (s->tuneLpt) {
+    } else if (s->tuneLpt || split > 0) {
         if (n <= kLptSmallMax) {
             lpt_small<<<1, 1024, 0, st>>>(n, L.order, s->srcCost, s->lptOrder);
         } else {
@@ -640,7 +644,16 @@ void launch_forces_ex(cssg_system* s, bool kick, bool useScreen, double* forceOu
             L.rowChord = s->maxChord;
             L.rowCap = s->candCap;
         }
+        if (split > 0) {
+            // the costliest sources with source groups (their windows fill a group's lanes)
+            GeoLaunch G = L;
+            G.nSrc = split;
+            cssg_launch_geodesic(G, st);
+        }
         GeoLaunch LL = L;
+        LL.order = L.order + split;
+        LL.nSrc = n - split;
+        LL.workCounter = s->work + 5;
         LL.scratch = s->laneScratch;
         LL.nSlots = s->nLaneWarps;
         cssg_launch_lanes(LL, s->laneCaps, s->laneLanes, st);
@@ -828,7 +841,7 @@ extern "C" int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh*
     TRY(alloc((void**)&s->srcStatus, sizeof(int) * n));
     TRY(alloc((void**)&s->statusBits, sizeof(int)));
     TRY(alloc((void**)&s->counters, sizeof(unsigned long long) * 8));
-    TRY(alloc((void**)&s->work, sizeof(int) * 5));
+    TRY(alloc((void**)&s->work, sizeof(int) * 6));
     TRY(alloc((void**)&s->failList, sizeof(int) * n));
     TRY(alloc((void**)&s->failList2, sizeof(int) * n));
     TRY(alloc((void**)&s->srcCost, sizeof(int) * n));
@@ -1074,8 +1087,12 @@ extern "C" int cssg_system_kernels_per_step(cssg_system* s, int* count)
     // forces: [cell list: assign, scan x3, scatter, sort] + [screen: candidates, clamp, scan x3, compact, features,
     // inference, decisions, counts] + [longest-first order: 1 or 3] + three geodesic passes; NVE: walk (with both
     // kicks folded in) + forces; NVT: chain, scale, walk, forces, kick, KE, walk, chain, scale
-    const int lpt = s->tuneLpt ? ((s->laneLanes > 0 || s->n <= kLptSmallMax) ? 1 : 3) : 0;
-    const int forces = (s->useCells ? 6 : 0) + (s->screen ? 10 : (s->laneLanes > 0 ? 1 : 0)) + lpt + 3;
+    // with the lane pass: its candidate rows (no screen), the segmented order (1; the global one with a split) and,
+    // with a split, the group pass over the costliest sources
+    const int split = s->laneLanes > 0 && s->laneSplit > 0 ? 1 : 0;
+    const int global = s->n <= kLptSmallMax ? 1 : 3;
+    const int lpt = split ? global : (s->tuneLpt ? (s->laneLanes > 0 ? 1 : global) : 0);
+    const int forces = (s->useCells ? 6 : 0) + (s->screen ? 10 : (s->laneLanes > 0 ? 1 : 0)) + lpt + split + 3;
     *count = s->P.integrator == 0 ? 1 + forces : 8 + forces;
     return CSSG_OK;
 }
@@ -1271,6 +1288,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     int prior = 0;
     CSSG_CUDA(cudaMemcpyAsync(&prior, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost, st));
     CSSG_CUDA(cudaStreamSynchronize(st));
+    s->laneLanes = 0;  // the source-group candidates first
     for (double d : deltas)
         for (const auto& sh : shapes)
             for (int m : mids) {
@@ -1309,7 +1327,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
             }
     // the one-source-per-lane pass (16 or 32 sources per warp, cell or longest-first order); the group tuning found
     // above still serves the sources it hands to the medium and large passes
-    int bLanes = 0;
+    int bLanes = 0, bSplit = 0;
     if (s->useCells) {
         s->tuneDelta = bd;
         s->tuneWpb = bw;
@@ -1317,33 +1335,40 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
         s->tuneGroup = bg;
         s->tuneWide = bx;
         s->nMidSlots = bm;
+        // splits: none, or the costliest 1/64, 1/16 or 1/4 of the sources to the group pass
+        const int splits[] = {0, s->n / 64, s->n / 16, s->n / 4};
         for (int lanes : {16, 32})
-            for (int lpt = 0; lpt < 2; ++lpt) {
-                if (set_lanes(s, lanes) != CSSG_OK) break;
-                s->tuneLpt = lpt != 0;
-                launch_forces(s);
-                launch_forces(s);  // warm-up (and the longest-first order from a lane-pass evaluation)
-                cudaEventRecord(e0, st);
-                for (int r = 0; r < reps; ++r) launch_forces(s);
-                cudaEventRecord(e1, st);
-                cudaError_t err = cudaEventSynchronize(e1);
-                if (err != cudaSuccess) {
-                    cudaEventDestroy(e0);
-                    cudaEventDestroy(e1);
-                    return cssg_cuda_fail(err, "cssg_system_autotune");
+            for (int lpt = 0; lpt < 2; ++lpt)
+                for (int sp = 0; sp < 4; ++sp) {
+                    if (sp > 0 && (lpt == 0 || splits[sp] == 0)) continue;  // a split always orders by cost
+                    if (set_lanes(s, lanes) != CSSG_OK) break;
+                    s->laneSplit = splits[sp];
+                    s->tuneLpt = lpt != 0;
+                    launch_forces(s);
+                    launch_forces(s);  // warm-up (and the longest-first order from a lane-pass evaluation)
+                    cudaEventRecord(e0, st);
+                    for (int r = 0; r < reps; ++r) launch_forces(s);
+                    cudaEventRecord(e1, st);
+                    cudaError_t err = cudaEventSynchronize(e1);
+                    if (err != cudaSuccess) {
+                        cudaEventDestroy(e0);
+                        cudaEventDestroy(e1);
+                        return cssg_cuda_fail(err, "cssg_system_autotune");
+                    }
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    int bits = 0;
+                    cudaMemcpy(&bits, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost);
+                    cudaMemset(s->statusBits, 0, sizeof(int));
+                    if (bits == 0 && ms < best) {
+                        best = ms;
+                        bLanes = lanes;
+                        bSplit = splits[sp];
+                        bl = lpt != 0;
+                    }
                 }
-                float ms = 0;
-                cudaEventElapsedTime(&ms, e0, e1);
-                int bits = 0;
-                cudaMemcpy(&bits, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost);
-                cudaMemset(s->statusBits, 0, sizeof(int));
-                if (bits == 0 && ms < best) {
-                    best = ms;
-                    bLanes = lanes;
-                    bl = lpt != 0;
-                }
-            }
         set_lanes(s, bLanes);
+        s->laneSplit = bSplit;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1548,6 +1573,31 @@ extern "C" int cssg_system_lanes(cssg_system* s, int* lanes_per_warp)
 {
     if (!s || !lanes_per_warp) return cssg_bad_args("cssg_system_lanes");
     *lanes_per_warp = s->laneLanes;
+    return CSSG_OK;
+}
+
+extern "C" int cssg_system_set_lane_split(cssg_system* s, int group_sources)
+{
+    if (!s || group_sources < 0) return cssg_bad_args("cssg_system_set_lane_split");
+    s->laneSplit = std::min(group_sources, s->n);
+    drop_graph(s);
+    return CSSG_OK;
+}
+
+extern "C" int cssg_system_lane_split(cssg_system* s, int* group_sources)
+{
+    if (!s || !group_sources) return cssg_bad_args("cssg_system_lane_split");
+    *group_sources = s->laneSplit;
+    return CSSG_OK;
+}
+
+extern "C" int cssg_system_source_costs(cssg_system* s, int capacity, int* cost_host)
+{
+    if (!s || !cost_host || capacity < s->n) return cssg_bad_args("cssg_system_source_costs");
+    DeviceScope scope(s->ctx->device);
+    CSSG_CUDA(scope.err);
+    CSSG_CUDA(cudaMemcpyAsync(cost_host, s->srcCost, sizeof(int) * s->n, cudaMemcpyDeviceToHost, s->ctx->stream));
+    CSSG_CUDA(cudaStreamSynchronize(s->ctx->stream));
     return CSSG_OK;
 }
 

@@ -214,10 +214,12 @@ int cssg_system_set_tuning(cssg_system* sys, double delta_scale, int warps_per_b
 /* Autotuner: times `reps` force evaluations on the current state for each candidate (delta_scale in {0.5, 1, 2, 4}
  * x (warps_per_block, warps_per_sm, lpt_order, warps_per_source, wide_registers) in {(8,0,0,1,0), (4,0,0,1,0),
  * (8,0,1,1,0), (8,8,1,1,0), (8,4,1,1,0), (8,0,1,2,0), (8,0,1,4,0), (8,0,1,8,0), (8,0,1,1,1), (8,0,1,2,1),
- * (8,0,1,4,1)} x medium slots in {allocated, 8 per SM}), rejects candidates that overflow a table, keeps the fastest
- * and recomputes the forces with it.  result_host (nullable, 8 doubles) = {delta_scale, warps_per_block, mid_slots,
- * warps_per_sm, lpt_order, ms per force evaluation, warps_per_source, wide_registers}.  Synchronises the context's
- * stream. */
+ * (8,0,1,4,1)} x medium slots in {allocated, 8 per SM}), then, on cell-list systems, the
+ * one-source-per-lane pass (cssg_system_set_lanes) with 16 and 32 lanes x lpt_order in {0, 1} x the splits of
+ * cssg_system_set_lane_split; rejects candidates that overflow a table, keeps the fastest and recomputes the forces
+ * with it.  result_host (nullable, 8 doubles) = {delta_scale, warps_per_block, mid_slots, warps_per_sm, lpt_order,
+ * ms per force evaluation, warps_per_source, wide_registers}; the chosen lane
+ * width and split are read with cssg_system_lanes and cssg_system_lane_split.  Synchronises the context's stream. */
 int cssg_system_autotune(cssg_system* sys, int reps, double* result_host);
 /* The reference throws at the first failing walk or geodesic (ERRORERROR, inc/debuggingHelp.h:19-31); here failures
  * are collected. Error summary since the last call (synchronises): OR of (1 << CSSG_ST_*) over walks and sources,
@@ -254,6 +256,16 @@ int cssg_system_screen_counters(cssg_system* sys, unsigned long long* out_host);
  * cssg_system_lanes reports the current one.  Drops the captured step graph. */
 int cssg_system_set_lanes(cssg_system* sys, int lanes_per_warp);
 int cssg_system_lanes(cssg_system* sys, int* lanes_per_warp);
+/* No reference counterpart.  With the lane pass on: the group_sources costliest sources of the last force evaluation
+ * (ordered longest first by cost) are solved by the source-group pass first and the rest by the lane pass (a long
+ * source fills a group's lanes; a warp of lanes waits for its longest source).  0 = the lane pass takes every
+ * source.  Results are the same either way.  cssg_system_autotune tries 0 and 1/64, 1/16 and 1/4 of the sources.
+ * Drops the captured step graph. */
+int cssg_system_set_lane_split(cssg_system* sys, int group_sources);
+int cssg_system_lane_split(cssg_system* sys, int* group_sources);
+/* No reference counterpart (diagnostics).  Work of each source in the last force evaluation (windows processed +
+ * vertex launches + 1, and 8 per round in the group pass): host array of at least the system's particle count. */
+int cssg_system_source_costs(cssg_system* sys, int capacity, int* cost_host);
 /* No reference counterpart (the reference's propagation and walk loops are unbounded, and a failing walk throws:
  * triangulatedMeshSpace.cpp:474, :534-541).  Per-source work caps of the three propagation passes, in windows
  * processed: a source that exceeds the regular pass's cap (or its tables) is redone by the medium pass, then by the

@@ -66,6 +66,14 @@ def test_null_handles_are_argument_errors_without_gpu():
         "cssg_distance_batch_noalloc": (N, N, 1, N, N, N, N, N, 0, 1.0, N, 1.0, N, N, N, N, N),
         "cssg_mesh_set_boundary": (N, 1),
         "cssg_system_create": (N, N, 0, N, N),
+        "cssg_system_set_lanes": (N, 0),
+        "cssg_system_lanes": (N, N),
+        "cssg_system_set_lane_split": (N, 0),
+        "cssg_system_lane_split": (N, N),
+        "cssg_system_source_costs": (N, 0, N),
+        "cssg_system_set_work_caps": (N, 0, 0, 0),
+        "cssg_system_set_screen_audit": (N, 0),
+        "cssg_system_screen_audit_status": (N, N),
     }
     for name, args in calls.items():
         assert getattr(L, name)(*args) == 1, name  # CSSG_ERR_ARG

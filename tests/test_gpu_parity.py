@@ -156,15 +156,20 @@ def test_nvt_patch_matches_oracle(gpu, oracle_mod, lanes):
     np.testing.assert_allclose(S.chain(), ch, rtol=1e-9, atol=1e-12)
 
 
-@pytest.mark.parametrize("lanes", [0, 16, 32])
-def test_pair_sets_identical(gpu, oracle_mod, lanes):
+@pytest.mark.parametrize("lanes,split", [(0, 0), (16, 0), (32, 0), (32, 500)])
+def test_pair_sets_identical(gpu, oracle_mod, lanes, split):
     """Torus 200x100, N=2000: in-range pair sets, distances and forces of one force pass against the oracle, with the
-    source-group pass (lanes = 0) and the one-source-per-lane pass (16 or 32 sources per warp)."""
+    source-group pass (lanes = 0), the one-source-per-lane pass (16 or 32 sources per warp) and the split of the two
+    (the 500 costliest sources of a first evaluation to the group pass)."""
     api, ctx = gpu
     V, F = ms.torus(200, 100)
     n, sigma = 2000, 0.3
     S, f, b, vel = _system(api, ctx, V, F, n, 3, "nvt", sigma, True, sigma, 0.002, 0.05)
     S.set_lanes(lanes)
+    S.set_lane_split(split)
+    if split:
+        S.set_tuning(1.0, 8, 0, 0, True, 1)
+        S.compute_forces()  # costs for the split
     S.enable_pairs()
     S.compute_forces()
     i, j, d, t = S.pairs()
