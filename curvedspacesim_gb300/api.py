@@ -461,12 +461,13 @@ class System:
         p = _lib.cssg_fire_params(int(maximum_iterations), float(alpha_start), float(dt_max), float(dt_min),
                                   float(dt_inc), float(dt_dec), float(alpha_dec), int(n_min), float(force_cutoff),
                                   float(alpha_min))
-        out = np.zeros(5)
+        out = np.zeros(5 * self.K)
         with self.ctx.use():
             check(_lib.load().cssg_system_fire(self.h, ctypes.byref(p), int(bool(reset)), _np_ptr(out)),
                   "cssg_system_fire")
-        return {"iterations": int(out[0]), "force_max": float(out[1]), "dt": float(out[2]), "alpha": float(out[3]),
-                "n_since_negative_power": int(out[4])}
+        res = [{"iterations": int(o[0]), "force_max": float(o[1]), "dt": float(o[2]), "alpha": float(o[3]),
+                "n_since_negative_power": int(o[4])} for o in out.reshape(self.K, 5)]
+        return res[0] if self.K == 1 else res
 
     def stress(self):
         """simulation::computeMonodisperseStress on the current state: 3x3 array."""

@@ -115,7 +115,7 @@ int cssg_bad_args(const char* fn);
 void cssg_launch_transport(const DevMesh* meshes, const int* meshOf, int n, int* face, double* bary, double* disp,
                            double* transport, int nT, int* status, unsigned long long* crossings, double* pos_out,
                            cudaStream_t s, const int* skip = nullptr, int* status_bits = nullptr,
-                           const double* kick_force = nullptr, double kick_dt = 0.0);
+                           const double* kick_force = nullptr, double kick_dt = 0.0, const int* skip_sys = nullptr);
 void cssg_launch_positions(const DevMesh* meshes, const int* meshOf, int n, const int* face, const double* bary,
                            double* pos, cudaStream_t s);
 

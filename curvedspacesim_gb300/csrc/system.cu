@@ -352,7 +352,7 @@ struct cssg_system {
     // FIRE minimisation (device state, transport buffer, reduction partials) and stress partials
     void* fireState = nullptr;
     double* fireTrans = nullptr;  // n x 2 x 3: force and velocity carried by the walk
-    double* firePartials = nullptr;
+    int* fireDone = nullptr;      // K + 1: per-system stop flags, then "every system stopped"
     double* stressPartials = nullptr;
     // NVT
     double* chains = nullptr;
@@ -1037,7 +1037,7 @@ extern "C" int cssg_system_destroy(cssg_system* s)
                     s->statusBits, s->counters, s->cellOf, s->cellCount, s->cellStart, s->cellCursor, s->cellList,
                     s->slotOf, s->scanBlocks, s->scratch, s->midScratch, s->bigScratch, s->work, s->failList,
                     s->failList2, s->srcCost, s->lptOrder, s->lptBuckets, s->fireState, s->fireTrans,
-                    s->firePartials, s->stressPartials, s->pairD, s->pairT,
+                    s->fireDone, s->stressPartials, s->pairD, s->pairT,
                     s->pairJ, s->pairCount, s->chains, s->ke, s->dsys, s->dmeshes, s->sysOf, s->dPartBase,
                     s->mlpParams, s->candJPad, s->candCount, s->maxChord, s->candOff, s->pairI, s->pairJc, s->X,
                     s->chordS, s->yhat, s->skip, s->candScanBlocks, s->mlpErr, s->screenCounters, s->dsysScreen,
@@ -1695,13 +1695,22 @@ struct FireState {
 constexpr int kFireBlock = 256;
 constexpr int kFireChunk = 16;
 
-__global__ void fire_first_half(int n, double* __restrict__ v, const double* __restrict__ f, double* __restrict__ disp,
-                                double* __restrict__ trans, const FireState* __restrict__ st)
+// Each system of a batched object has its own FireState (deltaT, alpha, counters, stop flag) and stops on its own:
+// the per-particle kernels leave the particles of a stopped system alone, and the walk skips them (fireDone[k]).
+__device__ __forceinline__ const FireState& fire_of(const FireState* st, const int* sysOf, int i)
 {
-    if (st->done) return;
+    return st[sysOf ? sysOf[i] : 0];
+}
+
+__global__ void fire_first_half(int n, const int* __restrict__ sysOf, double* __restrict__ v,
+                                const double* __restrict__ f, double* __restrict__ disp, double* __restrict__ trans,
+                                const FireState* __restrict__ st)
+{
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double dt = st->dt;
+    const FireState& S = fire_of(st, sysOf, i);
+    if (S.done) return;
+    const double dt = S.dt;
     for (int c = 0; c < 3; ++c) {
         const int k = 3 * i + c;
         disp[k] = dt * v[k] + 0.5 * dt * dt * f[k];
@@ -1711,148 +1720,144 @@ __global__ void fire_first_half(int n, double* __restrict__ v, const double* __r
     }
 }
 
-__global__ void fire_unpack(int n, const double* __restrict__ trans, double* __restrict__ v, const FireState* st)
+// the transported velocity back, then (after the forces) the second half kick v += dt/2 f
+__global__ void fire_unpack(int n, const int* __restrict__ sysOf, const double* __restrict__ trans,
+                            double* __restrict__ v, const FireState* st)
 {
-    if (st->done) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || fire_of(st, sysOf, i).done) return;
     for (int c = 0; c < 3; ++c) v[3 * i + c] = trans[6 * i + 3 + c];
 }
 
-// v += dt/2 f, then per-block partial sums of F.F, v.v, F.v (fixed order within a block)
-__global__ void __launch_bounds__(kFireBlock) fire_second_half(int n, double* __restrict__ v,
-                                                               const double* __restrict__ f, const FireState* st,
-                                                               double* __restrict__ partials)
+__global__ void fire_second_half(int n, const int* __restrict__ sysOf, double* __restrict__ v,
+                                 const double* __restrict__ f, const FireState* st)
 {
-    if (st->done) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double ff = 0, vv = 0, fv = 0;
-    if (i < n) {
-        const double dt = st->dt;
-        double a[3], b[3];
-        for (int c = 0; c < 3; ++c) {
-            v[3 * i + c] += 0.5 * dt * f[3 * i + c];
-            a[c] = f[3 * i + c];
-            b[c] = v[3 * i + c];
-        }
-        ff = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
-        vv = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
-        fv = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
-    }
+    if (i >= n) return;
+    const FireState& S = fire_of(st, sysOf, i);
+    if (S.done) return;
+    for (int c = 0; c < 3; ++c) v[3 * i + c] += 0.5 * S.dt * f[3 * i + c];
+}
+
+// fixed-order block sum of three values (every thread gets the totals)
+__device__ void fire_block_sum3(double& a, double& b, double& c)
+{
     __shared__ double sh[3][kFireBlock];
-    sh[0][threadIdx.x] = ff;
-    sh[1][threadIdx.x] = vv;
-    sh[2][threadIdx.x] = fv;
+    sh[0][threadIdx.x] = a;
+    sh[1][threadIdx.x] = b;
+    sh[2][threadIdx.x] = c;
     __syncthreads();
     for (int w = kFireBlock / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w)
             for (int k = 0; k < 3; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0)
-        for (int k = 0; k < 3; ++k) partials[3 * blockIdx.x + k] = sh[k][0];
+    a = sh[0][0];
+    b = sh[1][0];
+    c = sh[2][0];
 }
 
-// fireStep's scalar part: scaling from the norms, then the deltaT / alpha update on the sign of the power
-__global__ void fire_scalar(int nBlocks, const double* __restrict__ partials, FireState* st)
+// fireStep (fireMinimization.cpp:38-77) for system blockIdx.x: F.F, v.v, F.v over its particles (fixed order), the
+// mixing scale, then the deltaT / alpha update on the sign of the power
+__global__ void __launch_bounds__(kFireBlock) fire_scalar(const int* __restrict__ partBase,
+                                                          const double* __restrict__ v, const double* __restrict__ f,
+                                                          FireState* st)
 {
-    if (st->done || threadIdx.x != 0) return;
+    FireState& S = st[blockIdx.x];
+    if (S.done) return;  // uniform over the block
     double forceNorm = 0, velocityNorm = 0, power = 0;
-    for (int b = 0; b < nBlocks; ++b) {
-        forceNorm += partials[3 * b];
-        velocityNorm += partials[3 * b + 1];
-        power += partials[3 * b + 2];
+    for (int i = partBase[blockIdx.x] + threadIdx.x; i < partBase[blockIdx.x + 1]; i += kFireBlock) {
+        const double* a = &f[3 * i];
+        const double* b = &v[3 * i];
+        forceNorm += a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+        velocityNorm += b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+        power += a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
     }
+    fire_block_sum3(forceNorm, velocityNorm, power);
+    if (threadIdx.x != 0) return;
     double scaling = 0.0;
     if (forceNorm > 0) scaling = sqrt(velocityNorm / forceNorm);
-    st->mixAlpha = st->alpha;
-    st->mixScale = scaling;
+    S.mixAlpha = S.alpha;
+    S.mixScale = scaling;
     if (power > 0) {
-        if (st->nSince > st->nMin) {
-            st->dt = fmin(st->dt * st->dtInc, st->dtMax);
-            st->alpha = fmax(st->alpha * st->alphaDec, st->alphaMin);
+        if (S.nSince > S.nMin) {
+            S.dt = fmin(S.dt * S.dtInc, S.dtMax);
+            S.alpha = fmax(S.alpha * S.alphaDec, S.alphaMin);
         }
-        st->nSince += 1;
-        st->resetV = 0;
+        S.nSince += 1;
+        S.resetV = 0;
     } else {
-        st->nSince = 0;
-        st->dt = fmax(st->dt * st->dtDec, st->dtMin);
-        st->alpha = st->alphaStart;
-        st->resetV = 1;
+        S.nSince = 0;
+        S.dt = fmax(S.dt * S.dtDec, S.dtMin);
+        S.alpha = S.alphaStart;
+        S.resetV = 1;
     }
 }
 
-// v = (1 - alpha) v + alpha * scaling * F (zero after a non-positive power), then per-block max |F|^2
-__global__ void __launch_bounds__(kFireBlock) fire_mix(int n, double* __restrict__ v, const double* __restrict__ f,
-                                                       const FireState* st, double* __restrict__ partialMax)
+// v = (1 - alpha) v + alpha * scaling * F (zero after a non-positive power)
+__global__ void fire_mix(int n, const int* __restrict__ sysOf, double* __restrict__ v, const double* __restrict__ f,
+                         const FireState* st)
 {
-    if (st->done) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double q = 0;
-    if (i < n) {
-        const double a = st->mixAlpha, as = st->mixAlpha * st->mixScale;
-        const bool reset = st->resetV != 0;
-        for (int c = 0; c < 3; ++c) {
-            const int k = 3 * i + c;
-            v[k] = reset ? 0.0 : (1 - a) * v[k] + as * f[k];
-        }
-        q = f[3 * i] * f[3 * i] + f[3 * i + 1] * f[3 * i + 1] + f[3 * i + 2] * f[3 * i + 2];
+    if (i >= n) return;
+    const FireState& S = fire_of(st, sysOf, i);
+    if (S.done) return;
+    const double a = S.mixAlpha, as = S.mixAlpha * S.mixScale;
+    const bool reset = S.resetV != 0;
+    for (int c = 0; c < 3; ++c) {
+        const int k = 3 * i + c;
+        v[k] = reset ? 0.0 : (1 - a) * v[k] + as * f[k];
     }
+}
+
+// getMaxForce (baseUpdater.cpp:39-54) for system blockIdx.x and the loop condition of minimizeByFire
+// (fireMinimization.cpp:12-20); count = 1 after an iteration (iterations += 1), 0 for the check before the loop.
+// done[k] mirrors the system's stop flag for the walk.
+__global__ void __launch_bounds__(kFireBlock) fire_check(const int* __restrict__ partBase,
+                                                         const double* __restrict__ f, FireState* st,
+                                                         int* __restrict__ done, int count)
+{
+    FireState& S = st[blockIdx.x];
+    if (count && S.done) return;  // uniform over the block
+    double q = 0;
+    for (int i = partBase[blockIdx.x] + threadIdx.x; i < partBase[blockIdx.x + 1]; i += kFireBlock)
+        q = fmax(q, f[3 * i] * f[3 * i] + f[3 * i + 1] * f[3 * i + 1] + f[3 * i + 2] * f[3 * i + 2]);
     for (int o = 16; o > 0; o >>= 1) q = fmax(q, __shfl_xor_sync(0xffffffffu, q, o));
     __shared__ double sh[kFireBlock / 32];
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = q;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = 0;
-        for (int w = 0; w < kFireBlock / 32; ++w) m = fmax(m, sh[w]);
-        partialMax[blockIdx.x] = m;
-    }
+    if (threadIdx.x != 0) return;
+    double m = 0;
+    for (int w = 0; w < kFireBlock / 32; ++w) m = fmax(m, sh[w]);
+    S.forceMax = sqrt(m);
+    if (count) S.iterations += 1;
+    if (!(S.iterations < S.maxIterations && S.forceMax > S.forceCutoff)) S.done = 1;
+    done[blockIdx.x] = S.done;
 }
 
-__global__ void __launch_bounds__(kFireBlock) fire_force_max(int n, const double* __restrict__ f,
-                                                             double* __restrict__ partialMax)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double q = 0;
-    if (i < n) q = f[3 * i] * f[3 * i] + f[3 * i + 1] * f[3 * i + 1] + f[3 * i + 2] * f[3 * i + 2];
-    for (int o = 16; o > 0; o >>= 1) q = fmax(q, __shfl_xor_sync(0xffffffffu, q, o));
-    __shared__ double sh[kFireBlock / 32];
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = q;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = 0;
-        for (int w = 0; w < kFireBlock / 32; ++w) m = fmax(m, sh[w]);
-        partialMax[blockIdx.x] = m;
-    }
-}
-
-// forceMax from the block maxima; `count` = 1 after an iteration (iterations += 1), 0 for the initial check
-__global__ void fire_check(int nBlocks, const double* __restrict__ partialMax, FireState* st, int count)
+// done[K] = every system has stopped (the walk then returns at once, and the host ends the loop)
+__global__ void fire_all_done(int K, int* done)
 {
     if (threadIdx.x != 0) return;
-    if (count && st->done) return;
-    double m = 0;
-    for (int b = 0; b < nBlocks; ++b) m = fmax(m, partialMax[b]);
-    st->forceMax = sqrt(m);
-    if (count) st->iterations += 1;
-    if (!(st->iterations < st->maxIterations && st->forceMax > st->forceCutoff)) st->done = 1;
+    int all = 1;
+    for (int k = 0; k < K; ++k) all &= done[k] != 0;
+    done[K] = all;
 }
 
 void fire_iteration(cssg_system* s, FireState* dst, int nBlocks)
 {
     cudaStream_t st = s->ctx->stream;
-    const int n = s->n;
-    double* partials = s->firePartials;
-    double* partialMax = s->firePartials + 3 * nBlocks;
-    fire_first_half<<<nBlocks, kFireBlock, 0, st>>>(n, s->vel, s->force, s->disp, s->fireTrans, dst);
+    const int n = s->n, K = s->K;
+    fire_first_half<<<nBlocks, kFireBlock, 0, st>>>(n, s->sysOf, s->vel, s->force, s->disp, s->fireTrans, dst);
     cssg_launch_transport(s->dmeshes, s->sysOf, n, s->face, s->bary, s->disp, s->fireTrans, 2, s->walkStatus,
-                          s->counters, s->pos, st, &dst->done, s->statusBits);
-    fire_unpack<<<nBlocks, kFireBlock, 0, st>>>(n, s->fireTrans, s->vel, dst);
+                          s->counters, s->pos, st, s->fireDone + K, s->statusBits, nullptr, 0.0, s->fireDone);
+    fire_unpack<<<nBlocks, kFireBlock, 0, st>>>(n, s->sysOf, s->fireTrans, s->vel, dst);
     launch_forces(s);
-    fire_second_half<<<nBlocks, kFireBlock, 0, st>>>(n, s->vel, s->force, dst, partials);
-    fire_scalar<<<1, 32, 0, st>>>(nBlocks, partials, dst);
-    fire_mix<<<nBlocks, kFireBlock, 0, st>>>(n, s->vel, s->force, dst, partialMax);
-    fire_check<<<1, 32, 0, st>>>(nBlocks, partialMax, dst, 1);
+    fire_second_half<<<nBlocks, kFireBlock, 0, st>>>(n, s->sysOf, s->vel, s->force, dst);
+    fire_scalar<<<K, kFireBlock, 0, st>>>(s->dPartBase, s->vel, s->force, dst);
+    fire_mix<<<nBlocks, kFireBlock, 0, st>>>(n, s->sysOf, s->vel, s->force, dst);
+    fire_check<<<K, kFireBlock, 0, st>>>(s->dPartBase, s->force, dst, s->fireDone, 1);
+    fire_all_done<<<1, 32, 0, st>>>(K, s->fireDone);
 }
 
 // stress partials per block: f(t, d) (x) t over every stored pair and, once per pair, v_i (x) v_i
@@ -1913,49 +1918,53 @@ __global__ void __launch_bounds__(256) stress_partials(int n, int pairCap, const
 
 extern "C" int cssg_system_fire(cssg_system* s, const cssg_fire_params* fp, int reset, double* result_host)
 {
-    if (!s || !fp || s->K != 1 || fp->maximum_iterations < 0) {
-        cssg_set_error("cssg_system_fire: bad arguments (one system per call object; maximum_iterations >= 0)");
+    if (!s || !fp || fp->maximum_iterations < 0) {
+        cssg_set_error("cssg_system_fire: bad arguments (maximum_iterations >= 0)");
         return CSSG_ERR_ARG;
     }
     DeviceScope scope(s->ctx->device);
     CSSG_CUDA(scope.err);
     cudaStream_t st = s->ctx->stream;
-    const int n = s->n;
+    const int n = s->n, K = s->K;
     const int nBlocks = (n + kFireBlock - 1) / kFireBlock;
     if (!s->fireState) {
-        if (int rc = alloc(&s->fireState, sizeof(FireState))) return rc;
+        if (int rc = alloc(&s->fireState, sizeof(FireState) * (size_t)K)) return rc;
         if (int rc = alloc((void**)&s->fireTrans, sizeof(double) * 6 * (size_t)n)) return rc;
-        if (int rc = alloc((void**)&s->firePartials, sizeof(double) * 4 * (size_t)nBlocks)) return rc;
+        if (int rc = alloc((void**)&s->fireDone, sizeof(int) * (size_t)(K + 1))) return rc;
         reset = 1;
     }
-    FireState h;
+    std::vector<FireState> h(K);
     FireState* dst = (FireState*)s->fireState;
     if (reset) {
-        memset(&h, 0, sizeof(h));
-        h.dt = s->P.dt;
-        h.alpha = fp->alpha_start;
+        memset(h.data(), 0, sizeof(FireState) * K);
+        for (auto& x : h) {
+            x.dt = s->P.dt;
+            x.alpha = fp->alpha_start;
+        }
     } else {
-        CSSG_CUDA(cudaMemcpyAsync(&h, dst, sizeof(h), cudaMemcpyDeviceToHost, st));
+        CSSG_CUDA(cudaMemcpyAsync(h.data(), dst, sizeof(FireState) * K, cudaMemcpyDeviceToHost, st));
         CSSG_CUDA(cudaStreamSynchronize(st));
     }
-    h.alphaStart = fp->alpha_start;
-    h.dtMax = fp->dt_max;
-    h.dtMin = fp->dt_min;
-    h.dtInc = fp->dt_inc;
-    h.dtDec = fp->dt_dec;
-    h.alphaDec = fp->alpha_dec;
-    h.forceCutoff = fp->force_cutoff;
-    h.alphaMin = fp->alpha_min;
-    h.nMin = fp->n_min;
-    h.maxIterations = fp->maximum_iterations;
-    h.iterations = 0;
-    h.done = 0;
-    CSSG_CUDA(cudaMemcpyAsync(dst, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+    for (auto& x : h) {
+        x.alphaStart = fp->alpha_start;
+        x.dtMax = fp->dt_max;
+        x.dtMin = fp->dt_min;
+        x.dtInc = fp->dt_inc;
+        x.dtDec = fp->dt_dec;
+        x.alphaDec = fp->alpha_dec;
+        x.forceCutoff = fp->force_cutoff;
+        x.alphaMin = fp->alpha_min;
+        x.nMin = fp->n_min;
+        x.maxIterations = fp->maximum_iterations;
+        x.iterations = 0;
+        x.done = 0;
+    }
+    CSSG_CUDA(cudaMemcpyAsync(dst, h.data(), sizeof(FireState) * K, cudaMemcpyHostToDevice, st));
     // minimizeByFire: forces and forceMax before the loop
     launch_forces(s);
-    fire_force_max<<<nBlocks, kFireBlock, 0, st>>>(n, s->force, s->firePartials + 3 * nBlocks);
-    fire_check<<<1, 32, 0, st>>>(nBlocks, s->firePartials + 3 * nBlocks, dst, 0);
-    // chunks of iterations as one graph; the stop flag is read after each chunk
+    fire_check<<<K, kFireBlock, 0, st>>>(s->dPartBase, s->force, dst, s->fireDone, 0);
+    fire_all_done<<<1, 32, 0, st>>>(K, s->fireDone);
+    // chunks of iterations as one graph; the all-stopped flag is read after each chunk
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
     CSSG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1967,7 +1976,7 @@ extern "C" int cssg_system_fire(cssg_system* s, const cssg_fire_params* fp, int 
     const int maxChunks = fp->maximum_iterations / kFireChunk + 2;
     int done = 0;
     for (int c = 0; c < maxChunks; ++c) {
-        CSSG_CUDA(cudaMemcpyAsync(&done, &dst->done, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CSSG_CUDA(cudaMemcpyAsync(&done, s->fireDone + K, sizeof(int), cudaMemcpyDeviceToHost, st));
         CSSG_CUDA(cudaStreamSynchronize(st));
         if (done) break;
         e = cudaGraphLaunch(ge, st);
@@ -1977,16 +1986,17 @@ extern "C" int cssg_system_fire(cssg_system* s, const cssg_fire_params* fp, int 
         }
     }
     cudaGraphExecDestroy(ge);
-    CSSG_CUDA(cudaMemcpyAsync(&h, dst, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CSSG_CUDA(cudaMemcpyAsync(h.data(), dst, sizeof(FireState) * K, cudaMemcpyDeviceToHost, st));
     CSSG_CUDA(cudaStreamSynchronize(st));
     CSSG_CUDA(cudaGetLastError());
-    if (result_host) {
-        result_host[0] = h.iterations;
-        result_host[1] = h.forceMax;
-        result_host[2] = h.dt;
-        result_host[3] = h.alpha;
-        result_host[4] = h.nSince;
-    }
+    if (result_host)
+        for (int k = 0; k < K; ++k) {
+            result_host[5 * k] = h[k].iterations;
+            result_host[5 * k + 1] = h[k].forceMax;
+            result_host[5 * k + 2] = h[k].dt;
+            result_host[5 * k + 3] = h[k].alpha;
+            result_host[5 * k + 4] = h[k].nSince;
+        }
     return CSSG_OK;
 }
 

@@ -536,12 +536,14 @@ __global__ void __launch_bounds__(128) transport_kernel(const DevMesh* __restric
                                                         double* __restrict__ transport, int ntv, int* __restrict__ status,
                                                         unsigned long long* crossings, double* __restrict__ posOut,
                                                         const int* __restrict__ skip, int* __restrict__ statusBits,
-                                                        const double* __restrict__ kickForce, double kickDt)
+                                                        const double* __restrict__ kickForce, double kickDt,
+                                                        const int* __restrict__ skipSys)
 {
     if (skip && *skip) return;  // a device-side stop flag (FIRE after convergence): nothing moves
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int cr = 0, bits = 0;
-    if (i < n) {
+    // skipSys: per-system stop flags (batched FIRE), the particles of a stopped system stay where they are
+    if (i < n && !(skipSys && skipSys[meshOf ? meshOf[i] : 0])) {
         const DevMesh& M = meshes[meshOf ? meshOf[i] : 0];
         int f = face[i];
         double b[3] = {bary[3 * i], bary[3 * i + 1], bary[3 * i + 2]};
@@ -607,7 +609,8 @@ __global__ void positions_kernel(const DevMesh* __restrict__ meshes, const int* 
 
 void cssg_launch_transport(const DevMesh* meshes, const int* meshOf, int n, int* face, double* bary, double* disp,
                            double* transport, int nT, int* status, unsigned long long* crossings, double* pos_out,
-                           cudaStream_t s, const int* skip, int* status_bits, const double* kick_force, double kick_dt)
+                           cudaStream_t s, const int* skip, int* status_bits, const double* kick_force, double kick_dt,
+                           const int* skip_sys)
 {
     if (n <= 0) return;
     // A warp's FP64 instructions share its SM sub-partition's FP64 pipe with the other warps there.  While the
@@ -619,7 +622,7 @@ void cssg_launch_transport(const DevMesh* meshes, const int* meshOf, int n, int*
     if (nT < 1) kick_force = nullptr;  // the kick needs the velocity as transported vector 0
     transport_kernel<<<(n + threads - 1) / threads, threads, 0, s>>>(meshes, meshOf, n, face, bary, disp, transport, nT,
                                                                      status, crossings, pos_out, skip, status_bits,
-                                                                     kick_force, kick_dt);
+                                                                     kick_force, kick_dt, skip_sys);
 }
 
 void cssg_launch_positions(const DevMesh* meshes, const int* meshOf, int n, const int* face, const double* bary,

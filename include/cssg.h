@@ -176,8 +176,11 @@ int cssg_system_compute_forces(cssg_system* sys);
  * the walk (simpleModel.cpp:44-66), fireStep (fireMinimization.cpp:38-77), getMaxForce (baseUpdater.cpp:39-54).
  * Fields as setFIREParameters (:79-96).  The initial deltaT is the system's dt (the reference's setFIREParameters
  * does not apply its _deltaT argument either).  deltaT, alpha and nSinceNegativePower persist between calls like the
- * reference's members; reset = 1 (or the first call) restarts them at (dt, alpha_start, 0).  One system per object.
- * result_host (nullable, 5 doubles) = {iterations, forceMax, deltaT, alpha, nSinceNegativePower}.  Synchronises. */
+ * reference's members; reset = 1 (or the first call) restarts them at (dt, alpha_start, 0).  A batched object
+ * (cssg_system_create_batched) minimises every system at once, each with its own FIRE state and stopping rule (one
+ * fireMinimization updater per system, same parameters): a converged system stops moving while the others go on.
+ * result_host (nullable, 5 doubles per system) = {iterations, forceMax, deltaT, alpha, nSinceNegativePower} for
+ * system 0, then system 1, ...  Synchronises. */
 typedef struct cssg_fire_params {
     int maximum_iterations;
     double alpha_start, dt_max, dt_min, dt_inc, dt_dec, alpha_dec;

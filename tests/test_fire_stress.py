@@ -127,3 +127,64 @@ def test_gradient_descent_matches_oracle(gpu, oracle_mod, transport_velocity):
     np.testing.assert_allclose(OM.r3(fg, bg), OM.r3(fo, bo), atol=1e-9)
     np.testing.assert_allclose(fcg, fco, atol=1e-9)
     np.testing.assert_allclose(vg, vo if transport_velocity else vel, atol=1e-9)
+
+
+@pytest.mark.gpu
+def test_batched_fire_matches_oracle_and_single_systems(gpu, oracle_mod):
+    """FIRE on a batched object of three systems (different meshes, counts and sigmas): 20 iterations of each system
+    against the oracle's minimizeByFire on that system alone, then minimisation to convergence against the same calls
+    on each system as its own object (each system stops on its own rule; a converged one no longer moves)."""
+    api, ctx = gpu
+    rng = np.random.default_rng(11)
+    specs = [(ms.icosphere(3), 60), (ms.torus(50, 25, 3.0, 1.0), 150), (ms.ellipsoid(3, (1.5, 1.0, 0.7)), 40)]
+    dt = 0.01
+    systems = []
+    for (V, F), n in specs:
+        sigma = ms.sigma_for_area_fraction(ms.total_area(V, F), n, 0.6)
+        f, b = ms.area_weighted_positions(V, F, n, rng)
+        systems.append((V, F, n, sigma, f, b))
+
+    def make(group):
+        meshes = [api.Mesh(V, F) for V, F, *_ in group]
+        params = [api.make_params("nve", "harmonic", k=1 / sg ** 2, sigma=sg, range_=sg, submesh=True, max_dist=sg,
+                                  cutoff=sg, dt=dt) for _, _, _, sg, _, _ in group]
+        S = api.System(ctx, meshes if len(meshes) > 1 else meshes[0], [g[2] for g in group] if len(group) > 1
+                       else group[0][2], params if len(params) > 1 else params[0])
+        n = sum(g[2] for g in group)
+        S.set_state(np.concatenate([g[4] for g in group]), np.concatenate([g[5] for g in group]), np.zeros((n, 3)),
+                    np.zeros((n, 3)))
+        return S
+
+    B = make(systems)
+    res = B.fire(maximum_iterations=20, force_cutoff=1e-300, reset=True)
+    assert isinstance(res, list) and len(res) == 3
+    assert B.check()[0] == 0
+    fg, bg, vg, fcg = B.get_state()
+    off = np.cumsum([0] + [g[2] for g in systems])
+    for k, (V, F, n, sg, f, b) in enumerate(systems):
+        OM = oracle_mod.OracleMesh(V, F)
+        prm = OM.params(0, k=1 / sg ** 2, sigma=sg, rng=sg, submesh=1, max_dist=sg, cutoff=sg, dt=dt)
+        fo, bo, vo, fco, st, it, fmax, err = OM.fire(f, b, np.zeros((n, 3)), np.zeros((n, 3)), prm,
+                                                     maximum_iterations=20, force_cutoff=1e-300)
+        a, e = off[k], off[k + 1]
+        assert err == 0 and it == 20 and res[k]["iterations"] == 20
+        assert np.array_equal(fg[a:e], fo)
+        np.testing.assert_allclose(OM.r3(fg[a:e], bg[a:e]), OM.r3(fo, bo), atol=1e-9)
+        np.testing.assert_allclose(vg[a:e], vo, atol=1e-9)
+        np.testing.assert_allclose(fcg[a:e], fco, atol=1e-9)
+        assert res[k]["dt"] == pytest.approx(st[0], rel=1e-12)
+        assert res[k]["force_max"] == pytest.approx(fmax, rel=1e-9)
+    res2 = B.fire(maximum_iterations=3000, force_cutoff=1e-10)
+    fg2, bg2, _, fcg2 = B.get_state()
+    iters = [r["iterations"] for r in res2]
+    for k, g in enumerate(systems):
+        S = make([g])
+        S.fire(maximum_iterations=20, force_cutoff=1e-300, reset=True)
+        r = S.fire(maximum_iterations=3000, force_cutoff=1e-10)
+        a, e = off[k], off[k + 1]
+        assert res2[k]["force_max"] <= 1e-10 and abs(res2[k]["iterations"] - r["iterations"]) <= 1, (k, res2[k], r)
+        fs, bs, _, _ = S.get_state()
+        OM = oracle_mod.OracleMesh(g[0], g[1])
+        np.testing.assert_allclose(OM.r3(fg2[a:e], bg2[a:e]), OM.r3(fs, bs), atol=1e-7)
+        assert np.max(np.linalg.norm(fcg2[a:e], axis=1)) <= 1e-10
+    assert len(set(iters)) > 1, iters  # the systems converged at different iterations
