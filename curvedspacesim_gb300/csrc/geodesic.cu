@@ -265,7 +265,7 @@ __device__ __forceinline__ int window_dest(const DevMesh& M, const Slot& S, cons
     return (double)key <= ctl->thr ? 1 : 2;
 }
 
-__device__ __noinline__ void push_win(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, Win w)
+__device__ __forceinline__ void push_win(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, WarpCtl* ctl, Win w)
 {
     const int dest = window_dest(M, S, C, src, ctl, w);
     if (dest == 0) return;

@@ -1360,7 +1360,9 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
                     int bits = 0;
                     cudaMemcpy(&bits, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost);
                     cudaMemset(s->statusBits, 0, sizeof(int));
-                    if (bits == 0 && ms < best) {
+                    // the lane pass must beat the source groups by 5%: its time depends more on the state (a warp
+                    // waits for its slowest source; the split follows the last evaluation's costs)
+                    if (bits == 0 && ms < (bLanes ? best : 0.95 * best)) {
                         best = ms;
                         bLanes = lanes;
                         bSplit = splits[sp];

@@ -219,8 +219,8 @@ int cssg_system_set_tuning(cssg_system* sys, double delta_scale, int warps_per_b
  * (8,0,1,1,0), (8,8,1,1,0), (8,4,1,1,0), (8,0,1,2,0), (8,0,1,4,0), (8,0,1,8,0), (8,0,1,1,1), (8,0,1,2,1),
  * (8,0,1,4,1)} x medium slots in {allocated, 8 per SM}), then, on cell-list systems, the
  * one-source-per-lane pass (cssg_system_set_lanes) with 16 and 32 lanes x lpt_order in {0, 1} x the splits of
- * cssg_system_set_lane_split; rejects candidates that overflow a table, keeps the fastest and recomputes the forces
- * with it.  result_host (nullable, 8 doubles) = {delta_scale, warps_per_block, mid_slots, warps_per_sm, lpt_order,
+ * cssg_system_set_lane_split; rejects candidates that overflow a table, keeps the fastest (a lane-pass candidate only
+ * when it beats the best source-group one by 5%) and recomputes the forces with it.  result_host (nullable, 8 doubles) = {delta_scale, warps_per_block, mid_slots, warps_per_sm, lpt_order,
  * ms per force evaluation, warps_per_source, wide_registers}; the chosen lane
  * width and split are read with cssg_system_lanes and cssg_system_lane_split.  Synchronises the context's stream. */
 int cssg_system_autotune(cssg_system* sys, int reps, double* result_host);
