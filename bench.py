@@ -727,7 +727,7 @@ def _parse_tuning(text):
     fields = text.split(",")
     d, w, m, cap, lpt = fields[:5]
     g = int(fields[5]) if len(fields) > 5 else 1
-    wide = bool(int(fields[6])) if len(fields) > 6 else False
+    wide = int(fields[6]) if len(fields) > 6 else 0
     return float(d), int(w), int(m), int(cap), bool(int(lpt)), g, wide
 
 

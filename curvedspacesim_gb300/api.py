@@ -437,12 +437,12 @@ class System:
 
     def set_tuning(self, delta_scale: float = 1.0, warps_per_block: int = 8, mid_slots: int = 0,
                    warps_per_sm: int = 0, lpt_order: bool = False, warps_per_source: int = 1,
-                   wide_registers: bool = False):
+                   wide_registers: int = 0):
         """Band width scale, block size (warps), medium-pass slots, per-SM warp cap, longest-first source order,
-        warps per source and the 255-register kernel build."""
+        warps per source and the kernel build (bit 0: 255 registers, bit 1: out-of-line hash-table probes)."""
         check(_lib.load().cssg_system_set_tuning(self.h, float(delta_scale), int(warps_per_block), int(mid_slots),
                                                  int(warps_per_sm), int(bool(lpt_order)), int(warps_per_source),
-                                                 int(bool(wide_registers))), "cssg_system_set_tuning")
+                                                 int(wide_registers)), "cssg_system_set_tuning")
 
     def autotune(self, reps: int = 3):
         """Pick the fastest tuning on the current state (cssg_system_autotune); returns it with its time."""
@@ -451,7 +451,8 @@ class System:
             check(_lib.load().cssg_system_autotune(self.h, int(reps), _np_ptr(out)), "cssg_system_autotune")
         return {"delta_scale": float(out[0]), "warps_per_block": int(out[1]), "mid_slots": int(out[2]),
                 "warps_per_sm": int(out[3]), "lpt_order": bool(out[4]), "ms_per_force_pass": float(out[5]),
-                "warps_per_source": int(out[6]), "wide_registers": bool(out[7]), "lanes_per_warp": self.lanes(),
+                "warps_per_source": int(out[6]), "wide_registers": bool(int(out[7]) & 1),
+                "outlined_probes": bool(int(out[7]) & 2), "lanes_per_warp": self.lanes(),
                 "lane_split": self.lane_split()}
 
     def fire(self, maximum_iterations=1000, alpha_start=0.99, dt_max=0.1, dt_min=1e-5, dt_inc=1.1, dt_dec=0.95,

@@ -21,7 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr"]
 PER_FILE = {"walk.cu": ["-fmad=false"]}
-SOURCES = ["mesh.cu", "walk.cu", "geodesic.cu", "lanes.cu", "system.cu", "diag.cu", "mlp.cu", "noalloc.cu"]
+SOURCES = ["mesh.cu", "walk.cu", "geodesic.cu", "geodesic_outlined.cu", "lanes.cu", "system.cu", "diag.cu", "mlp.cu",
+           "noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -214,6 +214,7 @@ struct GeoLaunch {
     int warpsPerSM;              // > 0: at most this many source warps per SM (the rest of the slots stay idle)
     int groupWarps;              // warps that solve one source together: 1 (default), 2, 4 or 8
     int wideRegs;                // 1: the kernel build with up to 255 registers per thread (fewer warps per SM)
+    int hashOutline;             // 1: the kernel build with out-of-line hash-table probes (geodesic_outlined.cu)
     int* srcCost;                // nullable: work of each source (windows + launches + rounds), for the next order
     int smemTables;              // set by cssg_launch_geodesic: hash tables in shared memory
     int device;                  // the CUDA device the launch runs on (SM count, occupancy, attributes)
@@ -236,6 +237,9 @@ size_t cssg_geo_smem_per_warp(const GeoCaps& c);
 // Fills slots with their initial (empty) state; call once after allocating the scratch.
 void cssg_geo_init_scratch(void* scratch, size_t slotBytes, int nSlots, const GeoCaps& c, cudaStream_t s);
 void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s);
+// the same kernels built with out-of-line hash-table probes (geodesic_outlined.cu); cssg_launch_geodesic calls it
+// when L.hashOutline is set
+void cssg_launch_geodesic_outlined(GeoLaunch L, cudaStream_t s);
 // ---- one source per lane (lanes.cu) ----------------------------------------------------------------------------------
 // Per-lane table capacities: targets, face table and vertex table (powers of two), window slab.
 struct LaneCaps {

@@ -145,7 +145,14 @@ __device__ inline void carve_smem(const GeoCaps& c, char* base, Slot* S)
 __device__ __forceinline__ unsigned hash_int(int k) { return (unsigned)k * 2654435761u; }
 
 // ---- hash tables ----------------------------------------------------------------------------------------------
-__device__ int vfind(const Slot& S, int CV, int v)
+// CSSG_GEO_OUTLINE (geodesic_outlined.cu) compiles the probes out of line: one copy of each instead of one per call
+// site, a smaller kernel with fewer instruction-cache misses where sources are small and every phase is hot.
+#ifdef CSSG_GEO_OUTLINE
+#define CSSG_PROBE __noinline__
+#else
+#define CSSG_PROBE
+#endif
+__device__ CSSG_PROBE int vfind(const Slot& S, int CV, int v)
 {
     unsigned h = hash_int(v) & (CV - 1);
     for (int p = 0; p < CV; ++p) {
@@ -157,7 +164,7 @@ __device__ int vfind(const Slot& S, int CV, int v)
     return -1;
 }
 
-__device__ int vinsert(const Slot& S, int CV, int v, WarpCtl* ctl)
+__device__ CSSG_PROBE int vinsert(const Slot& S, int CV, int v, WarpCtl* ctl)
 {
     unsigned h = hash_int(v) & (CV - 1);
     for (int p = 0; p < CV; ++p) {
@@ -178,7 +185,7 @@ __device__ int vinsert(const Slot& S, int CV, int v, WarpCtl* ctl)
     return -1;
 }
 
-__device__ int ffind(const Slot& S, int CF, int f)
+__device__ CSSG_PROBE int ffind(const Slot& S, int CF, int f)
 {
     unsigned h = hash_int(f) & (CF - 1);
     for (int p = 0; p < CF; ++p) {
@@ -191,7 +198,7 @@ __device__ int ffind(const Slot& S, int CF, int f)
 }
 
 // returns slot; *fresh = 1 when this call inserted the key
-__device__ int finsert(const Slot& S, int CF, int f, WarpCtl* ctl, int* fresh)
+__device__ CSSG_PROBE int finsert(const Slot& S, int CF, int f, WarpCtl* ctl, int* fresh)
 {
     *fresh = 0;
     unsigned h = hash_int(f) & (CF - 1);
@@ -1374,6 +1381,7 @@ __global__ void max_count_kernel(int n, const int* off, int* out)
     }
 }
 
+#ifndef CSSG_GEO_OUTLINE
 int next_pow2(long long x)
 {
     int p = 1;
@@ -1381,8 +1389,10 @@ int next_pow2(long long x)
     return p;
 }
 
+#endif
 }  // namespace
 
+#ifndef CSSG_GEO_OUTLINE
 // warp per source: the same candidate search as the fused kernel's cell-list mode, written out as padded rows
 __global__ void __launch_bounds__(256) candidates_kernel(GeoLaunch L, int n, int cap, int* __restrict__ candJ,
                                                          int* __restrict__ count, double* __restrict__ maxChord)
@@ -1449,7 +1459,9 @@ void cssg_geo_init_scratch(void* scratch, size_t slotBytes, int nSlots, const Ge
 }
 
 size_t cssg_geo_smem_per_warp(const GeoCaps& c) { return smem_per_warp(c); }
+#endif
 
+namespace {
 template <int G, int MINB>
 void launch_groups(GeoLaunch L, cudaStream_t s)
 {
@@ -1487,8 +1499,20 @@ void launch_groups(GeoLaunch L, cudaStream_t s)
     geodesic_kernel<G, MINB><<<blocks, 32 * G * gpb, smem, s>>>(L);
 }
 
+}  // namespace
+
+#ifdef CSSG_GEO_OUTLINE
+void cssg_launch_geodesic_outlined(GeoLaunch L, cudaStream_t s)
+#else
 void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
+#endif
 {
+#ifndef CSSG_GEO_OUTLINE
+    if (L.hashOutline) {
+        cssg_launch_geodesic_outlined(L, s);
+        return;
+    }
+#endif
     if (L.wideRegs) {
         if (L.groupWarps == 8) launch_groups<8, 1>(L, s);
         else if (L.groupWarps == 4) launch_groups<4, 1>(L, s);
@@ -1502,6 +1526,7 @@ void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
     }
 }
 
+#ifndef CSSG_GEO_OUTLINE
 GeoSizing cssg_geo_sizing(const cssg_mesh* mesh, int maxTargets, int submesh, double max_dist, double cutoff)
 {
     GeoSizing z;
@@ -1612,3 +1637,4 @@ extern "C" int cssg_distance_batch(cssg_ctx* ctx, const cssg_mesh* mesh, int nSr
     CSSG_CUDA(cudaFreeAsync(work, s));
     return CSSG_OK;
 }
+#endif  // CSSG_GEO_OUTLINE

@@ -366,7 +366,7 @@ struct cssg_system {
     int tuneWpb = 8;
     int tuneWarpsPerSM = 0;  // 0: every slot
     int tuneGroup = 1;       // warps per source (1, 2, 4, 8)
-    int tuneWide = 0;        // 1: the 255-register kernel build
+    int tuneWide = 0;        // kernel build: bit 0 = up to 255 registers, bit 1 = out-of-line hash-table probes
     bool tuneLpt = false;    // sources in decreasing order of their last cost (longest first) instead of cell order
     int* srcCost = nullptr;  // n: work of each source in the last force evaluation
     int* lptOrder = nullptr; // n
@@ -592,7 +592,8 @@ void launch_forces_ex(cssg_system* s, bool kick, bool useScreen, double* forceOu
     L.wpbMax = s->tuneWpb;
     L.warpsPerSM = s->tuneWarpsPerSM;
     L.groupWarps = s->tuneGroup;
-    L.wideRegs = s->tuneWide;
+    L.wideRegs = s->tuneWide & 1;
+    L.hashOutline = (s->tuneWide >> 1) & 1;
     L.srcCost = s->srcCost;
     L.device = s->ctx->device;
     // split of the regular pass: the costliest sources go to the source-group pass, the rest to the lane pass (the
@@ -1241,13 +1242,14 @@ extern "C" int cssg_system_set_tuning(cssg_system* s, double delta_scale, int wa
                                       int warps_per_sm, int lpt_order, int warps_per_source, int wide_registers)
 {
     if (!s || !(delta_scale > 0) || warps_per_block < 1 || warps_per_block > 8 || warps_per_sm < 0 ||
-        (warps_per_source != 1 && warps_per_source != 2 && warps_per_source != 4 && warps_per_source != 8)) {
+        (warps_per_source != 1 && warps_per_source != 2 && warps_per_source != 4 && warps_per_source != 8) ||
+        wide_registers < 0 || wide_registers > 3) {
         cssg_set_error("cssg_system_set_tuning: bad arguments (delta_scale > 0, 1 <= warps_per_block <= 8, "
-                       "warps_per_sm >= 0, warps_per_source in {1, 2, 4, 8})");
+                       "warps_per_sm >= 0, warps_per_source in {1, 2, 4, 8}, kernel build 0..3)");
         return CSSG_ERR_ARG;
     }
     s->tuneGroup = warps_per_source;
-    s->tuneWide = wide_registers != 0;
+    s->tuneWide = wide_registers;
     s->tuneDelta = delta_scale;
     s->tuneWpb = warps_per_block;
     if (mid_slots > 0) s->nMidSlots = std::min(mid_slots, s->midSlotsMax);
@@ -1273,7 +1275,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     // (warps per block, warps per SM cap, longest-first order, warps per source, wide registers)
     const int shapes[][5] = {{8, 0, 0, 1, 0}, {4, 0, 0, 1, 0}, {8, 0, 1, 1, 0}, {8, 8, 1, 1, 0}, {8, 4, 1, 1, 0},
                              {8, 0, 1, 2, 0}, {8, 0, 1, 4, 0}, {8, 0, 1, 8, 0}, {8, 0, 1, 1, 1}, {8, 0, 1, 2, 1},
-                             {8, 0, 1, 4, 1}};
+                             {8, 0, 1, 4, 1}, {8, 0, 1, 1, 3}, {8, 0, 1, 1, 2}, {8, 0, 1, 2, 3}};
     std::vector<int> mids{s->midSlotsMax};
     if (s->midSlotsMax > sms * 8) mids.push_back(sms * 8);
     cudaEvent_t e0, e1;

@@ -209,15 +209,16 @@ int cssg_system_stress(cssg_system* sys, double* stress_host);
  * (<= the number allocated at creation; <= 0 keeps the current value); warps_per_sm: > 0 caps the source warps of
  * the regular pass per SM (0: all slots); lpt_order: 1 processes sources longest first by their cost in the last
  * force evaluation, 0 in cell order; warps_per_source: 1, 2, 4 or 8 warps solve one source together (a few sources
- * on many SMs want more); wide_registers: 1 selects the kernel build with up to 255 registers per thread (no
- * register spills, at most 8 warps per SM).  Results do not depend on these, only the work and its balance do.
+ * on many SMs want more); wide_registers: the kernel build, bit 0 = up to 255 registers per thread (no register
+ * spills, at most 8 warps per SM; else 128), bit 1 = hash-table probes out of line (a smaller kernel, faster where
+ * sources are small).  Results do not depend on these, only the work and its balance do.
  * Drops the captured step graph. */
 int cssg_system_set_tuning(cssg_system* sys, double delta_scale, int warps_per_block, int mid_slots, int warps_per_sm,
                            int lpt_order, int warps_per_source, int wide_registers);
 /* Autotuner: times `reps` force evaluations on the current state for each candidate (delta_scale in {0.5, 1, 2, 4}
  * x (warps_per_block, warps_per_sm, lpt_order, warps_per_source, wide_registers) in {(8,0,0,1,0), (4,0,0,1,0),
  * (8,0,1,1,0), (8,8,1,1,0), (8,4,1,1,0), (8,0,1,2,0), (8,0,1,4,0), (8,0,1,8,0), (8,0,1,1,1), (8,0,1,2,1),
- * (8,0,1,4,1)} x medium slots in {allocated, 8 per SM}), then, on cell-list systems, the
+ * (8,0,1,4,1), (8,0,1,1,3), (8,0,1,1,2), (8,0,1,2,3)} x medium slots in {allocated, 8 per SM}), then, on cell-list systems, the
  * one-source-per-lane pass (cssg_system_set_lanes) with 16 and 32 lanes x lpt_order in {0, 1} x the splits of
  * cssg_system_set_lane_split; rejects candidates that overflow a table, keeps the fastest (a lane-pass candidate only
  * when it beats the best source-group one by 5%) and recomputes the forces with it.  result_host (nullable, 8 doubles) = {delta_scale, warps_per_block, mid_slots, warps_per_sm, lpt_order,

@@ -43,8 +43,10 @@ def _compare_pairs(i, j, d, src, idx, do, sigma, sources=None):
     return rel
 
 
-@pytest.mark.parametrize("lanes", [0, 32])
-def test_bumpy_sphere7_exact_and_screened_match_oracle(gpu, oracle_mod, lanes):
+@pytest.mark.parametrize("lanes,build", [(0, 0), (32, 0), (0, 3)])
+def test_bumpy_sphere7_exact_and_screened_match_oracle(gpu, oracle_mod, lanes, build):
+    """Config 4 (bumpy sphere 7, N=20,000): one exact and one screened force pass against the oracle, with the
+    source-group pass (default build, and the 255-register build with out-of-line probes) and the lane pass."""
     api, ctx = gpu
     from curvedspacesim_gb300 import screen
     bench = _bench()
@@ -72,6 +74,8 @@ def test_bumpy_sphere7_exact_and_screened_match_oracle(gpu, oracle_mod, lanes):
     for screened in (False, True):
         S = api.System(ctx, M, n, p)
         S.set_lanes(lanes)
+        if build:
+            S.set_tuning(2.0, 8, 0, 0, True, 1, build)
         S.set_state(f, b, vel, np.zeros((n, 3)))
         if screened:
             S.set_screen(params, margin)
@@ -82,7 +86,7 @@ def test_bumpy_sphere7_exact_and_screened_match_oracle(gpu, oracle_mod, lanes):
         i, j, d, _ = S.pairs()
         rel = _compare_pairs(i, j, d, src, idx, do, sigma)
         np.testing.assert_allclose(S.get_state()[3], fo, atol=1e-9)
-        print(f"bumpy sphere 7, lanes {lanes}, {'screened' if screened else 'exact'}: {cnt['in_range_pairs']} pairs, "
+        print(f"bumpy sphere 7, lanes {lanes}, build {build}, {'screened' if screened else 'exact'}: {cnt['in_range_pairs']} pairs, "
               f"max relative distance error {rel:.2e}")
 
 

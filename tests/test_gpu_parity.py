@@ -245,7 +245,8 @@ def test_autotune_keeps_results(gpu, oracle_mod):
     np.testing.assert_allclose(f1, f0, rtol=0, atol=1e-12)
     for args in ((0.5, 4, 0, 0, False, 1), (2.0, 8, 0, 2, True, 1), (1.0, 8, 0, 4, True, 1), (1.0, 8, 0, 0, True, 2),
                  (4.0, 8, 0, 0, False, 4), (0.5, 4, 0, 8, True, 4), (2.0, 8, 0, 0, True, 8),
-                 (4.0, 8, 0, 0, True, 2, True), (1.0, 8, 0, 0, True, 1, True)):
+                 (4.0, 8, 0, 0, True, 2, True), (1.0, 8, 0, 0, True, 1, True), (2.0, 8, 0, 0, True, 1, 3),
+                 (1.0, 8, 0, 0, True, 2, 2), (0.5, 4, 0, 0, False, 4, 3)):
         S.set_tuning(*args)
         S.compute_forces()
         S.compute_forces()  # the second evaluation uses the longest-first order built from the first
