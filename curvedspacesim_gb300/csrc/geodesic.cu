@@ -71,6 +71,7 @@ struct Slot {
     double* vty;
     unsigned long long* vtok;
     unsigned long long* vlaunched;  // label bits a vertex was last launched with
+    signed char* vcan;              // can the vertex become a pseudo-source: -1 not evaluated yet, 0 no, 1 yes
     int* vlist;
     int* fkey;
     int* fhead;
@@ -110,6 +111,7 @@ __host__ __device__ inline size_t carve(const GeoCaps& c, char* base, Slot* S)
     CARVE(vty, double, c.CV);
     CARVE(vtok, unsigned long long, c.CV);
     CARVE(vlaunched, unsigned long long, c.CV);
+    CARVE(vcan, signed char, c.CV);
     CARVE(vlist, int, c.CV);
     CARVE(flist, int, c.CF);
     CARVE(wA, Win, c.CW);
@@ -128,10 +130,10 @@ __host__ __device__ inline size_t carve(const GeoCaps& c, char* base, Slot* S)
 }
 
 // the probed hash tables live in shared memory when they fit (else in the global slot): vertex labels (key, label
-// bits) and faces (key, target-list head)
+// bits, launchability) and faces (key, target-list head)
 __host__ __device__ inline size_t smem_per_warp(const GeoCaps& c)
 {
-    return (size_t)c.CV * 8 + (size_t)c.CV * 4 + (size_t)c.CF * 8;
+    return (size_t)c.CV * 8 + (size_t)c.CV * 4 + (size_t)c.CF * 8 + (size_t)c.CV;
 }
 
 __device__ inline void carve_smem(const GeoCaps& c, char* base, Slot* S)
@@ -140,6 +142,7 @@ __device__ inline void carve_smem(const GeoCaps& c, char* base, Slot* S)
     S->vkey = (int*)(base + (size_t)c.CV * 8);
     S->fkey = (int*)(base + (size_t)c.CV * 12);
     S->fhead = (int*)(base + (size_t)c.CV * 12 + (size_t)c.CF * 4);
+    S->vcan = (signed char*)(base + (size_t)c.CV * 12 + (size_t)c.CF * 8);
 }
 
 __device__ __forceinline__ unsigned hash_int(int k) { return (unsigned)k * 2654435761u; }
@@ -320,13 +323,19 @@ __device__ __forceinline__ void propose_from(const Slot& S, const GeoCaps& C, Wa
     if (rec.slot >= 0) start_dir_l(w, px, py, l, rec.dx, rec.dy);
 }
 
-__device__ __noinline__ bool launchable(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int v)
+// Can vertex v (vertex-table slot h) become a pseudo-source: a border or saddle vertex of the mesh, or on a patch, a
+// vertex with an incident face outside the patch.  The patch is complete before the first call, so the answer is
+// cached per slot (lanes that evaluate the same vertex at once store the same value).
+__device__ __noinline__ bool launchable(const DevMesh& M, const Slot& S, const GeoCaps& C, const Src& src, int v, int h)
 {
     if (M.vflag[v] & (VF_BORDER | VF_SADDLE)) return true;
     if (src.full) return false;
-    for (int i = M.vfStart[v]; i < M.vfStart[v + 1]; ++i)
-        if (ffind(S, C.CF, M.vfList[i]) < 0) return true;
-    return false;
+    const signed char known = *(volatile signed char*)&S.vcan[h];
+    if (known >= 0) return known != 0;
+    bool out = false;
+    for (int i = M.vfStart[v]; i < M.vfStart[v + 1] && !out; ++i) out = ffind(S, C.CF, M.vfList[i]) < 0;
+    S.vcan[h] = out ? 1 : 0;
+    return out;
 }
 
 // after __syncwarp: the surviving proposal writes the start direction and queues a pseudo-source launch
@@ -338,7 +347,7 @@ __device__ void resolve(const DevMesh& M, const Slot& S, const GeoCaps& C, const
     if (ldv(&S.vlab[r.slot]) != b) return;
     S.vtx[r.slot] = r.dx;
     S.vty[r.slot] = r.dy;
-    if (r.d <= src.cutoff && launchable(M, S, C, src, r.v)) {
+    if (r.d <= src.cutoff && launchable(M, S, C, src, r.v, r.slot)) {
         if (atomicExch(&S.vtok[r.slot], b) != b) {
             int pos = atomicAdd(&ctl->nLA, 1);
             if (pos < C.CL) S.lA[pos] = r.v;
@@ -1265,6 +1274,7 @@ __device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, const 
         S.vlab[h] = INF_BITS;
         S.vtok[h] = ~0ull;
         S.vlaunched[h] = ~0ull;
+        S.vcan[h] = -1;
     }
     for (int q = lane; q < nF; q += NT) {
         int h = S.flist[q];
@@ -1279,6 +1289,7 @@ __device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, const 
             S.vlab[q] = INF_BITS;
             S.vtok[q] = ~0ull;
             S.vlaunched[q] = ~0ull;
+            S.vcan[q] = -1;
         }
         for (int q = lane; q < C.CF; q += NT) {
             S.fkey[q] = -1;
@@ -1321,6 +1332,7 @@ __global__ void __launch_bounds__(256, MINB) geodesic_kernel(GeoLaunch L)
         for (int q = gp.t; q < L.caps.CV; q += NT) {
             S.vkey[q] = -1;
             S.vlab[q] = INF_BITS;
+            S.vcan[q] = -1;
         }
         for (int q = gp.t; q < L.caps.CF; q += NT) {
             S.fkey[q] = -1;
@@ -1356,6 +1368,7 @@ __global__ void init_scratch_kernel(char* scratch, size_t slotBytes, int nSlots,
     for (int q = threadIdx.x; q < C.CV; q += blockDim.x) {
         S.vtok[q] = ~0ull;
         S.vlaunched[q] = ~0ull;
+        S.vcan[q] = -1;
         S.vkey[q] = -1;
         S.vlab[q] = INF_BITS;
     }
@@ -1477,7 +1490,9 @@ void launch_groups(GeoLaunch L, cudaStream_t s)
         gpb = (int)std::max<size_t>(1, std::min<size_t>(gpb, budget / per));
         smem = per * gpb;
         static std::atomic<unsigned long long> configured{0};
-        if (smem > 48 * 1024) cssg_raise_smem_once(configured, geodesic_kernel<G, MINB>, (int)budget, dev);
+        // the 48 KB default covers static + dynamic shared memory together, so raise the limit whenever the tables
+        // are in shared memory (once per device)
+        cssg_raise_smem_once(configured, geodesic_kernel<G, MINB>, (int)budget, dev);
     }
     // spread the groups evenly over the SMs: sources are FP64-pipe bound per SM, so an SM holding two blocks while
     // another holds one would take twice as long.  Full occupancy = sms * bps blocks; fewer slots than that get
