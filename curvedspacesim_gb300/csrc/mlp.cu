@@ -58,6 +58,29 @@ __device__ __forceinline__ float gelu_grad(float x)
 
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16(x)); }
 
+// GELU for the inference epilogue: the same tanh form, with tanh(u) = 1 - 2 / (exp(2u) + 1) from the fast exponential
+// and division intrinsics (absolute error ~1e-7, far below the BF16 rounding of the activations that follows;
+// exp(2u) = inf gives tanh = 1, exp(2u) = 0 gives -1)
+__device__ __forceinline__ float gelu_fast(float x)
+{
+    const float k0 = 0.7978845608028654f, k1 = 0.044715f;
+    const float u = k0 * (x + k1 * x * x * x);
+    const float t = 1.0f - __fdividef(2.0f, __expf(2.0f * u) + 1.0f);
+    return 0.5f * x * (1.0f + t);
+}
+
+// eight BF16 values as one 16-byte word (k-contiguous run of a core matrix row)
+__device__ __forceinline__ uint4 pack8_bf16(const float* v)
+{
+    uint4 w;
+    uint32_t* p = reinterpret_cast<uint32_t*>(&w);
+    for (int i = 0; i < 4; ++i) {
+        const __nv_bfloat162 b = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+        p[i] = *reinterpret_cast<const uint32_t*>(&b);
+    }
+    return w;
+}
+
 // ---- features ------------------------------------------------------------------------------------------------
 // In the frame of the source face with u = in-plane chord direction and w = n_i x u:
 //   rho/s, c.n_i/s, n_j.u, n_j.w, n_j.n_i, |c|/s, H_i s, K_i s^2, H_j s, K_j s^2, c.n_j/s, e_i/s, e_j/s, |c|^2/s^2
@@ -240,10 +263,17 @@ __global__ void __launch_bounds__(128) mlp_infer_tc(const __nv_bfloat16* __restr
     float h[NH];
     for (int tile = blockIdx.x; tile * TILE_M < n && ok; tile += gridDim.x) {
         const int row = tile * TILE_M + t;
-        // layer 1 operand: this thread's 16 features
-        for (int k = 0; k < NIN; ++k) {
-            __nv_bfloat16 x = row < n ? X[(size_t)row * NIN + k] : __float2bfloat16(0.f);
-            S.A[core_off(t, k, NIN) / 2] = x;
+        // layer 1 operand: this thread's 16 features (32 bytes of its row: two 16-byte words, each the k-contiguous
+        // run of one core matrix row)
+        {
+            uint4 x0 = make_uint4(0, 0, 0, 0), x1 = x0;
+            if (row < n) {
+                const uint4* xr = reinterpret_cast<const uint4*>(X + (size_t)row * NIN);
+                x0 = __ldg(xr);
+                x1 = __ldg(xr + 1);
+            }
+            *reinterpret_cast<uint4*>(reinterpret_cast<char*>(S.A) + core_off(t, 0, NIN)) = x0;
+            *reinterpret_cast<uint4*>(reinterpret_cast<char*>(S.A) + core_off(t, 8, NIN)) = x1;
         }
         for (int layer = 0; layer < 3 && ok; ++layer) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -271,9 +301,11 @@ __global__ void __launch_bounds__(128) mlp_infer_tc(const __nv_bfloat16* __restr
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             tmem_ld64(taddr, h);
             const float* b = layer == 0 ? S.b1 : (layer == 1 ? S.b2 : S.b3);
-            for (int q = 0; q < NH; ++q) h[q] = gelu(h[q] + b[q]);
+            for (int q = 0; q < NH; ++q) h[q] = gelu_fast(h[q] + b[q]);
             if (layer < 2)
-                for (int q = 0; q < NH; ++q) S.A[core_off(t, q, NH) / 2] = __float2bfloat16(h[q]);
+                for (int g = 0; g < NH / 8; ++g)
+                    *reinterpret_cast<uint4*>(reinterpret_cast<char*>(S.A) + core_off(t, 8 * g, NH)) =
+                        pack8_bf16(&h[8 * g]);
         }
         if (ok && row < n) {
             float y = S.b4;
@@ -452,6 +484,16 @@ __global__ void screen_decide(int n, const int* __restrict__ nDev, const float* 
 
 size_t infer_smem() { return sizeof(InferSmem) + 128; }
 
+// resident CTAs per SM for the persistent grid (registers and shared memory decide; each CTA holds 64 of the 512
+// tensor-memory columns, so at most 8)
+int infer_ctas_per_sm(int dev)
+{
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, mlp_infer_tc, 128, infer_smem()) != cudaSuccess) bps = 4;
+    (void)dev;
+    return std::max(1, std::min(bps, 8));
+}
+
 // devices on which mlp_infer_tc's dynamic shared-memory limit has been raised
 std::atomic<unsigned long long> g_inferSmemSet{0};
 
@@ -469,8 +511,8 @@ void cssg_launch_screen(const SysDesc* sys, const int* sysOf, int maxPairs, cons
     screen_features<<<(maxPairs + 127) / 128, 128, 0, s>>>(sys, sysOf, maxPairs, nPairsDev, pi, pj, face, pos,
                                                             (__nv_bfloat16*)X, chord);
     int tiles = (maxPairs + TILE_M - 1) / TILE_M;
-    mlp_infer_tc<<<std::min(tiles, sms * 4), 128, infer_smem(), s>>>((const __nv_bfloat16*)X, maxPairs, nPairsDev,
-                                                                      params, yhat, errFlag);
+    mlp_infer_tc<<<std::min(tiles, sms * infer_ctas_per_sm(dev)), 128, infer_smem(), s>>>(
+        (const __nv_bfloat16*)X, maxPairs, nPairsDev, params, yhat, errFlag);
     screen_decide<<<(maxPairs + 255) / 256, 256, 0, s>>>(maxPairs, nPairsDev, chord, yhat, margin, skip, disable);
 }
 
@@ -510,6 +552,10 @@ extern "C" int cssg_mlp_infer(cssg_ctx* ctx, const void* X_bf16, int n, const fl
         cssg_set_error("cssg_mlp_infer: bad arguments");
         return CSSG_ERR_ARG;
     }
+    if (reinterpret_cast<uintptr_t>(X_bf16) % 16 != 0) {  // rows are read as 16-byte words
+        cssg_set_error("cssg_mlp_infer: X must be 16-byte aligned");
+        return CSSG_ERR_ARG;
+    }
     if (n == 0) return CSSG_OK;
     DeviceScope scope(ctx->device);
     CSSG_CUDA(scope.err);
@@ -518,7 +564,7 @@ extern "C" int cssg_mlp_infer(cssg_ctx* ctx, const void* X_bf16, int n, const fl
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     int tiles = (n + TILE_M - 1) / TILE_M;
-    int blocks = std::min(tiles, sms * 4);
+    int blocks = std::min(tiles, sms * infer_ctas_per_sm(ctx->device));
     mlp_infer_tc<<<blocks, 128, smem, ctx->stream>>>((const __nv_bfloat16*)X_bf16, n, nullptr, params, y, err_flag);
     CSSG_CUDA(cudaGetLastError());
     return CSSG_OK;

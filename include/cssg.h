@@ -314,8 +314,9 @@ int cssg_mlp_param_count(void);
  * and |chord| / sigma (nullable).  face[], pos[3*] are the particles' faces and R3 positions. */
 int cssg_screen_features(cssg_ctx* ctx, const cssg_mesh* mesh, double sigma, int nPairs, const int* pi, const int* pj,
                          const int* face, const double* pos, void* X_bf16, float* chord_over_sigma);
-/* Inference on the tensor cores (tcgen05, BF16 operands, FP32 accumulation in tensor memory): y[n].  err_flag
- * (nullable, device int) is set to 1 if a tensor-core completion wait timed out. */
+/* Inference on the tensor cores (tcgen05, BF16 operands, FP32 accumulation in tensor memory): y[n].  X_bf16 must be
+ * 16-byte aligned (rows are read as 16-byte words; else CSSG_ERR_ARG).  err_flag (nullable, device int) is set to 1
+ * if a tensor-core completion wait timed out. */
 int cssg_mlp_infer(cssg_ctx* ctx, const void* X_bf16, int n, const float* params, float* y, int* err_flag);
 /* Gradient of 0.5 sum_p (f(x_p) - y_p)^2 with respect to params (FP32 forward/backward with the BF16 roundings of
  * inference): grad[cssg_mlp_param_count()] is overwritten; loss (nullable) receives the sum. */
