@@ -44,7 +44,7 @@ BYTES_PER_FACE = 12 + 12 + 72         # patch face: vertex ids, neighbours, edge
 # (profiles/geodesic_kernel_torus200x100_N2000_nvt.txt, geodesic_kernel_bumpy_sphere7_N20000_screen.txt and
 # lane_kernel_noisy_torus1000x500_N100000_nvt.txt, each with the pass the autotuner picks there); workloads without a
 # capture report null
-TRAFFIC_BYTES = {"torus200x100_N2000_nvt_patch": 47_415_808 + 112_837_888,
+TRAFFIC_BYTES = {"torus200x100_N2000_nvt_patch": 50_715_648 + 116_845_824,
                  "bumpy_sphere7_N20000_nve_patch_screen": 98_510_592 + 43_534_336,
                  "noisy_torus1000x500_N100000_nvt_patch": 7_921_458 + 976_500_992}
 

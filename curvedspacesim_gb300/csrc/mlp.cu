@@ -484,14 +484,19 @@ __global__ void screen_decide(int n, const int* __restrict__ nDev, const float* 
 
 size_t infer_smem() { return sizeof(InferSmem) + 128; }
 
-// resident CTAs per SM for the persistent grid (registers and shared memory decide; each CTA holds 64 of the 512
-// tensor-memory columns, so at most 8)
+// resident CTAs per SM for the persistent grid, from the kernel's registers and the SM's shared memory (each CTA
+// also holds 64 of the 512 tensor-memory columns, so at most 8)
 int infer_ctas_per_sm(int dev)
 {
-    int bps = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, mlp_infer_tc, 128, infer_smem()) != cudaSuccess) bps = 4;
-    (void)dev;
-    return std::max(1, std::min(bps, 8));
+    cudaFuncAttributes fa;
+    int smemSM = 0, regsSM = 0;
+    if (cudaFuncGetAttributes(&fa, mlp_infer_tc) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&regsSM, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess)
+        return 4;
+    const int byRegs = regsSM / std::max(1, fa.numRegs * 128);
+    const int bySmem = (int)(smemSM / (infer_smem() + fa.sharedSizeBytes + 1024));  // 1 KB reserved per CTA
+    return std::max(1, std::min(std::min(byRegs, bySmem), 8));
 }
 
 // devices on which mlp_infer_tc's dynamic shared-memory limit has been raised
@@ -508,6 +513,7 @@ void cssg_launch_screen(const SysDesc* sys, const int* sysOf, int maxPairs, cons
     int dev = 0;
     cudaGetDevice(&dev);
     cssg_raise_smem_once(g_inferSmemSet, mlp_infer_tc, (int)infer_smem(), dev);
+    cudaFuncSetAttribute(mlp_infer_tc, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     screen_features<<<(maxPairs + 127) / 128, 128, 0, s>>>(sys, sysOf, maxPairs, nPairsDev, pi, pj, face, pos,
                                                             (__nv_bfloat16*)X, chord);
     int tiles = (maxPairs + TILE_M - 1) / TILE_M;
@@ -561,6 +567,7 @@ extern "C" int cssg_mlp_infer(cssg_ctx* ctx, const void* X_bf16, int n, const fl
     CSSG_CUDA(scope.err);
     size_t smem = infer_smem();
     CSSG_CUDA(cssg_raise_smem_once(g_inferSmemSet, mlp_infer_tc, (int)smem, ctx->device));
+    CSSG_CUDA(cudaFuncSetAttribute(mlp_infer_tc, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     int tiles = (n + TILE_M - 1) / TILE_M;
