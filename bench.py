@@ -336,7 +336,8 @@ def run_ours(args, cfg):
         _apply_tuning(S, args.tuning)
         d, w, m, cap, lpt, g, wide = _parse_tuning(args.tuning)
         tune = {"delta_scale": d, "warps_per_block": w, "mid_slots": m, "warps_per_sm": cap, "lpt_order": lpt,
-                "warps_per_source": g, "wide_registers": wide, "lanes_per_warp": S.lanes(), "lane_split": S.lane_split(), "source": "--tuning"}
+                "warps_per_source": g, "wide_registers": wide, "lanes_per_warp": S.lanes(), "lane_split": S.lane_split(),
+                "pass_groups": list(S.pass_groups()), "source": "--tuning"}
         S.step(1, graph=not args.profile)
         torch.cuda.synchronize()
     elif not args.no_autotune:
@@ -721,9 +722,10 @@ def run_screen(args, cfg):
 
 
 def _parse_tuning(text):
-    """delta_scale,warps_per_block,mid_slots,warps_per_sm,lpt[,warps_per_source[,wide_registers[,lanes[,split]]]]: the
-    first seven are System.set_tuning's arguments, the eighth System.set_lanes' (0: source groups), the ninth
-    System.set_lane_split's (the costliest sources that the group pass takes before the lane pass)."""
+    """delta_scale,warps_per_block,mid_slots,warps_per_sm,lpt[,warps_per_source[,wide_registers[,lanes[,split[,medium,
+    large]]]]]: the first seven are System.set_tuning's arguments, the eighth System.set_lanes' (0: source groups), the
+    ninth System.set_lane_split's (the costliest sources that the group pass takes before the lane pass), the last two
+    System.set_pass_groups' (warps per source of the medium and large passes)."""
     fields = text.split(",")
     d, w, m, cap, lpt = fields[:5]
     g = int(fields[5]) if len(fields) > 5 else 1
@@ -736,6 +738,7 @@ def _apply_tuning(S, text):
     fields = text.split(",")
     S.set_lanes(int(fields[7]) if len(fields) > 7 else 0)
     S.set_lane_split(int(fields[8]) if len(fields) > 8 else 0)
+    S.set_pass_groups(int(fields[9]) if len(fields) > 9 else 0, int(fields[10]) if len(fields) > 10 else 0)
 
 
 def run_mlp(args, cfg):
@@ -861,7 +864,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tuning (band width 1, 8 warps)")
     ap.add_argument("--tuning", default="",
                     help="explicit tuning instead of the autotuner: delta_scale,warps_per_block,mid_slots,"
-                         "warps_per_sm,lpt[,warps_per_source[,wide_registers[,lanes_per_warp[,lane_split]]]] "
+                         "warps_per_sm,lpt[,warps_per_source[,wide_registers[,lanes_per_warp[,lane_split[,medium,"
+                         "large]]]]] "
                          "(e.g. 4,8,0,0,1,2,0 or 2,8,0,0,0,1,1,32)")
     ap.add_argument("--profile", action="store_true",
                     help="minimal run for ncu: warm-up steps, then one step without graph replay, no other legs")

@@ -29,7 +29,8 @@ EXPORTS = [
     "cssg_mesh_set_boundary", "cssg_diag_reciprocal", "cssg_system_step_host",
     "cssg_system_gradient_descent", "cssg_system_set_screen_audit", "cssg_system_screen_audit_status",
     "cssg_system_set_work_caps", "cssg_system_set_lanes", "cssg_system_lanes", "cssg_diag_flops_per_window",
-    "cssg_system_set_lane_split", "cssg_system_lane_split", "cssg_system_source_costs",
+    "cssg_system_set_lane_split", "cssg_system_lane_split", "cssg_system_source_costs", "cssg_system_set_pass_groups",
+    "cssg_system_pass_groups",
 ]
 
 
@@ -136,6 +137,8 @@ def load(build_if_missing: bool = True):
     L.cssg_system_set_lane_split.argtypes = [P, I]
     L.cssg_system_lane_split.argtypes = [P, P]
     L.cssg_system_source_costs.argtypes = [P, I, P]
+    L.cssg_system_set_pass_groups.argtypes = [P, I, I]
+    L.cssg_system_pass_groups.argtypes = [P, P, P]
     L.cssg_system_screen_audit_status.argtypes = [P, P]
     L.cssg_screen_features.argtypes = [P, P, D, I, P, P, P, P, P, P]
     L.cssg_mlp_infer.argtypes = [P, P, I, P, P, P]

@@ -409,6 +409,16 @@ class System:
         check(_lib.load().cssg_system_lane_split(self.h, ctypes.byref(out)), "cssg_system_lane_split")
         return out.value
 
+    def set_pass_groups(self, medium_warps: int = 0, large_warps: int = 0):
+        """Warps per source of the medium and large passes (0: the regular pass's; cssg_system_set_pass_groups)."""
+        check(_lib.load().cssg_system_set_pass_groups(self.h, int(medium_warps), int(large_warps)),
+              "cssg_system_set_pass_groups")
+
+    def pass_groups(self):
+        a, b = ctypes.c_int(), ctypes.c_int()
+        check(_lib.load().cssg_system_pass_groups(self.h, ctypes.byref(a), ctypes.byref(b)), "cssg_system_pass_groups")
+        return a.value, b.value
+
     def source_costs(self):
         """Work of each source in the last force evaluation (cssg_system_source_costs)."""
         out = np.zeros(self.n, dtype=np.int32)
@@ -453,7 +463,7 @@ class System:
                 "warps_per_sm": int(out[3]), "lpt_order": bool(out[4]), "ms_per_force_pass": float(out[5]),
                 "warps_per_source": int(out[6]), "wide_registers": bool(int(out[7]) & 1),
                 "outlined_probes": bool(int(out[7]) & 2), "lanes_per_warp": self.lanes(),
-                "lane_split": self.lane_split()}
+                "lane_split": self.lane_split(), "pass_groups": list(self.pass_groups())}
 
     def fire(self, maximum_iterations=1000, alpha_start=0.99, dt_max=0.1, dt_min=1e-5, dt_inc=1.1, dt_dec=0.95,
              alpha_dec=0.9, n_min=4, force_cutoff=1e-12, alpha_min=0.0, reset=False):

@@ -336,6 +336,7 @@ struct cssg_system {
     // capacities, scratch of nLaneWarps warps
     int laneLanes = 0;
     int laneSplit = 0;  // with the lane pass: the costliest sources (by the last evaluation) that the group pass takes
+    int tuneMidGroup = 0, tuneBigGroup = 0;  // warps per source of the medium and large passes (0: the regular pass's)
     LaneCaps laneCaps{};
     void* laneScratch = nullptr;
     int nLaneWarps = 0;
@@ -676,6 +677,7 @@ void launch_forces_ex(cssg_system* s, bool kick, bool useScreen, double* forceOu
     R.warpsPerSM = 0;
     R.maxRounds = 1 << 15;
     R.maxWindows = s->midMaxWindows;
+    if (s->tuneMidGroup) R.groupWarps = s->tuneMidGroup;
     cssg_launch_geodesic(R, st);
     // large pass: medium-pass overflows
     GeoLaunch B = R;
@@ -689,6 +691,7 @@ void launch_forces_ex(cssg_system* s, bool kick, bool useScreen, double* forceOu
     B.failList = nullptr;
     B.failCount = nullptr;
     B.maxWindows = s->bigMaxWindows;
+    B.groupWarps = s->tuneBigGroup ? s->tuneBigGroup : L.groupWarps;
     cssg_launch_geodesic(B, st);
     record(s);
 }
@@ -1290,7 +1293,8 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     int prior = 0;
     CSSG_CUDA(cudaMemcpyAsync(&prior, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost, st));
     CSSG_CUDA(cudaStreamSynchronize(st));
-    s->laneLanes = 0;  // the source-group candidates first
+    s->laneLanes = 0;  // the source-group candidates first, every pass with the same group size
+    s->tuneMidGroup = s->tuneBigGroup = 0;
     for (double d : deltas)
         for (const auto& sh : shapes)
             for (int m : mids) {
@@ -1330,6 +1334,7 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     // the one-source-per-lane pass (16 or 32 sources per warp, cell or longest-first order); the group tuning found
     // above still serves the sources it hands to the medium and large passes
     int bLanes = 0, bSplit = 0;
+    const bool blGroup = bl;  // the source groups' order choice, kept if the lane pass is not taken
     if (s->useCells) {
         s->tuneDelta = bd;
         s->tuneWpb = bw;
@@ -1371,9 +1376,99 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
                         bl = lpt != 0;
                     }
                 }
+        if (bLanes > 0) {
+            // confirm the lane pass on a steadier state (its time depends more on the state: the split follows the
+            // last evaluation's costs, a warp waits for its slowest source): more evaluations of each, then the same
+            // 5% margin against the best source-group configuration
+            auto steady = [&](int warm, float* ms) -> cudaError_t {
+                for (int r = 0; r < warm; ++r) launch_forces(s);
+                cudaEventRecord(e0, st);
+                for (int r = 0; r < reps; ++r) launch_forces(s);
+                cudaEventRecord(e1, st);
+                cudaError_t err = cudaEventSynchronize(e1);
+                if (err == cudaSuccess) err = cudaEventElapsedTime(ms, e0, e1);
+                int bits = 0;
+                cudaMemcpy(&bits, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost);
+                cudaMemset(s->statusBits, 0, sizeof(int));
+                if (bits) *ms = 1e30f;
+                return err;
+            };
+            float lms = 0, gms = 0;
+            set_lanes(s, bLanes);
+            s->laneSplit = bSplit;
+            s->tuneLpt = bl;
+            cudaError_t err = steady(4, &lms);
+            s->laneLanes = 0;
+            s->laneSplit = 0;
+            s->tuneLpt = blGroup;
+            if (err == cudaSuccess) err = steady(4, &gms);
+            if (err != cudaSuccess) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return cssg_cuda_fail(err, "cssg_system_autotune");
+            }
+            if (lms < 0.95f * gms) {
+                best = lms;
+            } else {
+                best = gms;
+                bLanes = 0;
+                bSplit = 0;
+                bl = blGroup;
+            }
+        }
         set_lanes(s, bLanes);
         s->laneSplit = bSplit;
+        s->tuneLpt = bl;
     }
+    // the medium and large passes take the largest sources: try 8-warp groups there (a few huge patches are the
+    // tail of a force pass)
+    s->tuneDelta = bd;
+    s->tuneWpb = bw;
+    s->tuneWarpsPerSM = bc;
+    s->tuneLpt = bl;
+    s->tuneGroup = bg;
+    s->tuneWide = bx;
+    s->nMidSlots = bm;
+    int bMid = 0, bBig = 0;
+    {
+        // (regular, medium, large) warps per source; smaller regular groups pay off once the large sources have
+        // their own 8-warp groups
+        const int passGroups[][3] = {{bg, 0, 0}, {bg, 8, 0}, {bg, 8, 8}, {2, 8, 8}, {1, 8, 8}};
+        bool first = true;
+        for (int c = 0; c < 5; ++c) {
+            const int* pg = passGroups[c];
+            if ((c == 1 || c == 2) && bg == 8) continue;  // 8-warp passes are the regular pass's own groups
+            if (c >= 3 && pg[0] >= bg) continue;          // only smaller regular groups than the chosen one
+            s->tuneGroup = pg[0];
+            s->tuneMidGroup = pg[1];
+            s->tuneBigGroup = pg[2];
+            launch_forces(s);
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < reps; ++r) launch_forces(s);
+            cudaEventRecord(e1, st);
+            cudaError_t err = cudaEventSynchronize(e1);
+            if (err != cudaSuccess) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return cssg_cuda_fail(err, "cssg_system_autotune");
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            int bits = 0;
+            cudaMemcpy(&bits, s->statusBits, sizeof(int), cudaMemcpyDeviceToHost);
+            cudaMemset(s->statusBits, 0, sizeof(int));
+            // the first candidate re-times the configuration chosen above (the reference for the others)
+            if (bits == 0 && (first || ms < best)) {
+                best = ms;
+                bg = pg[0];
+                bMid = pg[1];
+                bBig = pg[2];
+            }
+            first = false;
+        }
+    }
+    s->tuneMidGroup = bMid;
+    s->tuneBigGroup = bBig;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     s->timing = timing;
@@ -1592,6 +1687,24 @@ extern "C" int cssg_system_lane_split(cssg_system* s, int* group_sources)
 {
     if (!s || !group_sources) return cssg_bad_args("cssg_system_lane_split");
     *group_sources = s->laneSplit;
+    return CSSG_OK;
+}
+
+extern "C" int cssg_system_set_pass_groups(cssg_system* s, int medium_warps, int large_warps)
+{
+    auto ok = [](int g) { return g == 0 || g == 1 || g == 2 || g == 4 || g == 8; };
+    if (!s || !ok(medium_warps) || !ok(large_warps)) return cssg_bad_args("cssg_system_set_pass_groups");
+    s->tuneMidGroup = medium_warps;
+    s->tuneBigGroup = large_warps;
+    drop_graph(s);
+    return CSSG_OK;
+}
+
+extern "C" int cssg_system_pass_groups(cssg_system* s, int* medium_warps, int* large_warps)
+{
+    if (!s || !medium_warps || !large_warps) return cssg_bad_args("cssg_system_pass_groups");
+    *medium_warps = s->tuneMidGroup;
+    *large_warps = s->tuneBigGroup;
     return CSSG_OK;
 }
 

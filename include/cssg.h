@@ -218,12 +218,14 @@ int cssg_system_set_tuning(cssg_system* sys, double delta_scale, int warps_per_b
 /* Autotuner: times `reps` force evaluations on the current state for each candidate (delta_scale in {0.5, 1, 2, 4}
  * x (warps_per_block, warps_per_sm, lpt_order, warps_per_source, wide_registers) in {(8,0,0,1,0), (4,0,0,1,0),
  * (8,0,1,1,0), (8,8,1,1,0), (8,4,1,1,0), (8,0,1,2,0), (8,0,1,4,0), (8,0,1,8,0), (8,0,1,1,1), (8,0,1,2,1),
- * (8,0,1,4,1), (8,0,1,1,3), (8,0,1,1,2), (8,0,1,2,3)} x medium slots in {allocated, 8 per SM}), then, on cell-list systems, the
- * one-source-per-lane pass (cssg_system_set_lanes) with 16 and 32 lanes x lpt_order in {0, 1} x the splits of
- * cssg_system_set_lane_split; rejects candidates that overflow a table, keeps the fastest (a lane-pass candidate only
- * when it beats the best source-group one by 5%) and recomputes the forces with it.  result_host (nullable, 8 doubles) = {delta_scale, warps_per_block, mid_slots, warps_per_sm, lpt_order,
- * ms per force evaluation, warps_per_source, wide_registers}; the chosen lane
- * width and split are read with cssg_system_lanes and cssg_system_lane_split.  Synchronises the context's stream. */
+ * (8,0,1,4,1), (8,0,1,1,3), (8,0,1,1,2), (8,0,1,2,3)} x medium slots in {allocated, 8 per SM}), then, on cell-list
+ * systems, the one-source-per-lane pass (cssg_system_set_lanes) with 16 and 32 lanes x lpt_order in {0, 1} x the
+ * splits of cssg_system_set_lane_split, then the medium and large passes' group sizes (cssg_system_set_pass_groups);
+ * rejects candidates that overflow a table, keeps the fastest (a lane-pass candidate only when it beats the best
+ * source-group one by 5%) and recomputes the forces with it.  result_host (nullable, 8 doubles) = {delta_scale,
+ * warps_per_block, mid_slots, warps_per_sm, lpt_order, ms per force evaluation, warps_per_source, wide_registers};
+ * the chosen lane width, split and pass group sizes are read with cssg_system_lanes, cssg_system_lane_split and
+ * cssg_system_pass_groups.  Synchronises the context's stream. */
 int cssg_system_autotune(cssg_system* sys, int reps, double* result_host);
 /* The reference throws at the first failing walk or geodesic (ERRORERROR, inc/debuggingHelp.h:19-31); here failures
  * are collected. Error summary since the last call (synchronises): OR of (1 << CSSG_ST_*) over walks and sources,
@@ -266,6 +268,12 @@ int cssg_system_lanes(cssg_system* sys, int* lanes_per_warp);
  * source.  Results are the same either way.  cssg_system_autotune tries 0 and 1/64, 1/16 and 1/4 of the sources.
  * Drops the captured step graph. */
 int cssg_system_set_lane_split(cssg_system* sys, int group_sources);
+/* No reference counterpart.  Warps per source of the medium and large propagation passes (the sources whose tables
+ * or caps overflow the regular pass: the largest patches), 1, 2, 4 or 8; 0 = the regular pass's warps_per_source.
+ * A few huge patches are often the tail of a force evaluation, and more warps per source shorten it.  The autotuner
+ * tries (0, 0), (8, 0) and (8, 8) after choosing the rest.  Results do not depend on it.  Drops the step graph. */
+int cssg_system_set_pass_groups(cssg_system* sys, int medium_warps, int large_warps);
+int cssg_system_pass_groups(cssg_system* sys, int* medium_warps, int* large_warps);
 int cssg_system_lane_split(cssg_system* sys, int* group_sources);
 /* No reference counterpart (diagnostics).  Work of each source in the last force evaluation (windows processed +
  * vertex launches + 1, and 8 per round in the group pass): host array of at least the system's particle count. */

@@ -76,8 +76,8 @@ def test_nan_position_reaches_system_check(gpu):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("lanes", [0, 32])
-def test_propagation_caps_escalate_then_report_capacity(gpu, oracle_mod, lanes):
+@pytest.mark.parametrize("lanes,pass_warps", [(0, 0), (32, 0), (0, 8), (32, 2)])
+def test_propagation_caps_escalate_then_report_capacity(gpu, oracle_mod, lanes, pass_warps):
     """Host-forced tiny work caps: sources that exceed the regular pass's cap are redone by the medium (then large)
     pass with the same results; when every pass's cap is exceeded they report CSSG_ST_CAPACITY."""
     api, ctx = gpu
@@ -90,6 +90,7 @@ def test_propagation_caps_escalate_then_report_capacity(gpu, oracle_mod, lanes):
                         max_dist=sigma, cutoff=sigma, dt=1e-3)
     S = api.System(ctx, M, n, p)
     S.set_lanes(lanes)
+    S.set_pass_groups(pass_warps, pass_warps)  # group size of the medium and large passes (0: the regular one's)
     S.set_state(f, b, np.zeros((n, 3)), np.zeros((n, 3)))
     S.compute_forces()
     assert S.check()[0] == 0

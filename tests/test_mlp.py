@@ -58,6 +58,31 @@ def test_tensor_core_inference_matches_reference():
 
 
 @pytest.mark.gpu
+def test_inference_rejects_misaligned_rows_and_covers_many_tiles():
+    """Rows are read as 16-byte words: a feature array that does not start on a 16-byte boundary is an argument
+    error (no launch); a batch of many tiles on the persistent grid (more tiles than resident CTAs, a ragged last
+    tile) still matches the reference."""
+    import torch
+    from curvedspacesim_gb300 import _lib, api
+    ctx = api.Context(0)
+    p = R.init_params(7)
+    pt = torch.tensor(p, dtype=torch.float32, device="cuda")
+    X, _ = _data(200_003, 8)
+    Xt = torch.tensor(R.bf16(X), dtype=torch.bfloat16, device="cuda")
+    flat = torch.zeros(Xt.numel() + 8, dtype=torch.bfloat16, device="cuda")
+    shifted = flat[4:4 + Xt.numel()].view(-1, 16)  # 8 bytes past an aligned base
+    shifted.copy_(Xt)
+    with pytest.raises(_lib.CssgError, match="16-byte aligned"):
+        api.mlp_infer(ctx, shifted, pt)
+    y = api.mlp_infer(ctx, Xt, pt).cpu().numpy()
+    yr, _ = R.forward(X, p.astype(np.float32).astype(np.float64))
+    err = np.abs(y - yr)
+    scale = np.abs(yr).mean() + 1e-3
+    assert np.quantile(err, 0.995) < 2e-3 * scale + 1e-5, np.quantile(err, 0.995)
+    assert err.max() < 5e-2 * scale + 1e-4, err.max()
+
+
+@pytest.mark.gpu
 def test_training_gradient_matches_reference():
     import torch
     from curvedspacesim_gb300 import api
