@@ -173,6 +173,8 @@ def test_pair_sets_identical(gpu, oracle_mod, lanes, split):
     S.enable_pairs()
     S.compute_forces()
     i, j, d, t = S.pairs()
+    cost = S.source_costs()  # windows + launches (+ rounds in the group pass) of each source: every source did work
+    assert cost.shape == (n,) and (cost >= 1).all() and cost.max() > 10
     OM = oracle_mod.OracleMesh(V, F)
     off, idx, mc = OM.candidates(f, b, sigma)
     do, tso, _ = OM.neighbor_distances(f, b, off, idx, mc, 1, sigma, sigma)
