@@ -215,6 +215,7 @@ struct GeoLaunch {
     int groupWarps;              // warps that solve one source together: 1 (default), 2, 4 or 8
     int wideRegs;                // 1: the kernel build with up to 255 registers per thread (fewer warps per SM)
     int hashOutline;             // 1: the kernel build with out-of-line hash-table probes (geodesic_outlined.cu)
+    int patchSystems;            // 1: every system takes reference patches and cell-list or screened candidates
     int* srcCost;                // nullable: work of each source (windows + launches + rounds), for the next order
     int smemTables;              // set by cssg_launch_geodesic: hash tables in shared memory
     int device;                  // the CUDA device the launch runs on (SM count, occupancy, attributes)

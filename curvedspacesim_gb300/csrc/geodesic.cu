@@ -627,7 +627,9 @@ __device__ __noinline__ bool settled(const DevMesh& M, const Slot& S, const GeoC
 }
 
 // The per-source solve (one source group).  Leaves results in the slot and the outputs.
-template <int G>
+// MODE 1: every system takes reference patches with cell-list (search mode 1) or screened-CSR (3) candidates, so the
+// code of the other modes is compiled out (a smaller kernel); MODE 0 reads the mode of each system.
+template <int G, int MODE>
 __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, const Grp<G>& gp,
                              unsigned long long* cnt)
 {
@@ -637,6 +639,8 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     const GeoCaps& C = Lp.caps;
     const SysDesc& D = Lp.sys[Lp.sysOf ? Lp.sysOf[si] : 0];
     const DevMesh& M = D.mesh;
+    const int searchMode = MODE == 1 ? (D.searchMode == 3 ? 3 : 1) : D.searchMode;
+    const bool submesh = MODE == 1 ? true : D.submesh != 0;
     if (D.bigBin && Lp.routeBig && Lp.failList) {
         // binned to the large-table pass
         if (t0 == 0) {
@@ -660,7 +664,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             if (Lp.inRangeOut) Lp.inRangeOut[si] = 0;
             if (Lp.srcCost) Lp.srcCost[si] = 1;
         }
-        if (D.searchMode == 0)
+        if (searchMode == 0)
             for (int o = Lp.candOff[si] + t0; o < Lp.candOff[si + 1]; o += Grp<G>::NT) {
                 Lp.dOut[o] = CUDART_INF;
                 for (int c = 0; c < 3; ++c) {
@@ -680,14 +684,14 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     gp.sync();
     // ---- targets ---------------------------------------------------------------------------------------------
     double maxChord2 = 0;
-    if (D.searchMode == 0 || D.searchMode == 3) {
+    if (searchMode == 0 || searchMode == 3) {
         int beg = Lp.candOff[si], nT = Lp.candOff[si + 1] - beg;
         if (nT > C.CT) {
             if (t0 == 0) ctl->err = CSSG_ST_CAPACITY;
             nT = 0;
         }
         for (int t = t0; t < nT; t += NT) {
-            if (D.searchMode == 0) {
+            if (searchMode == 0) {
                 S.tface[t] = Lp.candFace[beg + t];
                 S.tidx[t] = beg + t;
                 for (int c = 0; c < 3; ++c) S.tb[3 * t + c] = Lp.candBary[3 * (beg + t) + c];
@@ -700,7 +704,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             }
         }
         if (t0 == 0) ctl->nT = nT;
-        if (D.searchMode == 3 && Lp.pairCount && t0 == 0) Lp.pairCount[si] = nT;
+        if (searchMode == 3 && Lp.pairCount && t0 == 0) Lp.pairCount[si] = nT;
     } else if (gp.wig == 0) {
         // candidates j != i with chord^2 < range2 (cell list: 27 cells in (x, y, z) loop order; or all particles);
         // the first warp of the group searches, in the reference's order
@@ -713,7 +717,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
                 const double* Pj = &Lp.partPos[3 * jj];
                 double dx = Pi[0] - Pj[0], dy = Pi[1] - Pj[1], dz = Pi[2] - Pj[2];
                 d2 = dx * dx + dy * dy + dz * dz;
-                take = (D.searchMode == 2) || (d2 < D.range2);
+                take = (searchMode == 2) || (d2 < D.range2);
             }
             unsigned m = __ballot_sync(FULL, take);
             if (take) {
@@ -727,7 +731,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             }
             count += __popc(m);
         };
-        if (D.searchMode == 2) {
+        if (searchMode == 2) {
             for (int base = 0; base < D.nPart; base += 32) consider(D.partBase + base + lane, base + lane < D.nPart);
         } else {
             int ci[3];
@@ -786,16 +790,16 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     }
     gp.sync();
     // ---- domain: whole mesh or the reference patch ---------------------------------------------------------------
-    src.full = !D.submesh;
+    src.full = !submesh;
     double r = D.maxDist;
-    if (D.searchMode == 0 || D.searchMode == 3) {
+    if (searchMode == 0 || searchMode == 3) {
         if (Lp.threshold && Lp.threshold[si] < r) r = Lp.threshold[si];
     } else {
         double mc = sqrt(maxChord2);
-        if (D.searchMode == 2) mc = 1e20;
+        if (searchMode == 2) mc = 1e20;
         if (mc < r) r = mc;
     }
-    if (D.submesh) {
+    if (submesh) {
         int fresh;
         bool notInF0 = false, notInSeeds = false;
         int nb[3];
@@ -1180,7 +1184,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
     }
     double fx = 0, fy = 0, fz = 0;
     int inRange = 0;
-    const bool wantTe = D.searchMode == 0 && Lp.teOut;
+    const bool wantTe = searchMode == 0 && Lp.teOut;
     for (int t = t0; t < nT; t += NT) {
         double ts[3], te[3] = {0, 0, 0};
         const bool screened = S.tidx[t] < 0;
@@ -1190,7 +1194,7 @@ __device__ void solve_source(const GeoLaunch& Lp, Slot S, WarpCtl* ctl, int si, 
             d = CUDART_INF;
             ts[0] = ts[1] = ts[2] = te[0] = te[1] = te[2] = 0;
         }
-        if (D.searchMode == 0) {
+        if (searchMode == 0) {
             int o = S.tidx[t];
             if (!(d < CUDART_INF) && Lp.patchDisconnected) {
                 d = 2.0 * D.maxDist;
@@ -1303,7 +1307,7 @@ __device__ void reset_slot(const Slot& S, const GeoCaps& C, WarpCtl* ctl, const 
 // One source group (G warps) per slot; groups pull sources from the work counter until none are left.
 // MINB = 2 lets ptxas use up to 128 registers per thread (two full blocks per SM); MINB = 1 up to 255 (no spills,
 // at most 8 warps per SM).  The autotuner picks.
-template <int G, int MINB>
+template <int G, int MINB, int MODE>
 __global__ void __launch_bounds__(256, MINB) geodesic_kernel(GeoLaunch L)
 {
     constexpr int NT = 32 * G;
@@ -1350,7 +1354,7 @@ __global__ void __launch_bounds__(256, MINB) geodesic_kernel(GeoLaunch L)
         if (L.itemCountDev) nItems = min(nItems, *(volatile const int*)L.itemCountDev);
         if (item >= nItems) break;
         int si = L.order ? L.order[item] : item;
-        solve_source<G>(L, S, ctl, si, gp, cnt);
+        solve_source<G, MODE>(L, S, ctl, si, gp, cnt);
         reset_slot<G>(S, L.caps, ctl, gp);
     }
     if (gp.t == 0 && L.counters) {
@@ -1475,7 +1479,7 @@ size_t cssg_geo_smem_per_warp(const GeoCaps& c) { return smem_per_warp(c); }
 #endif
 
 namespace {
-template <int G, int MINB>
+template <int G, int MINB, int MODE = 0>
 void launch_groups(GeoLaunch L, cudaStream_t s)
 {
     // groups of G warps, each solving one source at a time in its own slot; a block holds gpb groups
@@ -1492,7 +1496,7 @@ void launch_groups(GeoLaunch L, cudaStream_t s)
         static std::atomic<unsigned long long> configured{0};
         // the 48 KB default covers static + dynamic shared memory together, so raise the limit whenever the tables
         // are in shared memory (once per device)
-        cssg_raise_smem_once(configured, geodesic_kernel<G, MINB>, (int)budget, dev);
+        cssg_raise_smem_once(configured, geodesic_kernel<G, MINB, MODE>, (int)budget, dev);
     }
     // spread the groups evenly over the SMs: sources are FP64-pipe bound per SM, so an SM holding two blocks while
     // another holds one would take twice as long.  Full occupancy = sms * bps blocks; fewer slots than that get
@@ -1500,7 +1504,7 @@ void launch_groups(GeoLaunch L, cudaStream_t s)
     int sms = 1, bps = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (L.warpsPerSM > 0) L.nSlots = (int)std::min<long long>(L.nSlots, std::max<long long>(1, (long long)sms * L.warpsPerSM / G));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, geodesic_kernel<G, MINB>, 32 * G * gpb, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, geodesic_kernel<G, MINB, MODE>, 32 * G * gpb, smem);
     bps = std::max(bps, 1);
     const long long full = (long long)sms * bps;
     int blocks;
@@ -1511,7 +1515,7 @@ void launch_groups(GeoLaunch L, cudaStream_t s)
         if (L.smemTables) smem = per * gpb;
         blocks = (int)full;
     }
-    geodesic_kernel<G, MINB><<<blocks, 32 * G * gpb, smem, s>>>(L);
+    geodesic_kernel<G, MINB, MODE><<<blocks, 32 * G * gpb, smem, s>>>(L);
 }
 
 }  // namespace
@@ -1525,6 +1529,18 @@ void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
 #ifndef CSSG_GEO_OUTLINE
     if (L.hashOutline) {
         cssg_launch_geodesic_outlined(L, s);
+        return;
+    }
+#else
+    // the out-of-line-probe build serves small patches: with 1 or 2 warps per source it has a patch-system version
+    if (L.patchSystems && L.groupWarps <= 2) {
+        if (L.wideRegs) {
+            if (L.groupWarps == 2) launch_groups<2, 1, 1>(L, s);
+            else launch_groups<1, 1, 1>(L, s);
+        } else {
+            if (L.groupWarps == 2) launch_groups<2, 2, 1>(L, s);
+            else launch_groups<1, 2, 1>(L, s);
+        }
         return;
     }
 #endif

@@ -337,6 +337,7 @@ struct cssg_system {
     int laneLanes = 0;
     int laneSplit = 0;  // with the lane pass: the costliest sources (by the last evaluation) that the group pass takes
     int tuneMidGroup = 0, tuneBigGroup = 0;  // warps per source of the medium and large passes (0: the regular pass's)
+    bool patchSystems = false;  // every system: reference patches and cell-list candidates (search mode 1 or 3)
     LaneCaps laneCaps{};
     void* laneScratch = nullptr;
     int nLaneWarps = 0;
@@ -595,6 +596,7 @@ void launch_forces_ex(cssg_system* s, bool kick, bool useScreen, double* forceOu
     L.groupWarps = s->tuneGroup;
     L.wideRegs = s->tuneWide & 1;
     L.hashOutline = (s->tuneWide >> 1) & 1;
+    L.patchSystems = s->patchSystems ? 1 : 0;
     L.srcCost = s->srcCost;
     L.device = s->ctx->device;
     // split of the regular pass: the costliest sources go to the source-group pass, the rest to the lane pass (the
@@ -870,6 +872,8 @@ extern "C" int cssg_system_create_batched(cssg_ctx* ctx, int K, const cssg_mesh*
     // per-system descriptors: mesh, interaction parameters, grid (hyperRectangularCellList::setGridSize: cells of
     // size >= range over the origin-including bounding box), particle and cell offsets
     s->useCells = params[0].range > 0;
+    s->patchSystems = s->useCells;
+    for (int k = 0; k < K; ++k) s->patchSystems = s->patchSystems && params[k].submesh != 0;
     long long cellTotal = 0;
     s->hsys.resize(K);
     std::vector<DevMesh> hm(K);
