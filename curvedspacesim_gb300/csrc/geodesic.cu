@@ -1531,8 +1531,8 @@ void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
         cssg_launch_geodesic_outlined(L, s);
         return;
     }
-#else
-    // the out-of-line-probe build serves small patches: with 1 or 2 warps per source it has a patch-system version
+#endif
+    // patch systems with 1 or 2 warps per source: the version with the search mode fixed
     if (L.patchSystems && L.groupWarps <= 2) {
         if (L.wideRegs) {
             if (L.groupWarps == 2) launch_groups<2, 1, 1>(L, s);
@@ -1543,7 +1543,6 @@ void cssg_launch_geodesic(GeoLaunch L, cudaStream_t s)
         }
         return;
     }
-#endif
     if (L.wideRegs) {
         if (L.groupWarps == 8) launch_groups<8, 1>(L, s);
         else if (L.groupWarps == 4) launch_groups<4, 1>(L, s);
