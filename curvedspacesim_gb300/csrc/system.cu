@@ -1339,7 +1339,9 @@ extern "C" int cssg_system_autotune(cssg_system* s, int reps, double* result_hos
     // above still serves the sources it hands to the medium and large passes
     int bLanes = 0, bSplit = 0;
     const bool blGroup = bl;  // the source groups' order choice, kept if the lane pass is not taken
-    if (s->useCells) {
+    // single-system objects only: on the 64-system batch the lane pass with a split timed 28 ms per evaluation here
+    // but 47 ms in the steps that followed (uneven systems whose costs move), while source groups held 32 ms
+    if (s->useCells && s->K == 1) {
         s->tuneDelta = bd;
         s->tuneWpb = bw;
         s->tuneWarpsPerSM = bc;

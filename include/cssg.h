@@ -218,8 +218,8 @@ int cssg_system_set_tuning(cssg_system* sys, double delta_scale, int warps_per_b
 /* Autotuner: times `reps` force evaluations on the current state for each candidate (delta_scale in {0.5, 1, 2, 4}
  * x (warps_per_block, warps_per_sm, lpt_order, warps_per_source, wide_registers) in {(8,0,0,1,0), (4,0,0,1,0),
  * (8,0,1,1,0), (8,8,1,1,0), (8,4,1,1,0), (8,0,1,2,0), (8,0,1,4,0), (8,0,1,8,0), (8,0,1,1,1), (8,0,1,2,1),
- * (8,0,1,4,1), (8,0,1,1,3), (8,0,1,1,2), (8,0,1,2,3)} x medium slots in {allocated, 8 per SM}), then, on cell-list
- * systems, the one-source-per-lane pass (cssg_system_set_lanes) with 16 and 32 lanes x lpt_order in {0, 1} x the
+ * (8,0,1,4,1), (8,0,1,1,3), (8,0,1,1,2), (8,0,1,2,3)} x medium slots in {allocated, 8 per SM}), then, on single
+ * cell-list systems, the one-source-per-lane pass (cssg_system_set_lanes) with 16 and 32 lanes x lpt_order in {0, 1} x the
  * splits of cssg_system_set_lane_split, then the medium and large passes' group sizes (cssg_system_set_pass_groups);
  * rejects candidates that overflow a table, keeps the fastest (a lane-pass candidate only when it beats the best
  * source-group one by 5%) and recomputes the forces with it.  result_host (nullable, 8 doubles) = {delta_scale,
