@@ -45,7 +45,7 @@ BYTES_PER_FACE = 12 + 12 + 72         # patch face: vertex ids, neighbours, edge
 # lane_kernel_noisy_torus1000x500_N100000_nvt.txt, each with the pass the autotuner picks there); workloads without a
 # capture report null
 TRAFFIC_BYTES = {"torus200x100_N2000_nvt_patch": 50_715_648 + 116_845_824,
-                 "bumpy_sphere7_N20000_nve_patch_screen": 98_510_592 + 43_534_336,
+                 "bumpy_sphere7_N20000_nve_patch_screen": 98_532_096 + 43_409_920,
                  "noisy_torus1000x500_N100000_nvt_patch": 7_921_458 + 976_500_992}
 
 
