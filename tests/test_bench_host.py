@@ -62,3 +62,36 @@ def test_clock_sampler_without_nvidia_smi(tmp_path, monkeypatch):
     c.begin()
     c.end()
     assert c.stop() is None
+
+
+def test_tuning_string_maps_to_the_system_calls():
+    """--tuning: the first seven fields go to System.set_tuning, the eighth to set_lanes, the ninth to set_lane_split,
+    the last two to set_pass_groups; missing trailing fields take their defaults."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    class Fake:
+        def __init__(self):
+            self.calls = []
+
+        def set_tuning(self, *a):
+            self.calls.append(("tuning", a))
+
+        def set_lanes(self, k):
+            self.calls.append(("lanes", k))
+
+        def set_lane_split(self, k):
+            self.calls.append(("split", k))
+
+        def set_pass_groups(self, m, b):
+            self.calls.append(("passes", m, b))
+
+    S = Fake()
+    bench._apply_tuning(S, "2,8,0,0,1,1,3,32,1562,8,8")
+    assert S.calls == [("tuning", (2.0, 8, 0, 0, True, 1, 3)), ("lanes", 32), ("split", 1562), ("passes", 8, 8)]
+    S = Fake()
+    bench._apply_tuning(S, "4,8,0,0,0")
+    assert S.calls == [("tuning", (4.0, 8, 0, 0, False, 1, 0)), ("lanes", 0), ("split", 0), ("passes", 0, 0)]
+    # every named workload has a configuration (the sizes the measurements use)
+    for name in ("bumpy_screen", "torus_nvt", "ico_nve", "noisy_torus_nvt", "batch64", "mlp_infer"):
+        assert bench.workload_config(name)
