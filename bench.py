@@ -614,7 +614,9 @@ def run_screen(args, cfg):
     torch.cuda.synchronize()
     sampler.begin()
     ms_plain = _timed_steps(ctx, plain, args.steps, flush, stream)
+    audits0 = scr.screen_audit_status()["audits"] if cfg.get("audit_every") else 0
     ms_scr = _timed_steps(ctx, scr, args.steps, flush, stream)
+    audits_timed = (scr.screen_audit_status()["audits"] - audits0) if cfg.get("audit_every") else 0
     sampler.end()
     clocks = sampler.stop()
     barrier(pg)
@@ -707,7 +709,9 @@ def run_screen(args, cfg):
             "audit_vs_plain": audit_plain,
             "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": io_bytes,
                     "d2h_bytes_per_step": io_bytes},
-            "gpu_launches": scr.kernels_per_step() * args.steps,
+            "gpu_launches": scr.kernels_per_step() * (args.steps - audits_timed)
+                            + scr.kernels_per_audit_step() * audits_timed,
+            "audited_steps": audits_timed,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "GFLOP/s",
                          "frac": achieved / fp64_peak, "traffic": int(traffic) if traffic else None,
                          "kernel": "geodesic (screened path)", "kernel_ms": kt["screened"],

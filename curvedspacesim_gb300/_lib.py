@@ -30,7 +30,7 @@ EXPORTS = [
     "cssg_system_gradient_descent", "cssg_system_set_screen_audit", "cssg_system_screen_audit_status",
     "cssg_system_set_work_caps", "cssg_system_set_lanes", "cssg_system_lanes", "cssg_diag_flops_per_window",
     "cssg_system_set_lane_split", "cssg_system_lane_split", "cssg_system_source_costs", "cssg_system_set_pass_groups",
-    "cssg_system_pass_groups",
+    "cssg_system_pass_groups", "cssg_system_kernels_per_audit_step",
 ]
 
 
@@ -139,6 +139,7 @@ def load(build_if_missing: bool = True):
     L.cssg_system_source_costs.argtypes = [P, I, P]
     L.cssg_system_set_pass_groups.argtypes = [P, I, I]
     L.cssg_system_pass_groups.argtypes = [P, P, P]
+    L.cssg_system_kernels_per_audit_step.argtypes = [P, P]
     L.cssg_system_screen_audit_status.argtypes = [P, P]
     L.cssg_screen_features.argtypes = [P, P, D, I, P, P, P, P, P, P]
     L.cssg_mlp_infer.argtypes = [P, P, I, P, P, P]

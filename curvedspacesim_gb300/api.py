@@ -297,6 +297,12 @@ class System:
     def reset_thermostat(self):
         check(_lib.load().cssg_system_reset_thermostat(self.h), "cssg_system_reset_thermostat")
 
+    def kernels_per_audit_step(self):
+        c = ctypes.c_int()
+        check(_lib.load().cssg_system_kernels_per_audit_step(self.h, ctypes.byref(c)),
+              "cssg_system_kernels_per_audit_step")
+        return c.value
+
     def kernels_per_step(self):
         c = ctypes.c_int()
         check(_lib.load().cssg_system_kernels_per_step(self.h, ctypes.byref(c)), "cssg_system_kernels_per_step")

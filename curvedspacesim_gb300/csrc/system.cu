@@ -1105,6 +1105,24 @@ extern "C" int cssg_system_kernels_per_step(cssg_system* s, int* count)
     return CSSG_OK;
 }
 
+extern "C" int cssg_system_kernels_per_audit_step(cssg_system* s, int* count)
+{
+    if (!s || !count) return cssg_bad_args("cssg_system_kernels_per_audit_step");
+    int base = 0;
+    if (int rc = cssg_system_kernels_per_step(s, &base)) return rc;
+    if (!(s->screen && s->auditEvery > 0)) {
+        *count = base;
+        return CSSG_OK;
+    }
+    // the exact pass on the same positions (no cell list, no screen chain; the lane pass's candidate rows) and the
+    // comparison kernel
+    const int split = s->laneLanes > 0 && s->laneSplit > 0 ? 1 : 0;
+    const int global = s->n <= kLptSmallMax ? 1 : 3;
+    const int lpt = split ? global : (s->tuneLpt ? (s->laneLanes > 0 ? 1 : global) : 0);
+    *count = base + lpt + (s->laneLanes > 0 ? 1 : 0) + split + 3 + 1;
+    return CSSG_OK;
+}
+
 extern "C" int cssg_system_get_state(cssg_system* s, int* face, double* bary, double* vel, double* force)
 {
     if (!s) return cssg_bad_args("cssg_system_get_state");

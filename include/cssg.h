@@ -298,6 +298,9 @@ int cssg_system_screen_audit_status(cssg_system* sys, long long* out_host);
 /* No reference counterpart.  Number of kernels one step() launches (the integrator's fixed sequence).  A step that
  * audits the screen launches the longest-first ordering kernels (0, 1 or 3) + 4 more. */
 int cssg_system_kernels_per_step(cssg_system* sys, int* count);
+/* No reference counterpart.  Kernels of a step that audits the screen (the same as cssg_system_kernels_per_step
+ * when the audit is off). */
+int cssg_system_kernels_per_audit_step(cssg_system* sys, int* count);
 
 /* ---- diagnostics ------------------------------------------------------------------------------------------------
  * No reference counterpart.  Measured FP64 fused-multiply-add issue rate of the device (GFLOP/s, 2 flops per FMA),

@@ -73,6 +73,7 @@ def test_null_handles_are_argument_errors_without_gpu():
         "cssg_system_source_costs": (N, 0, N),
         "cssg_system_set_pass_groups": (N, 0, 0),
         "cssg_system_pass_groups": (N, N, N),
+        "cssg_system_kernels_per_audit_step": (N, N),
         "cssg_system_set_work_caps": (N, 0, 0, 0),
         "cssg_system_set_screen_audit": (N, 0),
         "cssg_system_screen_audit_status": (N, N),
